@@ -1,0 +1,246 @@
+/*
+ * itg.h — C ABI of libitg.so, a GB300 (sm_103a) dense FP64 tensor backend for
+ * two-site DMRG.
+ *
+ * The reference (ITensorsGPU.jl) has no C boundary: it plugs into ITensors.jl by
+ * adding Julia methods for `CuDense` / `CuDiag` storage (src/ITensorsGPU.jl:32-43).
+ * Each entry point below is the device-side body of one of those methods; the
+ * Julia `ccall` glue and the Python ctypes mirror call these functions with plain
+ * device pointers.  Comments name the reference method each one replaces.
+ *
+ * Conventions
+ *  - Every function returns an int status (ITG_OK = 0).  No C++ exception crosses
+ *    this boundary.  itg_last_error(h) gives a message for the last failure.
+ *  - Tensors are dense, column-major (first index fastest), exactly like the flat
+ *    `Dense` storage of NDTensors (src/tensor/cudense.jl:19).  Dimensions are
+ *    int64, mode labels are int32.
+ *  - All device work is enqueued on the handle's stream and is asynchronous,
+ *    except where an output is documented as a host scalar.
+ *  - A handle is not thread-safe; use one per host thread.
+ *  - The library never frees caller memory.  Memory the library needs beyond the
+ *    caller's inputs and outputs (index tables, Jacobi scratch, reductions) comes
+ *    from a per-handle workspace that grows on demand and is freed by
+ *    itg_destroy.
+ */
+#ifndef ITG_H
+#define ITG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define ITG_API __attribute__((visibility("default")))
+#else
+#define ITG_API
+#endif
+
+typedef struct itg_handle itg_handle;
+
+enum {
+  ITG_OK = 0,
+  ITG_ERR_INVALID = 1,      /* bad argument (null pointer, bad enum)            */
+  ITG_ERR_SHAPE = 2,        /* DimensionMismatch in the reference               */
+  ITG_ERR_ALLOC = 3,        /* device allocation failed                         */
+  ITG_ERR_CUDA = 4,         /* a CUDA runtime call failed                       */
+  ITG_ERR_TIMEOUT = 5,      /* a bounded device-side wait ran out               */
+  ITG_ERR_NOTCONVERGED = 6, /* an iterative solver hit its sweep limit          */
+  ITG_ERR_UNSUPPORTED = 7   /* valid request the library does not implement     */
+};
+
+enum { ITG_F64 = 0 };
+
+/* Arithmetic used by itg_contract.
+ *  ITG_PREC_FP64  : native FP64 FMA; relative Frobenius error ~ K * 2^-53.
+ *  ITG_PREC_SPLIT : FP64 operands split into bf16 integer slices, products on
+ *                   the tcgen05 tensor cores with exact FP32 partial sums and an
+ *                   exact integer recombination; error bound stated per call by
+ *                   itg_split_error_bound. */
+enum { ITG_PREC_FP64 = 0, ITG_PREC_SPLIT = 1 };
+
+/* ---------------------------------------------------------------- handle */
+/* No reference counterpart: CUDA.jl owns the context and default stream. */
+ITG_API int itg_create(int device, itg_handle** out);
+ITG_API int itg_destroy(itg_handle* h);
+/* stream is a cudaStream_t (NULL = legacy default stream). */
+ITG_API int itg_set_stream(itg_handle* h, void* stream);
+ITG_API int itg_get_stream(itg_handle* h, void** stream);
+ITG_API int itg_synchronize(itg_handle* h);
+ITG_API const char* itg_last_error(itg_handle* h);
+ITG_API const char* itg_status_string(int status);
+/* Library version as major*10000 + minor*100 + patch. */
+ITG_API int itg_version(void);
+
+/* ---------------------------------------------------------------- memory */
+/* Replace CuVector allocation and the H2D/D2H copies of
+ * src/tensor/cudense.jl:4-13 (Dense{T,CuArray}(::Dense{T,Array}), cpu(x)). */
+ITG_API int itg_malloc(itg_handle* h, void** ptr, size_t bytes);
+ITG_API int itg_free(itg_handle* h, void* ptr);
+ITG_API int itg_memcpy_h2d(itg_handle* h, void* dst, const void* src, size_t bytes);
+ITG_API int itg_memcpy_d2h(itg_handle* h, void* dst, const void* src, size_t bytes);
+ITG_API int itg_memcpy_d2d(itg_handle* h, void* dst, const void* src, size_t bytes);
+ITG_API int itg_memset_zero(itg_handle* h, void* ptr, size_t bytes);
+
+/* ---------------------------------------------------------- contraction */
+/* C = alpha * A * B + beta * C over the modes A and B share.
+ * Replaces contract!! (src/tensor/cudense.jl:83-110), _contract!
+ * (src/tensor/cudense.jl:238-331) and _gemm_contract! (src/tensor/cudense.jl:170-236).
+ * Modes that appear in A and B but not C are summed; every mode of C appears in
+ * exactly one of A, B.  Ranks 0..16.  rank 0 tensors are scalars (one element).
+ * A mode shared by A, B and C (a batch mode) is ITG_ERR_UNSUPPORTED, as the
+ * reference's label construction (cudense.jl:255-283) never produces one.
+ * C must not alias A or B. */
+ITG_API int itg_contract(itg_handle* h, int dtype, double alpha,
+                 const void* A, int rankA, const int64_t* dimsA, const int32_t* modesA,
+                 const void* B, int rankB, const int64_t* dimsB, const int32_t* modesB,
+                 double beta,
+                 void* C, int rankC, const int64_t* dimsC, const int32_t* modesC,
+                 int precision);
+
+/* Bound on |C_split - C_exact|_F / (|A|_F |B|_F) for ITG_PREC_SPLIT with the
+ * library's slice count at contraction depth K (host-only arithmetic). */
+ITG_API double itg_split_error_bound(int64_t K);
+
+/* ----------------------------------------------------------- permutation */
+/* B = alpha * A, with B's modes a permutation of A's.
+ * Replaces permute! (src/tensor/cudense.jl:447-500) and permutedims!!
+ * (src/tensor/cudense.jl:38-60,112-127).  Ranks 0..16. B must not alias A. */
+ITG_API int itg_permute(itg_handle* h, int dtype, double alpha,
+                const void* A, int rank, const int64_t* dimsA, const int32_t* modesA,
+                void* B, const int32_t* modesB);
+
+/* C = alpha * permute(A -> modesB) + beta * B, with C laid out like B.
+ * C may alias B (in place update).  Replaces Base.:+ / Base.:- on CuDense
+ * (src/tensor/cudense.jl:333-445), which go through cuTENSOR elementwiseBinary!
+ * into a fresh buffer and a copy back. */
+ITG_API int itg_axpby_permuted(itg_handle* h, int dtype, double alpha,
+                       const void* A, int rank, const int64_t* dimsA, const int32_t* modesA,
+                       double beta, const void* B, const int32_t* modesB, void* C);
+
+/* ------------------------------------------------------------- diagonal */
+/* Contraction of a diagonal tensor D (all its modes share one diagonal index
+ * of length dims[0]; `uniform` = 1 means D has one stored value d[0]) with a
+ * dense tensor T.  C = alpha * D * T + beta * C.
+ * Replaces contract! for (Uniform|Nonuniform)Diag x CuDense
+ * (src/tensor/cudiag.jl:105-118,147-161), which densifies the diagonal, and
+ * respects the index permutation that cudiag.jl:105-112 ignores. */
+ITG_API int itg_diag_contract(itg_handle* h, int dtype, double alpha,
+                      const double* d, int uniform, int rankD, const int64_t* dimsD, const int32_t* modesD,
+                      const void* T, int rankT, const int64_t* dimsT, const int32_t* modesT,
+                      double beta,
+                      void* C, int rankC, const int64_t* dimsC, const int32_t* modesC);
+
+/* Diag x Diag: c[i] = alpha * a[i or 0] * b[i or 0] (elementwise product of the
+ * stored diagonals).  Replaces src/tensor/cudiag.jl:120-145. */
+ITG_API int itg_diag_diag(itg_handle* h, int64_t n, double alpha,
+                  const double* a, int a_uniform, const double* b, int b_uniform, double* c);
+
+/* Scatter a diagonal into a dense tensor with all modes of length dims[0]
+ * (dense(::NonuniformCuDiagTensor), src/tensor/cudiag.jl:8-13). */
+ITG_API int itg_diag_to_dense(itg_handle* h, const double* d, int uniform, int rank,
+                      const int64_t* dims, double* T);
+
+/* ------------------------------------------------------- vector kernels */
+/* FP64 level-1 operations on flat storage (norm, scalar *, /, axpy used by the
+ * eigensolver: src/tensor/cudense.jl:22-27,502).  Reductions are
+ * deterministic (fixed grid and tree order).  dot/nrm2 write a host double and
+ * synchronise the stream; the _dev variants write a device double and do not. */
+ITG_API int itg_scal(itg_handle* h, int64_t n, double alpha, double* x);
+ITG_API int itg_axpy(itg_handle* h, int64_t n, double alpha, const double* x, double* y);
+ITG_API int itg_axpby(itg_handle* h, int64_t n, double alpha, const double* x, double beta, double* y);
+ITG_API int itg_fill(itg_handle* h, int64_t n, double value, double* x);
+ITG_API int itg_dot(itg_handle* h, int64_t n, const double* x, const double* y, double* result);
+ITG_API int itg_nrm2(itg_handle* h, int64_t n, const double* x, double* result);
+ITG_API int itg_dot_dev(itg_handle* h, int64_t n, const double* x, const double* y, double* result_dev);
+/* out[j] = sum_i X[i + j*ldx] * y[i] for j < k (X^T y, k small); device output. */
+ITG_API int itg_gemv_t(itg_handle* h, int64_t n, int64_t k, const double* X, int64_t ldx,
+               const double* y, double* out_dev);
+/* y = beta*y + sum_j X[:, j] * c[j] (c is a device vector of length k). */
+ITG_API int itg_gemv_n(itg_handle* h, int64_t n, int64_t k, const double* X, int64_t ldx,
+               const double* c_dev, double beta, double* y);
+
+/* Standard normal FP64 numbers from a counter-based Philox-4x32-10 generator
+ * (Salmon et al., SC'11) followed by Box-Muller.  Element i depends only on
+ * (seed, i), so the CPU restatement produces the same numbers.  Replaces the
+ * CURAND randn! of src/cuitensor.jl:35-49 and src/mps/cumps.jl:44-53. */
+ITG_API int itg_random_normal(itg_handle* h, int64_t n, uint64_t seed, uint64_t offset, double* x);
+
+/* ------------------------------------------------------------ truncation */
+/* Truncate a descending spectrum P (device, length n) and report how many
+ * values to keep.  legacy_gpu = 1 restates src/tensor/cutruncate.jl:1-93
+ * exactly (its per-element threshold rule); legacy_gpu = 0 is ITensors' CPU
+ * rule (cumulative discarded weight <= cutoff * sum(P), then maxdim / mindim).
+ * Host outputs; synchronises the stream.  maxdim <= 0 means no limit. */
+ITG_API int itg_truncate(itg_handle* h, const double* P, int64_t n,
+                 int64_t maxdim, int64_t mindim, double cutoff,
+                 int absoluteCutoff, int doRelCutoff, int legacy_gpu,
+                 int64_t* n_keep, double* truncerr, double* docut);
+
+/* ---------------------------------------------------------- factorisation */
+/* Truncated SVD of the m x n column-major matrix A (lda >= m): A ~ U diag(S) V^T
+ * with S descending.  One-sided blocked Jacobi in FP64.  U must hold m*min(m,n)
+ * doubles (ldu = m), V n*min(m,n) (ldv = n), S min(m,n).  On return the first k
+ * columns hold the kept factors.  A is not modified.  Host outputs k, truncerr,
+ * docut; synchronises.  Replaces LinearAlgebra.svd(::CuDenseTensor)
+ * (src/tensor/culinearalgebra.jl:33-72) + truncate! (src/tensor/cutruncate.jl). */
+ITG_API int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
+                  int64_t maxdim, int64_t mindim, double cutoff,
+                  int absoluteCutoff, int doRelCutoff, int legacy_gpu,
+                  double* U, double* S, double* V,
+                  int64_t* k, double* truncerr, double* docut);
+
+/* Eigendecomposition of the symmetric n x n matrix A: A = U diag(D) U^T with D
+ * descending, then truncation of D as a spectrum.  U holds n*n doubles.
+ * Replaces eigen(::Hermitian{CuDenseTensor}) (src/tensor/culinearalgebra.jl:74-108). */
+ITG_API int itg_eigh_trunc(itg_handle* h, int64_t n, const double* A, int64_t lda,
+                   int64_t maxdim, int64_t mindim, double cutoff,
+                   int absoluteCutoff, int doRelCutoff, int legacy_gpu,
+                   double* D, double* U, int64_t* k, double* truncerr, double* docut);
+
+/* Thin QR of the m x n matrix A: A = Q R, Q m x r, R r x n, r = min(m,n).
+ * Replaces qr(::CuDenseTensor) (src/tensor/culinearalgebra.jl:110-121). */
+ITG_API int itg_qr(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
+           double* Q, double* R);
+
+/* Plain matrix product C = A * B of column-major matrices
+ * (Base.:* for order-2 tensors, src/tensor/culinearalgebra.jl:9-17). */
+ITG_API int itg_matmul(itg_handle* h, int64_t m, int64_t n, int64_t k,
+               const double* A, const double* B, double* C, int precision);
+
+/* ------------------------------------------------- two-site DMRG kernels */
+/* Effective Hamiltonian of two-site DMRG applied to psi:
+ *   out[a', s1', s2', b'] = sum L[a, w, a'] W1[w, s1', s1, x] W2[x, s2', s2, y]
+ *                               R[b, y, b'] psi[a, s1, s2, b]
+ * L is (chiL, wL, chiL), W1 (wL, d, d, wM), W2 (wM, d, d, wR), R (chiR, wR, chiR),
+ * psi and out (chiL, d, d, chiR), all column-major.  This is the ProjMPO product
+ * ITensors' dmrg evaluates inside its eigensolver through four ITensor `*` calls
+ * (each one contract!!, src/tensor/cudense.jl:83-110).  The call is a fixed chain
+ * of four gather-GEMM contractions through workspace; with precision
+ * ITG_PREC_SPLIT the two chi^3 steps run on the tensor cores. */
+ITG_API int itg_heff2_apply(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d,
+                    int64_t wL, int64_t wM, int64_t wR,
+                    const double* L, const double* W1, const double* W2, const double* R,
+                    const double* psi, double* out, int precision);
+
+/* Lowest eigenpair of the two-site effective Hamiltonian by Davidson with the
+ * diagonal preconditioner.  psi (device) is the start vector and is overwritten
+ * with the normalised eigenvector; energy (host) receives the eigenvalue.
+ * krylovdim = largest subspace before restart, maxiter = restarts, tol =
+ * residual-norm tolerance.  nmatvec (host, may be NULL) receives the number of
+ * H_eff applications.  This stands in for the eigensolver that ITensors' dmrg
+ * calls (KrylovKit eigsolve / ITensors davidson, exercised by
+ * test/test_cuiterativesolvers.jl:13-28). */
+ITG_API int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d,
+                       int64_t wL, int64_t wM, int64_t wR,
+                       const double* L, const double* W1, const double* W2, const double* R,
+                       double* psi, int krylovdim, int maxiter, double tol, int precision,
+                       double* energy, int* nmatvec);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ITG_H */

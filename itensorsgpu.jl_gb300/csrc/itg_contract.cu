@@ -1,0 +1,431 @@
+// Pairwise tensor contraction (K1): planner, plan cache and the FP64
+// gather-GEMM kernel.
+//
+// A contraction C = alpha*A*B + beta*C is lowered to one GEMM
+//     C[m, n] = alpha * sum_k A[m, k] * B[k, n] + beta * C[m, n]
+// where m runs over A's free modes (in C's order), n over B's free modes (in
+// C's order) and k over the contracted modes.  No tensor is permuted in memory:
+// every operand is addressed through per-plan offset tables
+//     A[m, k] = A[offAm[m] + offAk[k]],  B[k, n] = B[offBk[k] + offBn[n]],
+//     C[m, n] = C[offCm[m] + offCn[n]],
+// so the TTGT transposes are folded into the tile loads and the epilogue
+// stores.  The scalar (rank 0) and outer-product (K = 1) cases of
+// contract!! (src/tensor/cudense.jl:89-105) are the same GEMM with M, N or K
+// equal to 1.  Plans are cached per (dims, modes) key like the reference's
+// ContractionPlans (src/ITensorsGPU.jl:55, src/tensor/cudense.jl:284-294).
+#include "itg_internal.cuh"
+
+#include <algorithm>
+#include <sstream>
+
+struct ContractPlan {
+  int64_t M = 0, N = 0, K = 0;
+  int64_t* tables = nullptr;  // offAm[M] offCm[M] offBn[N] offCn[N] offAk[K] offBk[K]
+  bool a_kmaj = false, b_kmaj = false;
+  const int64_t* offAm() const { return tables; }
+  const int64_t* offCm() const { return tables + M; }
+  const int64_t* offBn() const { return tables + 2 * M; }
+  const int64_t* offCn() const { return tables + 2 * M + N; }
+  const int64_t* offAk() const { return tables + 2 * M + 2 * N; }
+  const int64_t* offBk() const { return tables + 2 * M + 2 * N + K; }
+  ~ContractPlan() {
+    if (tables) cudaFree(tables);
+  }
+};
+
+void itg_release_plans(itg_handle* h) { h->plans.clear(); }
+
+// ------------------------------------------------------------ FP64 kernel
+namespace {
+
+constexpr int GBM = 128, GBN = 128, GBK = 16, GTHREADS = 256;
+constexpr int SPAD = 4;  // shared-memory row padding (doubles)
+
+template <bool AK, bool BK>
+__global__ void __launch_bounds__(GTHREADS)
+k_gemm_gather_f64(const double* __restrict__ A, const double* __restrict__ B,
+                  double* __restrict__ C, const int64_t* __restrict__ offAm,
+                  const int64_t* __restrict__ offAk, const int64_t* __restrict__ offBk,
+                  const int64_t* __restrict__ offBn, const int64_t* __restrict__ offCm,
+                  const int64_t* __restrict__ offCn, int64_t M, int64_t N, int64_t K,
+                  double alpha, double beta) {
+  extern __shared__ double smem[];
+  double* As = smem;                              // [2][GBK][GBM+SPAD]
+  double* Bs = smem + 2 * GBK * (GBM + SPAD);     // [2][GBK][GBN+SPAD]
+  const int t = threadIdx.x;
+  const int64_t m0 = (int64_t)blockIdx.x * GBM;
+  const int64_t n0 = (int64_t)blockIdx.y * GBN;
+
+  // Load mapping.
+  // AK: kk = t&15, rows mm = (t>>4) + 16r.   !AK: mm = t&127, kk = (t>>7) + 2r.
+  int64_t aRow[8];
+  int64_t bCol[8];
+  if (AK) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      int64_t m = m0 + (t >> 4) + 16 * r;
+      aRow[r] = (m < M) ? offAm[m] : -1;
+    }
+  } else {
+    int64_t m = m0 + (t & 127);
+    aRow[0] = (m < M) ? offAm[m] : -1;
+  }
+  if (BK) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      int64_t n = n0 + (t >> 4) + 16 * r;
+      bCol[r] = (n < N) ? offBn[n] : -1;
+    }
+  } else {
+    int64_t n = n0 + (t & 127);
+    bCol[0] = (n < N) ? offBn[n] : -1;
+  }
+
+  double ra[8], rb[8];
+  auto load_tile = [&](int64_t k0) {
+    if (AK) {
+      int64_t k = k0 + (t & 15);
+      int64_t ok = (k < K) ? offAk[k] : 0;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) ra[r] = (k < K && aRow[r] >= 0) ? A[aRow[r] + ok] : 0.0;
+    } else {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        int64_t k = k0 + (t >> 7) + 2 * r;
+        ra[r] = (k < K && aRow[0] >= 0) ? A[aRow[0] + offAk[k]] : 0.0;
+      }
+    }
+    if (BK) {
+      int64_t k = k0 + (t & 15);
+      int64_t ok = (k < K) ? offBk[k] : 0;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) rb[r] = (k < K && bCol[r] >= 0) ? B[bCol[r] + ok] : 0.0;
+    } else {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        int64_t k = k0 + (t >> 7) + 2 * r;
+        rb[r] = (k < K && bCol[0] >= 0) ? B[offBk[k] + bCol[0]] : 0.0;
+      }
+    }
+  };
+  auto store_tile = [&](int buf) {
+    double* as = As + buf * GBK * (GBM + SPAD);
+    double* bs = Bs + buf * GBK * (GBN + SPAD);
+    if (AK) {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) as[(t & 15) * (GBM + SPAD) + (t >> 4) + 16 * r] = ra[r];
+    } else {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) as[((t >> 7) + 2 * r) * (GBM + SPAD) + (t & 127)] = ra[r];
+    }
+    if (BK) {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) bs[(t & 15) * (GBN + SPAD) + (t >> 4) + 16 * r] = rb[r];
+    } else {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) bs[((t >> 7) + 2 * r) * (GBN + SPAD) + (t & 127)] = rb[r];
+    }
+  };
+
+  const int tx = t & 15, ty = t >> 4;
+  double acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0;
+
+  const int64_t nk = (K + GBK - 1) / GBK;
+  if (nk > 0) {
+    load_tile(0);
+    store_tile(0);
+  }
+  __syncthreads();
+  for (int64_t kt = 0; kt < nk; ++kt) {
+    const int buf = (int)(kt & 1);
+    if (kt + 1 < nk) load_tile((kt + 1) * GBK);
+    const double* as = As + buf * GBK * (GBM + SPAD);
+    const double* bs = Bs + buf * GBK * (GBN + SPAD);
+#pragma unroll 4
+    for (int kk = 0; kk < GBK; ++kk) {
+      double a[8], b[8];
+      const double* ap = as + kk * (GBM + SPAD);
+      const double* bp = bs + kk * (GBN + SPAD);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        a[i] = ap[ty * 4 + i];
+        a[4 + i] = ap[64 + ty * 4 + i];
+        b[i] = bp[tx * 4 + i];
+        b[4 + i] = bp[64 + tx * 4 + i];
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    if (kt + 1 < nk) store_tile(buf ^ 1);
+    __syncthreads();
+  }
+
+  // Epilogue: scatter to C's layout.
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    int64_t m = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+    if (m >= M) continue;
+    int64_t cm = offCm[m];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      int64_t n = n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+      if (n >= N) continue;
+      double* c = C + cm + offCn[n];
+      double v = alpha * acc[i][j];
+      if (beta != 0.0) v = fma(beta, *c, v);
+      *c = v;
+    }
+  }
+}
+
+constexpr size_t GEMM_SMEM = sizeof(double) * 2 * GBK * ((GBM + SPAD) + (GBN + SPAD));
+
+template <bool AK, bool BK>
+int launch_gemm(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
+                double alpha, double beta) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    ITG_CUDA(h, cudaFuncSetAttribute(k_gemm_gather_f64<AK, BK>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM));
+    attr_set = true;
+  }
+  int64_t gx = (p.M + GBM - 1) / GBM, gy = (p.N + GBN - 1) / GBN;
+  if (gy > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "N=%lld too large", (long long)p.N);
+  dim3 grid((unsigned)gx, (unsigned)gy);
+  k_gemm_gather_f64<AK, BK><<<grid, GTHREADS, GEMM_SMEM, h->stream>>>(
+      A, B, C, p.offAm(), p.offAk(), p.offBk(), p.offBn(), p.offCm(), p.offCn(), p.M, p.N, p.K,
+      alpha, beta);
+  ITG_CHECK_LAUNCH(h);
+  return ITG_OK;
+}
+
+__global__ void k_scale_or_zero(int64_t n, double beta, double* __restrict__ C) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    C[i] = (beta == 0.0) ? 0.0 : beta * C[i];
+}
+
+// ------------------------------------------------------------ planning
+struct ModeInfo {
+  int32_t mode;
+  int64_t dim;
+  int64_t strA, strB, strC;  // -1 when absent
+};
+
+int build_plan(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA, int rankB,
+               const int64_t* dimsB, const int32_t* modesB, int rankC, const int64_t* dimsC,
+               const int32_t* modesC, std::shared_ptr<ContractPlan>& out) {
+  auto strides = [](int r, const int64_t* d, int64_t* s) {
+    int64_t x = 1;
+    for (int i = 0; i < r; ++i) { s[i] = x; x *= d[i]; }
+  };
+  int64_t sA[ITG_MAX_RANK], sB[ITG_MAX_RANK], sC[ITG_MAX_RANK];
+  strides(rankA, dimsA, sA);
+  strides(rankB, dimsB, sB);
+  strides(rankC, dimsC, sC);
+  auto find = [](int r, const int32_t* m, int32_t x) {
+    int pos = -1;
+    for (int i = 0; i < r; ++i)
+      if (m[i] == x) pos = (pos < 0) ? i : -2;
+    return pos;
+  };
+  for (int i = 0; i < rankA; ++i)
+    if (find(rankA, modesA, modesA[i]) == -2) return itg_fail(h, ITG_ERR_SHAPE, "repeated mode %d in A", modesA[i]);
+  for (int i = 0; i < rankB; ++i)
+    if (find(rankB, modesB, modesB[i]) == -2) return itg_fail(h, ITG_ERR_SHAPE, "repeated mode %d in B", modesB[i]);
+  for (int i = 0; i < rankC; ++i)
+    if (find(rankC, modesC, modesC[i]) == -2) return itg_fail(h, ITG_ERR_SHAPE, "repeated mode %d in C", modesC[i]);
+
+  std::vector<ModeInfo> freeA, freeB, contr;
+  // C's modes in C order
+  for (int i = 0; i < rankC; ++i) {
+    int ia = find(rankA, modesA, modesC[i]);
+    int ib = find(rankB, modesB, modesC[i]);
+    if (ia >= 0 && ib >= 0)
+      return itg_fail(h, ITG_ERR_UNSUPPORTED, "mode %d appears in A, B and C (batch mode)", modesC[i]);
+    if (ia < 0 && ib < 0) return itg_fail(h, ITG_ERR_SHAPE, "mode %d of C is in neither A nor B", modesC[i]);
+    ModeInfo mi{modesC[i], dimsC[i], -1, -1, sC[i]};
+    if (ia >= 0) {
+      if (dimsA[ia] != dimsC[i]) return itg_fail(h, ITG_ERR_SHAPE, "dimension mismatch for mode %d", modesC[i]);
+      mi.strA = sA[ia];
+      freeA.push_back(mi);
+    } else {
+      if (dimsB[ib] != dimsC[i]) return itg_fail(h, ITG_ERR_SHAPE, "dimension mismatch for mode %d", modesC[i]);
+      mi.strB = sB[ib];
+      freeB.push_back(mi);
+    }
+  }
+  for (int i = 0; i < rankA; ++i) {
+    if (find(rankC, modesC, modesA[i]) >= 0) continue;
+    int ib = find(rankB, modesB, modesA[i]);
+    if (ib < 0) return itg_fail(h, ITG_ERR_UNSUPPORTED, "mode %d of A is in neither B nor C", modesA[i]);
+    if (dimsA[i] != dimsB[ib]) return itg_fail(h, ITG_ERR_SHAPE, "dimension mismatch for contracted mode %d", modesA[i]);
+    contr.push_back({modesA[i], dimsA[i], sA[i], sB[ib], -1});
+  }
+  for (int i = 0; i < rankB; ++i) {
+    if (find(rankC, modesC, modesB[i]) >= 0) continue;
+    if (find(rankA, modesA, modesB[i]) < 0)
+      return itg_fail(h, ITG_ERR_UNSUPPORTED, "mode %d of B is in neither A nor C", modesB[i]);
+  }
+  // K order: A's order unless B's stride-1 mode is contracted and A's is not.
+  bool aFirstContr = rankA > 0 && find(rankC, modesC, modesA[0]) < 0 && dimsA[0] > 1;
+  bool bFirstContr = rankB > 0 && find(rankC, modesC, modesB[0]) < 0 && dimsB[0] > 1;
+  if (!aFirstContr && bFirstContr)
+    std::stable_sort(contr.begin(), contr.end(),
+                     [](const ModeInfo& x, const ModeInfo& y) { return x.strB < y.strB; });
+
+  auto p = std::make_shared<ContractPlan>();
+  auto prod = [](const std::vector<ModeInfo>& v) {
+    int64_t x = 1;
+    for (auto& m : v) x *= m.dim;
+    return x;
+  };
+  p->M = prod(freeA);
+  p->N = prod(freeB);
+  p->K = prod(contr);
+  // Tables.
+  std::vector<int64_t> tab(2 * p->M + 2 * p->N + 2 * p->K);
+  auto fill = [](const std::vector<ModeInfo>& v, int64_t count, int which1, int which2,
+                 int64_t* o1, int64_t* o2) {
+    // which: 0 = strA, 1 = strB, 2 = strC
+    auto st = [](const ModeInfo& m, int w) { return w == 0 ? m.strA : (w == 1 ? m.strB : m.strC); };
+    std::vector<int64_t> idx(v.size(), 0);
+    int64_t a = 0, b = 0;
+    for (int64_t l = 0; l < count; ++l) {
+      o1[l] = a;
+      o2[l] = b;
+      for (size_t i = 0; i < v.size(); ++i) {
+        idx[i]++;
+        a += st(v[i], which1);
+        b += st(v[i], which2);
+        if (idx[i] < v[i].dim) break;
+        a -= st(v[i], which1) * v[i].dim;
+        b -= st(v[i], which2) * v[i].dim;
+        idx[i] = 0;
+      }
+    }
+  };
+  int64_t* t = tab.data();
+  fill(freeA, p->M, 0, 2, t, t + p->M);
+  fill(freeB, p->N, 1, 2, t + 2 * p->M, t + 2 * p->M + p->N);
+  fill(contr, p->K, 0, 1, t + 2 * p->M + 2 * p->N, t + 2 * p->M + 2 * p->N + p->K);
+  p->a_kmaj = p->K > 1 && (t[2 * p->M + 2 * p->N + 1] - t[2 * p->M + 2 * p->N] == 1);
+  p->b_kmaj = p->K > 1 && (t[2 * p->M + 2 * p->N + p->K + 1] - t[2 * p->M + 2 * p->N + p->K] == 1);
+  if (!tab.empty()) {
+    cudaError_t e = cudaMalloc((void**)&p->tables, tab.size() * sizeof(int64_t));
+    if (e != cudaSuccess)
+      return itg_fail(h, ITG_ERR_ALLOC, "plan table allocation failed: %s", cudaGetErrorString(e));
+    ITG_CUDA(h, cudaMemcpy(p->tables, tab.data(), tab.size() * sizeof(int64_t),
+                           cudaMemcpyHostToDevice));
+  }
+  out = p;
+  return ITG_OK;
+}
+
+std::string plan_key(int rankA, const int64_t* dimsA, const int32_t* modesA, int rankB,
+                     const int64_t* dimsB, const int32_t* modesB, int rankC, const int64_t* dimsC,
+                     const int32_t* modesC) {
+  // Canonical labels: number modes by first appearance (C, then A, then B).
+  std::vector<int32_t> seen;
+  auto lab = [&](int32_t m) {
+    for (size_t i = 0; i < seen.size(); ++i)
+      if (seen[i] == m) return (int)i;
+    seen.push_back(m);
+    return (int)seen.size() - 1;
+  };
+  std::ostringstream os;
+  for (int i = 0; i < rankC; ++i) os << lab(modesC[i]) << ',' << dimsC[i] << ',';
+  os << '|';
+  for (int i = 0; i < rankA; ++i) os << lab(modesA[i]) << ',' << dimsA[i] << ',';
+  os << '|';
+  for (int i = 0; i < rankB; ++i) os << lab(modesB[i]) << ',' << dimsB[i] << ',';
+  return os.str();
+}
+
+}  // namespace
+
+int itg_split_gemm(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
+                   double alpha, double beta);  // itg_split.cu
+
+namespace itg {
+
+int get_plan(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA, int rankB,
+             const int64_t* dimsB, const int32_t* modesB, int rankC, const int64_t* dimsC,
+             const int32_t* modesC, std::shared_ptr<ContractPlan>& plan) {
+  std::string key = plan_key(rankA, dimsA, modesA, rankB, dimsB, modesB, rankC, dimsC, modesC);
+  auto it = h->plans.find(key);
+  if (it != h->plans.end()) {
+    plan = it->second;
+    return ITG_OK;
+  }
+  ITG_TRY(build_plan(h, rankA, dimsA, modesA, rankB, dimsB, modesB, rankC, dimsC, modesC, plan));
+  h->plans[key] = plan;
+  return ITG_OK;
+}
+
+int run_plan(itg_handle* h, const ContractPlan& p, double alpha, const double* A, const double* B,
+             double beta, double* C, int precision) {
+  if (p.M == 0 || p.N == 0) return ITG_OK;
+  if (p.K == 0) {
+    int64_t n = p.M * p.N;  // C is dense with exactly M*N elements
+    k_scale_or_zero<<<itg_blocks_for(n, 256, h->num_sms * 8), 256, 0, h->stream>>>(n, beta, C);
+    ITG_CHECK_LAUNCH(h);
+    return ITG_OK;
+  }
+  if (precision == ITG_PREC_SPLIT) return itg_split_gemm(h, p, A, B, C, alpha, beta);
+  if (p.a_kmaj && p.b_kmaj) return launch_gemm<true, true>(h, p, A, B, C, alpha, beta);
+  if (p.a_kmaj) return launch_gemm<true, false>(h, p, A, B, C, alpha, beta);
+  if (p.b_kmaj) return launch_gemm<false, true>(h, p, A, B, C, alpha, beta);
+  return launch_gemm<false, false>(h, p, A, B, C, alpha, beta);
+}
+
+int contract_f64(itg_handle* h, double alpha, const double* A, int rankA, const int64_t* dimsA,
+                 const int32_t* modesA, const double* B, int rankB, const int64_t* dimsB,
+                 const int32_t* modesB, double beta, double* C, int rankC, const int64_t* dimsC,
+                 const int32_t* modesC, int precision) {
+  std::shared_ptr<ContractPlan> plan;
+  ITG_TRY(get_plan(h, rankA, dimsA, modesA, rankB, dimsB, modesB, rankC, dimsC, modesC, plan));
+  return run_plan(h, *plan, alpha, A, B, beta, C, precision);
+}
+
+}  // namespace itg
+
+extern "C" int itg_contract(itg_handle* h, int dtype, double alpha, const void* A, int rankA,
+                            const int64_t* dimsA, const int32_t* modesA, const void* B, int rankB,
+                            const int64_t* dimsB, const int32_t* modesB, double beta, void* C,
+                            int rankC, const int64_t* dimsC, const int32_t* modesC, int precision) {
+  if (!h) return ITG_ERR_INVALID;
+  if (dtype != ITG_F64) return itg_fail(h, ITG_ERR_UNSUPPORTED, "dtype %d not supported", dtype);
+  if (precision != ITG_PREC_FP64 && precision != ITG_PREC_SPLIT)
+    return itg_fail(h, ITG_ERR_INVALID, "unknown precision %d", precision);
+  if (rankA < 0 || rankB < 0 || rankC < 0 || rankA > ITG_MAX_RANK || rankB > ITG_MAX_RANK ||
+      rankC > ITG_MAX_RANK)
+    return itg_fail(h, ITG_ERR_UNSUPPORTED, "rank outside 0..%d", ITG_MAX_RANK);
+  if ((rankA && (!dimsA || !modesA)) || (rankB && (!dimsB || !modesB)) ||
+      (rankC && (!dimsC || !modesC)))
+    return itg_fail(h, ITG_ERR_INVALID, "null dims/modes");
+  if (!A || !B || !C) return itg_fail(h, ITG_ERR_INVALID, "null tensor pointer");
+  if (C == A || C == B) return itg_fail(h, ITG_ERR_INVALID, "C must not alias A or B");
+  for (int i = 0; i < rankA; ++i)
+    if (dimsA[i] < 0) return itg_fail(h, ITG_ERR_SHAPE, "negative dimension");
+  for (int i = 0; i < rankB; ++i)
+    if (dimsB[i] < 0) return itg_fail(h, ITG_ERR_SHAPE, "negative dimension");
+  for (int i = 0; i < rankC; ++i)
+    if (dimsC[i] < 0) return itg_fail(h, ITG_ERR_SHAPE, "negative dimension");
+  return itg::contract_f64(h, alpha, (const double*)A, rankA, dimsA, modesA, (const double*)B, rankB,
+                           dimsB, modesB, beta, (double*)C, rankC, dimsC, modesC, precision);
+}
+
+extern "C" int itg_matmul(itg_handle* h, int64_t m, int64_t n, int64_t k, const double* A,
+                          const double* B, double* C, int precision) {
+  if (!h) return ITG_ERR_INVALID;
+  int64_t dA[2] = {m, k}, dB[2] = {k, n}, dC[2] = {m, n};
+  int32_t mA[2] = {0, 2}, mB[2] = {2, 1}, mC[2] = {0, 1};
+  return itg_contract(h, ITG_F64, 1.0, A, 2, dA, mA, B, 2, dB, mB, 0.0, C, 2, dC, mC, precision);
+}

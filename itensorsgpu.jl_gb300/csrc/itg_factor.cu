@@ -1,0 +1,612 @@
+// Factorisations: on-device truncation (K6), one-sided Jacobi SVD (K5),
+// symmetric eigendecomposition through the shifted SVD, and CGS2 thin QR (K7).
+#include "itg_internal.cuh"
+
+#include <cmath>
+
+// ============================================================== truncation
+// One thread walks the spectrum in the same sequential order as the CPU
+// rules it restates, so both give bit-identical sums.  n <= 2*chi is a few
+// thousand values: tens of microseconds, once per bond.
+__global__ void k_truncate(const double* __restrict__ P, int64_t n, int64_t maxdim,
+                           int64_t mindim, double cutoff, int absoluteCutoff, int doRelCutoff,
+                           int legacy, double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int64_t origm = n;
+  double truncerr = 0.0, docut = 0.0;
+  int64_t keep = 1;
+  if (origm == 0) {
+    out[0] = 0; out[1] = 0; out[2] = 0;
+    return;
+  }
+  if (maxdim <= 0 || maxdim > origm) maxdim = origm;
+  if (!legacy) {
+    // ITensors (NDTensors) CPU rule: cumulative discarded weight.
+    if (origm == 1) {
+      out[0] = 1; out[1] = 0.0; out[2] = fabs(P[0]) / 2;
+      return;
+    }
+    const double sgn = (P[0] < 0.0) ? -1.0 : 1.0;
+    // trailing negative weights count as zero
+    int64_t lastpos = origm;  // values at index >= lastpos are treated as 0
+    for (int64_t i = origm - 1; i >= 0; --i) {
+      if (sgn * P[i] >= 0.0) break;
+      lastpos = i;
+    }
+#define PV(i) ((i) >= lastpos ? 0.0 : sgn * P[(i)])
+    if (mindim < 1) mindim = 1;
+    int64_t nn = origm;
+    while (nn > maxdim) { truncerr += PV(nn - 1); nn--; }
+    if (absoluteCutoff) {
+      while (PV(nn - 1) <= cutoff && nn > mindim) { truncerr += PV(nn - 1); nn--; }
+    } else {
+      double scale = 1.0;
+      if (doRelCutoff) {
+        scale = 0.0;
+        for (int64_t i = 0; i < origm; ++i) scale += PV(i);
+        if (scale == 0.0) scale = 1.0;
+      }
+      const double thr = __dmul_rn(cutoff, scale);
+      while ((__dadd_rn(truncerr, PV(nn - 1)) <= thr) && nn > mindim) {
+        truncerr += PV(nn - 1);
+        nn--;
+      }
+      truncerr /= scale;
+    }
+    if (nn < 1) nn = 1;
+    if (nn < origm) {
+      docut = (PV(nn - 1) + PV(nn)) / 2;
+      if (fabs(PV(nn - 1) - PV(nn)) < __dmul_rn(1e-3, PV(nn - 1)))
+        docut = __dadd_rn(docut, __dmul_rn(1e-3, PV(nn - 1)));
+    }
+#undef PV
+    keep = nn;
+  } else {
+    // src/tensor/cutruncate.jl:1-93, step by step.
+    if (mindim < 1) mindim = 1;
+    if (mindim > maxdim) mindim = maxdim;
+    double maxP = P[0];
+    for (int64_t i = 1; i < origm; ++i) maxP = fmax(maxP, P[i]);
+    if (maxP == 0.0) {
+      out[0] = 1; out[1] = 0.0; out[2] = 0.0;
+      return;
+    }
+    if (origm == 1) {
+      out[0] = 1; out[1] = 0.0; out[2] = maxP / 2;
+      return;
+    }
+#define RP(i) (signbit(P[(i)]) ? 0.0 : P[(i)])
+    int64_t nn = origm;
+    if (nn > maxdim) {
+      for (int64_t i = 0; i < nn - maxdim; ++i) truncerr += RP(i);  // head sum, as written
+      nn = maxdim;
+    }
+    // cut_ind: first index whose value is strictly below the threshold
+    // (cuBLAS iamax over the +-2/0 flag vector), 0 when there is none.
+    int64_t cut_ind = 0;
+    if (absoluteCutoff) {
+      for (int64_t i = 0; i < origm; ++i)
+        if (RP(i) - cutoff < 0.0) { cut_ind = i; break; }
+      nn = min(maxdim, origm - cut_ind);
+      nn = max(nn, mindim);
+      for (int64_t i = cut_ind; i < origm; ++i) truncerr += RP(i);
+    } else {
+      double scale = 1.0;
+      if (doRelCutoff) {
+        scale = 0.0;
+        for (int64_t i = 0; i < origm; ++i) scale += P[i];
+        scale = scale > 0.0 ? scale : 1.0;
+      }
+      for (int64_t i = 0; i < origm; ++i)
+        if (__dsub_rn(__dadd_rn(RP(i), truncerr), __dmul_rn(cutoff, scale)) < 0.0) { cut_ind = i; break; }
+      if (cut_ind > 0) {
+        for (int64_t i = cut_ind; i < origm; ++i) truncerr += RP(i);
+      } else {
+        for (int64_t i = 0; i < maxdim; ++i) truncerr += RP(i);
+      }
+      nn = min(maxdim, origm - cut_ind);
+      nn = max(nn, mindim);
+      truncerr = (scale == 0.0) ? 0.0 : truncerr / scale;
+    }
+#undef RP
+    if (nn < 1) nn = 1;
+    if (nn < origm) {
+      docut = (P[nn - 1] + P[nn]) / 2;
+      if (fabs(P[nn - 1] - P[nn]) < __dmul_rn(1e-3, P[nn - 1]))
+        docut = __dadd_rn(docut, __dmul_rn(1e-3, P[nn - 1]));
+    }
+    keep = nn;
+  }
+  out[0] = (double)keep;
+  out[1] = truncerr;
+  out[2] = docut;
+}
+
+namespace itg {
+int truncate_dev(itg_handle* h, const double* P, int64_t n, int64_t maxdim, int64_t mindim,
+                 double cutoff, int absoluteCutoff, int doRelCutoff, int legacy_gpu, double* out3) {
+  k_truncate<<<1, 32, 0, h->stream>>>(P, n, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff,
+                                      legacy_gpu, out3);
+  ITG_CHECK_LAUNCH(h);
+  return ITG_OK;
+}
+}  // namespace itg
+
+static int read_out3(itg_handle* h, const double* out3, int64_t* n_keep, double* truncerr,
+                     double* docut) {
+  ITG_CUDA(h, cudaMemcpyAsync(h->pinned, out3, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (n_keep) *n_keep = (int64_t)h->pinned[0];
+  if (truncerr) *truncerr = h->pinned[1];
+  if (docut) *docut = h->pinned[2];
+  return ITG_OK;
+}
+
+extern "C" int itg_truncate(itg_handle* h, const double* P, int64_t n, int64_t maxdim,
+                            int64_t mindim, double cutoff, int absoluteCutoff, int doRelCutoff,
+                            int legacy_gpu, int64_t* n_keep, double* truncerr, double* docut) {
+  if (!h || n < 0 || (n > 0 && !P)) return ITG_ERR_INVALID;
+  ITG_TRY(itg_scratch_reserve(h, 4 * sizeof(double)));
+  double* out3 = (double*)h->scratch;
+  if (n == 0) {
+    if (n_keep) *n_keep = 0;
+    if (truncerr) *truncerr = 0;
+    if (docut) *docut = 0;
+    return ITG_OK;
+  }
+  ITG_TRY(itg::truncate_dev(h, P, n, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, out3));
+  return read_out3(h, out3, n_keep, truncerr, docut);
+}
+
+// ============================================================ Jacobi SVD
+// One-sided Jacobi (Hestenes 1958; Demmel & Veselic 1992) on the columns of the
+// m x n working matrix W (m >= n), accumulating the rotations in V (n x n).
+// Pairs follow the round-robin ("circle") ordering of Brent & Luk, so each of
+// the n'-1 steps of a sweep rotates n'/2 disjoint column pairs in parallel
+// (n' = n rounded up to even; the extra slot is a bye).
+//
+// Rotation for the pair (p, q) with a = |w_p|^2, b = |w_q|^2, g = w_p.w_q:
+//   zeta = (b - a) / (2g), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)),
+//   c = 1/sqrt(1 + t^2), s = c t;  w_p <- c w_p - s w_q,  w_q <- s w_p + c w_q.
+// A pair is skipped when |g| <= tol * sqrt(a b).
+
+__device__ __forceinline__ int rr_player(int pos, int step, int np) {
+  if (pos == 0) return 0;
+  return ((pos - 1 + step) % (np - 1)) + 1;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ bool jacobi_rotation(double a, double b, double g, double tol,
+                                                double& c, double& s) {
+  if (a == 0.0 || b == 0.0) return false;
+  if (fabs(g) <= tol * sqrt(a) * sqrt(b)) return false;
+  double zeta = (b - a) / (2.0 * g);
+  double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+  c = 1.0 / sqrt(1.0 + t * t);
+  s = c * t;
+  return true;
+}
+
+// Small problems: the whole sweep loop in one CTA; warps take pairs.
+__global__ void __launch_bounds__(1024)
+k_jacobi_onecta(double* __restrict__ W, int64_t m, int n, double* __restrict__ V, double tol,
+                int max_sweeps, int* __restrict__ sweeps_out) {
+  __shared__ int rotated;
+  const int np = n + (n & 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (threadIdx.x == 0) rotated = 0;
+    __syncthreads();
+    for (int step = 0; step < np - 1; ++step) {
+      for (int pi = warp; pi < np / 2; pi += nw) {
+        int p = rr_player(pi, step, np), q = rr_player(np - 1 - pi, step, np);
+        if (p >= n || q >= n) continue;
+        if (p > q) { int t = p; p = q; q = t; }
+        double* wp = W + (int64_t)p * m;
+        double* wq = W + (int64_t)q * m;
+        double a = 0, b = 0, g = 0;
+        for (int64_t i = lane; i < m; i += 32) {
+          double x = wp[i], y = wq[i];
+          a = fma(x, x, a);
+          b = fma(y, y, b);
+          g = fma(x, y, g);
+        }
+        a = warp_sum(a); b = warp_sum(b); g = warp_sum(g);
+        double c, s;
+        if (jacobi_rotation(a, b, g, tol, c, s)) {
+          for (int64_t i = lane; i < m; i += 32) {
+            double x = wp[i], y = wq[i];
+            wp[i] = c * x - s * y;
+            wq[i] = s * x + c * y;
+          }
+          double* vp = V + (int64_t)p * n;
+          double* vq = V + (int64_t)q * n;
+          for (int i = lane; i < n; i += 32) {
+            double x = vp[i], y = vq[i];
+            vp[i] = c * x - s * y;
+            vq[i] = s * x + c * y;
+          }
+          if (lane == 0) rotated = 1;
+        }
+      }
+      __syncthreads();
+    }
+    int r = rotated;
+    __syncthreads();
+    if (!r) break;
+  }
+  if (threadIdx.x == 0) *sweeps_out = sweep;
+}
+
+// Large problems: one launch per round-robin step, one CTA per pair.
+__global__ void __launch_bounds__(256)
+k_jacobi_step(double* __restrict__ W, int64_t m, int n, double* __restrict__ V, double tol,
+              int step, int* __restrict__ rotated) {
+  __shared__ double sh[3][8];
+  const int np = n + (n & 1);
+  const int pi = blockIdx.x;
+  int p = rr_player(pi, step, np), q = rr_player(np - 1 - pi, step, np);
+  if (p >= n || q >= n) return;
+  if (p > q) { int t = p; p = q; q = t; }
+  double* wp = W + (int64_t)p * m;
+  double* wq = W + (int64_t)q * m;
+  double a = 0, b = 0, g = 0;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+    double x = wp[i], y = wq[i];
+    a = fma(x, x, a);
+    b = fma(y, y, b);
+    g = fma(x, y, g);
+  }
+  a = warp_sum(a); b = warp_sum(b); g = warp_sum(g);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { sh[0][warp] = a; sh[1][warp] = b; sh[2][warp] = g; }
+  __syncthreads();
+  a = 0; b = 0; g = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a += sh[0][w]; b += sh[1][w]; g += sh[2][w]; }
+  double c, s;
+  if (!jacobi_rotation(a, b, g, tol, c, s)) return;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+    double x = wp[i], y = wq[i];
+    wp[i] = c * x - s * y;
+    wq[i] = s * x + c * y;
+  }
+  double* vp = V + (int64_t)p * n;
+  double* vq = V + (int64_t)q * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double x = vp[i], y = vq[i];
+    vp[i] = c * x - s * y;
+    vq[i] = s * x + c * y;
+  }
+  if (threadIdx.x == 0) *rotated = 1;
+}
+
+__global__ void k_identity(int n, double* __restrict__ V) {
+  int64_t nn = (int64_t)n * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn;
+       i += (int64_t)gridDim.x * blockDim.x)
+    V[i] = (i % (n + 1) == 0) ? 1.0 : 0.0;
+}
+
+__global__ void k_col_norms(const double* __restrict__ W, int64_t m, double* __restrict__ sig) {
+  __shared__ double sh[32];
+  const double* w = W + (int64_t)blockIdx.x * m;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) s = fma(w[i], w[i], s);
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh[i];
+    sig[blockIdx.x] = sqrt(t);
+  }
+}
+
+// Stable descending rank of each value (ties by index): order[rank] = j.
+__global__ void k_rank_desc(const double* __restrict__ sig, int n, double shift,
+                            int* __restrict__ order, double* __restrict__ S,
+                            double* __restrict__ P, int square) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    double v = sig[j];
+    int r = 0;
+    for (int i = 0; i < n; ++i) {
+      double u = sig[i];
+      r += (u > v) || (u == v && i < j);
+    }
+    order[r] = j;
+    double sv = v - shift;
+    S[r] = sv;
+    P[r] = square ? sv * sv : sv;
+  }
+}
+
+// out[:, r] = src[:, order[r]] * (scale_by_inv_sig ? 1/sig : 1) for r < ncols.
+__global__ void k_gather_cols(const double* __restrict__ src, int64_t rows, const int* __restrict__ order,
+                              const double* __restrict__ sig, int inv_scale, int ncols,
+                              double* __restrict__ dst, int64_t ldd) {
+  const int r = blockIdx.y;
+  if (r >= ncols) return;
+  const int j = order[r];
+  double f = 1.0;
+  if (inv_scale) {
+    double sv = sig[j];
+    f = (sv > 0.0) ? 1.0 / sv : 0.0;
+  }
+  const double* s = src + (int64_t)j * rows;
+  double* d = dst + (int64_t)r * ldd;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
+       i += (int64_t)gridDim.x * blockDim.x)
+    d[i] = s[i] * f;
+}
+
+__global__ void k_copy_matrix(const double* __restrict__ A, int64_t lda, int64_t m, int64_t n,
+                              double* __restrict__ W, double diag_shift) {
+  const int64_t total = m * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t j = t / m, i = t - j * m;
+    double v = A[i + j * lda];
+    if (i == j) v += diag_shift;
+    W[t] = v;
+  }
+}
+
+// Row-sum bound of |A| (Gershgorin) for the eigen shift.
+__global__ void k_gershgorin(const double* __restrict__ A, int64_t lda, int64_t n, double* out) {
+  __shared__ double sh[32];
+  double best = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    double s = 0.0;
+    for (int64_t j = 0; j < n; ++j) s += fabs(A[i + j * lda]);
+    best = fmax(best, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = best;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) b = fmax(b, sh[i]);
+    *out = b;
+  }
+}
+
+namespace {
+
+constexpr int JACOBI_MAX_SWEEPS = 60;
+constexpr int64_t ONECTA_MAX_N = 192;
+
+// Runs Jacobi on W (m x n, m >= n) with V = I.  Returns ITG_ERR_NOTCONVERGED
+// (results still usable) when the sweep limit is hit.
+int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* flag_dev,
+               int* sweeps_done) {
+  k_identity<<<itg_blocks_for(n * n, 256, h->num_sms * 8), 256, 0, h->stream>>>((int)n, V);
+  ITG_CHECK_LAUNCH(h);
+  const double tol = 2.220446049250313e-16 * sqrt((double)m);
+  if (n <= 1) { *sweeps_done = 0; return ITG_OK; }
+  if (n <= ONECTA_MAX_N) {
+    k_jacobi_onecta<<<1, 1024, 0, h->stream>>>(W, m, (int)n, V, tol, JACOBI_MAX_SWEEPS, flag_dev);
+    ITG_CHECK_LAUNCH(h);
+    int* hp = (int*)h->pinned;
+    ITG_CUDA(h, cudaMemcpyAsync(hp, flag_dev, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    *sweeps_done = hp[0];
+    return hp[0] >= JACOBI_MAX_SWEEPS ? ITG_ERR_NOTCONVERGED : ITG_OK;
+  }
+  const int np = (int)(n + (n & 1));
+  int* hp = (int*)h->pinned;
+  for (int sweep = 0; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
+    ITG_CUDA(h, cudaMemsetAsync(flag_dev, 0, sizeof(int), h->stream));
+    for (int step = 0; step < np - 1; ++step)
+      k_jacobi_step<<<np / 2, 256, 0, h->stream>>>(W, m, (int)n, V, tol, step, flag_dev);
+    ITG_CHECK_LAUNCH(h);
+    ITG_CUDA(h, cudaMemcpyAsync(hp, flag_dev, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hp[0] == 0) { *sweeps_done = sweep + 1; return ITG_OK; }
+  }
+  *sweeps_done = JACOBI_MAX_SWEEPS;
+  return ITG_ERR_NOTCONVERGED;
+}
+
+}  // namespace
+
+extern "C" int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
+                             int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
+                             int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
+                             int64_t* k, double* truncerr, double* docut) {
+  if (!h || m < 0 || n < 0 || lda < m || !A || !U || !S || !V) return ITG_ERR_INVALID;
+  if (m == 0 || n == 0) {
+    if (k) *k = 0;
+    if (truncerr) *truncerr = 0;
+    if (docut) *docut = 0;
+    return ITG_OK;
+  }
+  const bool tr = m < n;
+  const int64_t mm = tr ? n : m, nn = tr ? m : n;  // working shape, mm >= nn
+  if (nn > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "svd: min(m,n) too large");
+  // scratch: W (mm*nn) | Vw (nn*nn) | sig (nn) | S,P (2 nn) | order (nn ints) | out3 | flag
+  size_t off = 0;
+  auto take = [&](size_t bytes) { size_t o = off; off += itg_align256(bytes); return o; };
+  size_t oW = take(sizeof(double) * mm * nn), oV = take(sizeof(double) * nn * nn),
+         oSig = take(sizeof(double) * nn), oP = take(sizeof(double) * nn),
+         oOrd = take(sizeof(int) * nn), oOut = take(4 * sizeof(double)), oFlag = take(sizeof(int));
+  ITG_TRY(itg_scratch_reserve(h, off));
+  char* base = (char*)h->scratch;
+  double* W = (double*)(base + oW);
+  double* Vw = (double*)(base + oV);
+  double* sig = (double*)(base + oSig);
+  double* P = (double*)(base + oP);
+  int* order = (int*)(base + oOrd);
+  double* out3 = (double*)(base + oOut);
+  int* flag = (int*)(base + oFlag);
+  if (!tr) {
+    k_copy_matrix<<<itg_blocks_for(m * n, 256, h->num_sms * 16), 256, 0, h->stream>>>(A, lda, m, n, W, 0.0);
+    ITG_CHECK_LAUNCH(h);
+  } else {
+    if (lda != m) return itg_fail(h, ITG_ERR_UNSUPPORTED, "svd of a wide matrix needs lda == m");
+    ITG_TRY(itg::transpose(h, m, n, A, lda, W));
+  }
+  int sweeps = 0;
+  int st = jacobi_run(h, W, mm, nn, Vw, flag, &sweeps);
+  if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED) return st;
+  k_col_norms<<<(unsigned)nn, 256, 0, h->stream>>>(W, mm, sig);
+  k_rank_desc<<<itg_blocks_for(nn, 256, 1024), 256, 0, h->stream>>>(sig, (int)nn, 0.0, order, S, P, 1);
+  ITG_CHECK_LAUNCH(h);
+  ITG_TRY(itg::truncate_dev(h, P, nn, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, out3));
+  // Left factor of the working problem = W[:, order] / sig; right = Vw[:, order].
+  double* Uw_dst = tr ? V : U;  // rows mm
+  double* Vw_dst = tr ? U : V;  // rows nn
+  dim3 g1(itg_blocks_for(mm, 256, 64), (unsigned)nn), g2(itg_blocks_for(nn, 256, 64), (unsigned)nn);
+  k_gather_cols<<<g1, 256, 0, h->stream>>>(W, mm, order, sig, 1, (int)nn, Uw_dst, mm);
+  k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, nn, order, sig, 0, (int)nn, Vw_dst, nn);
+  ITG_CHECK_LAUNCH(h);
+  ITG_TRY(read_out3(h, out3, k, truncerr, docut));
+  if (st == ITG_ERR_NOTCONVERGED)
+    return itg_fail(h, ITG_ERR_NOTCONVERGED, "Jacobi SVD did not converge in %d sweeps", sweeps);
+  return ITG_OK;
+}
+
+extern "C" int itg_eigh_trunc(itg_handle* h, int64_t n, const double* A, int64_t lda,
+                              int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
+                              int doRelCutoff, int legacy_gpu, double* D, double* U, int64_t* k,
+                              double* truncerr, double* docut) {
+  if (!h || n < 0 || lda < n || !A || !D || !U) return ITG_ERR_INVALID;
+  if (n == 0) {
+    if (k) *k = 0;
+    if (truncerr) *truncerr = 0;
+    if (docut) *docut = 0;
+    return ITG_OK;
+  }
+  if (n > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "eigh: n too large");
+  // B = A + c I with c = max row sum of |A| is positive semidefinite, so its
+  // one-sided Jacobi SVD B V = W with |w_j| = lambda_j + c and V the
+  // eigenvectors; lambda_j = |w_j| - c.
+  size_t off = 0;
+  auto take = [&](size_t bytes) { size_t o = off; off += itg_align256(bytes); return o; };
+  size_t oW = take(sizeof(double) * n * n), oV = take(sizeof(double) * n * n),
+         oSig = take(sizeof(double) * n), oP = take(sizeof(double) * n),
+         oOrd = take(sizeof(int) * n), oOut = take(4 * sizeof(double)), oFlag = take(sizeof(int)),
+         oC = take(sizeof(double));
+  ITG_TRY(itg_scratch_reserve(h, off));
+  char* base = (char*)h->scratch;
+  double* W = (double*)(base + oW);
+  double* Vw = (double*)(base + oV);
+  double* sig = (double*)(base + oSig);
+  double* P = (double*)(base + oP);
+  int* order = (int*)(base + oOrd);
+  double* out3 = (double*)(base + oOut);
+  int* flag = (int*)(base + oFlag);
+  double* cdev = (double*)(base + oC);
+  k_gershgorin<<<1, 1024, 0, h->stream>>>(A, lda, n, cdev);
+  ITG_CHECK_LAUNCH(h);
+  ITG_CUDA(h, cudaMemcpyAsync(h->pinned, cdev, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  const double shift = h->pinned[0] > 0.0 ? h->pinned[0] : 1.0;
+  k_copy_matrix<<<itg_blocks_for(n * n, 256, h->num_sms * 16), 256, 0, h->stream>>>(A, lda, n, n, W, shift);
+  ITG_CHECK_LAUNCH(h);
+  int sweeps = 0;
+  int st = jacobi_run(h, W, n, n, Vw, flag, &sweeps);
+  if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED) return st;
+  k_col_norms<<<(unsigned)n, 256, 0, h->stream>>>(W, n, sig);
+  k_rank_desc<<<itg_blocks_for(n, 256, 1024), 256, 0, h->stream>>>(sig, (int)n, shift, order, D, P, 0);
+  ITG_CHECK_LAUNCH(h);
+  ITG_TRY(itg::truncate_dev(h, P, n, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, out3));
+  dim3 g2(itg_blocks_for(n, 256, 64), (unsigned)n);
+  k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, n, order, sig, 0, (int)n, U, n);
+  ITG_CHECK_LAUNCH(h);
+  ITG_TRY(read_out3(h, out3, k, truncerr, docut));
+  if (st == ITG_ERR_NOTCONVERGED)
+    return itg_fail(h, ITG_ERR_NOTCONVERGED, "Jacobi eigensolver did not converge in %d sweeps", sweeps);
+  return ITG_OK;
+}
+
+// ================================================================== QR
+// Classical Gram-Schmidt with one full re-orthogonalisation (CGS2; Giraud,
+// Langou, Rozloznik 2005): column j is projected against Q[:, :j] twice, so the
+// computed Q is orthonormal to working precision for numerically full-rank A.
+// R's diagonal is non-negative.
+
+// h[i] = Q[:, i] . q for i < j   (one block per i)
+__global__ void k_proj(const double* __restrict__ Q, int64_t m, const double* __restrict__ q,
+                       double* __restrict__ hcoef) {
+  __shared__ double sh[32];
+  const double* col = Q + (int64_t)blockIdx.x * m;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) s = fma(col[i], q[i], s);
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    hcoef[blockIdx.x] = t;
+  }
+}
+
+// q -= Q[:, :j] h ; racc[:j] += h (done by block 0)
+__global__ void k_cgs_update(const double* __restrict__ Q, int64_t m, int j,
+                             const double* __restrict__ hcoef, double* __restrict__ q,
+                             double* __restrict__ racc) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double s = q[i];
+    for (int c = 0; c < j; ++c) s = fma(-Q[i + c * m], hcoef[c], s);
+    q[i] = s;
+  }
+  if (blockIdx.x == 0)
+    for (int c = threadIdx.x; c < j; c += blockDim.x) racc[c] += hcoef[c];
+}
+
+__global__ void k_normalize_col(double* __restrict__ q, int64_t m, double* __restrict__ rjj) {
+  __shared__ double sh[32];
+  __shared__ double nrm;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) s = fma(q[i], q[i], s);
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    nrm = sqrt(t);
+    *rjj = nrm;
+  }
+  __syncthreads();
+  double f = nrm > 0.0 ? 1.0 / nrm : 0.0;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) q[i] *= f;
+}
+
+extern "C" int itg_qr(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda, double* Q,
+                      double* R) {
+  if (!h || m < 0 || n < 0 || lda < m || !A || !Q || !R) return ITG_ERR_INVALID;
+  const int64_t r = m < n ? m : n;
+  if (r == 0) return ITG_OK;
+  if (r > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "qr: min(m,n) too large");
+  ITG_CUDA(h, cudaMemsetAsync(R, 0, sizeof(double) * r * n, h->stream));
+  ITG_TRY(itg_scratch_reserve(h, sizeof(double) * (size_t)(r + 256)));
+  double* hc = (double*)h->scratch;
+  const int gb = itg_blocks_for(m, 256, h->num_sms * 4);
+  for (int64_t j = 0; j < n; ++j) {
+    const double* a = A + j * lda;
+    double* rcol = R + j * r;
+    if (j < r) {
+      double* q = Q + j * m;
+      ITG_CUDA(h, cudaMemcpyAsync(q, a, sizeof(double) * m, cudaMemcpyDeviceToDevice, h->stream));
+      if (j > 0) {
+        for (int pass = 0; pass < 2; ++pass) {
+          k_proj<<<(unsigned)j, 256, 0, h->stream>>>(Q, m, q, hc);
+          k_cgs_update<<<gb, 256, 0, h->stream>>>(Q, m, (int)j, hc, q, rcol);
+        }
+      }
+      k_normalize_col<<<1, 1024, 0, h->stream>>>(q, m, rcol + j);
+    } else {
+      k_proj<<<(unsigned)r, 256, 0, h->stream>>>(Q, m, a, rcol);
+    }
+    ITG_CHECK_LAUNCH(h);
+  }
+  return ITG_OK;
+}

@@ -1,0 +1,104 @@
+// Internal declarations shared by the libitg.so translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <cstdarg>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/itg.h"
+
+#define ITG_MAX_RANK 16
+
+struct ContractPlan;  // itg_contract.cu
+struct SplitPlan;     // itg_split.cu
+
+struct itg_handle {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  // Reusable device scratch.  Operations on one handle are ordered on its
+  // stream, so a buffer can be handed to the next call once the previous
+  // kernels using it were enqueued before the new ones.
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  // Small pinned host buffer for scalar results (dot, truncation outputs).
+  double* pinned = nullptr;
+  // Persistent device buffers of the contraction plans, keyed by shape.
+  std::unordered_map<std::string, std::shared_ptr<ContractPlan>> plans;
+  // Device status word for bounded waits (ITG_ERR_TIMEOUT reporting).
+  int* dev_status = nullptr;
+};
+
+// Error helpers ---------------------------------------------------------------
+int itg_fail(itg_handle* h, int code, const char* fmt, ...);
+
+#define ITG_CUDA(h, call)                                                        \
+  do {                                                                           \
+    cudaError_t _e = (call);                                                     \
+    if (_e != cudaSuccess)                                                       \
+      return itg_fail((h), ITG_ERR_CUDA, "%s failed: %s (%s:%d)", #call,          \
+                      cudaGetErrorString(_e), __FILE__, __LINE__);               \
+  } while (0)
+
+#define ITG_CHECK_LAUNCH(h) ITG_CUDA((h), cudaGetLastError())
+
+#define ITG_TRY(expr)            \
+  do {                           \
+    int _s = (expr);             \
+    if (_s != ITG_OK) return _s; \
+  } while (0)
+
+// Device scratch management ---------------------------------------------------
+// Stack-like arena: callers take `Scratch` regions for the duration of one API
+// call.  Growth reallocates only when nothing from the arena is live.
+struct ScratchArena {
+  itg_handle* h;
+  size_t used = 0;
+  explicit ScratchArena(itg_handle* hh) : h(hh) {}
+};
+
+// Ensure the handle's scratch holds at least `bytes`; synchronises the stream
+// before freeing an older, smaller buffer.
+int itg_scratch_reserve(itg_handle* h, size_t bytes);
+
+static inline size_t itg_align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Grid sizing helpers ---------------------------------------------------------
+static inline int itg_blocks_for(int64_t n, int threads, int cap) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (int)b;
+}
+
+// Internal entry points shared between translation units ----------------------
+namespace itg {
+
+// Deterministic dot product into a device double (two-stage reduction).
+int dot_dev(itg_handle* h, int64_t n, const double* x, const double* y, double* out,
+            double* partials);
+int nrm2_dev(itg_handle* h, int64_t n, const double* x, double* out, double* partials);
+
+// Truncation on device: writes {n_keep (as double), truncerr, docut} to out[0..2].
+int truncate_dev(itg_handle* h, const double* P, int64_t n, int64_t maxdim, int64_t mindim,
+                 double cutoff, int absoluteCutoff, int doRelCutoff, int legacy_gpu,
+                 double* out3);
+
+// Column-major transpose (out is n x m) of the m x n matrix in (lda).
+int transpose(itg_handle* h, int64_t m, int64_t n, const double* in, int64_t lda, double* out);
+
+// General contraction with explicit plan cache and no scratch use beyond the plan.
+int contract_f64(itg_handle* h, double alpha, const double* A, int rankA, const int64_t* dimsA,
+                 const int32_t* modesA, const double* B, int rankB, const int64_t* dimsB,
+                 const int32_t* modesB, double beta, double* C, int rankC, const int64_t* dimsC,
+                 const int32_t* modesC, int precision);
+
+}  // namespace itg

@@ -1,0 +1,326 @@
+"""Two-site DMRG driver over libitg.so (the dmrg(H, psi, sweeps) entry point).
+
+ITensors.jl's ``dmrg`` (ITensors 0.2, called at examples/dmrg.jl:25 and
+test/dmrg.jl:27,75 of the reference) sweeps bonds b = 1..N-1 and back
+(``sweepnext``), and for every bond: forms phi = psi[b] * psi[b+1], finds the
+lowest eigenvector of the ProjMPO effective Hamiltonian, factorises it with a
+truncated SVD (``replacebond!``/``factorize``) and updates the projected
+environments.  This module does the same with every tensor operation in
+libitg.so: Davidson with the fused H_eff chain (itg_davidson_heff2), Jacobi SVD
+with on-device truncation (itg_svd_trunc), gather/scale Diag kernels for S and
+gather-GEMM contractions for the environments.  The host only orchestrates.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import tensor as T
+from ._lib import ITG_F64, PREC_FP64, PREC_SPLIT, NotConverged, i32arr, i64arr
+from .mps import MPO, MPS
+from .tensor import Dense, ITensor, Index
+
+
+class Sweeps:
+    """Sweep schedule (ITensors' Sweeps with maxdim!/mindim!/cutoff!/noise!)."""
+
+    def __init__(self, nsweep: int, maxdim=None, mindim=None, cutoff=None, noise=None):
+        self.nsweep = int(nsweep)
+        self._maxdim = list(maxdim) if maxdim is not None else [1]
+        self._mindim = list(mindim) if mindim is not None else [1]
+        self._cutoff = list(cutoff) if cutoff is not None else [0.0]
+        self._noise = list(noise) if noise is not None else [0.0]
+
+    @staticmethod
+    def _at(v, i):
+        return v[min(i, len(v) - 1)]
+
+    def maxdim(self, i):
+        return int(self._at(self._maxdim, i))
+
+    def mindim(self, i):
+        return int(self._at(self._mindim, i))
+
+    def cutoff(self, i):
+        return float(self._at(self._cutoff, i))
+
+    def noise(self, i):
+        return float(self._at(self._noise, i))
+
+
+def maxdim_(sw: Sweeps, *v):
+    sw._maxdim = list(v)
+
+
+def mindim_(sw: Sweeps, *v):
+    sw._mindim = list(v)
+
+
+def cutoff_(sw: Sweeps, *v):
+    sw._cutoff = list(v)
+
+
+def noise_(sw: Sweeps, *v):
+    sw._noise = list(v)
+
+
+def sweepnext(N: int):
+    """(b, half) pairs of one sweep: bonds 0..N-2 left to right, then back."""
+    for b in range(N - 1):
+        yield b, 1
+    for b in range(N - 2, -1, -1):
+        yield b, 2
+
+
+@dataclass
+class SweepRecord:
+    energy: float
+    maxlinkdim: int
+    maxtruncerr: float
+    seconds: float
+    matvecs: int
+
+
+@dataclass
+class DMRGResult:
+    energy: float
+    psi: MPS
+    sweeps: list = field(default_factory=list)
+
+
+# ---------------------------------------------------------- raw helpers
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _contract_raw(h, A, dA, mA, B, dB, mB, dC, mC, precision=PREC_FP64, out=None):
+    n = int(np.prod(dC)) if len(dC) else 1
+    if out is None:
+        out = T.empty_dev(n)
+    h.call("itg_contract", ITG_F64, C.c_double(1.0), _ptr(A), len(dA), i64arr(dA), i32arr(mA),
+           _ptr(B), len(dB), i64arr(dB), i32arr(mB), C.c_double(0.0), _ptr(out), len(dC),
+           i64arr(dC), i32arr(mC), int(precision))
+    return out
+
+
+def _diag_raw(h, d, dD, mD, Tt, dT, mT, dC, mC):
+    n = int(np.prod(dC))
+    out = T.empty_dev(n)
+    h.call("itg_diag_contract", ITG_F64, C.c_double(1.0), _ptr(d), 0, len(dD), i64arr(dD), i32arr(mD),
+           _ptr(Tt), len(dT), i64arr(dT), i32arr(mT), C.c_double(0.0), _ptr(out), len(dC),
+           i64arr(dC), i32arr(mC))
+    return out
+
+
+def _permute_raw(h, A, dA, mA, mB):
+    out = T.empty_dev(int(np.prod(dA)))
+    h.call("itg_permute", ITG_F64, C.c_double(1.0), _ptr(A), len(dA), i64arr(dA), i32arr(mA),
+           _ptr(out), i32arr(mB))
+    return out
+
+
+class _Chain:
+    """Raw device view of an MPS / MPO for the sweep: arrays + shapes."""
+
+    def __init__(self, psi: MPS, H: MPO):
+        self.N = len(psi)
+        self.A = []   # (chiL, d, chiR)
+        self.Ad = []
+        for t in psi.tensors:
+            self.A.append(t.store.data.contiguous())
+            self.Ad.append(t.dims)
+        self.W = []
+        self.Wd = []
+        for t in H.tensors:
+            self.W.append(t.store.data.contiguous())
+            self.Wd.append(t.dims)  # (wl, d, d, wr)
+
+
+def _env_left(h, Lt, Ld, A, Ad, W, Wd, prec):
+    """L_new[b, x, b'] = sum L[a,w,a'] A[a,s,b] W[w,s',s,x] A[a',s',b']."""
+    a, d, b = Ad
+    wl, _, _, x = Wd
+    # modes: a=1 w=2 ap=3 s=4 b=5 sp=6 x=7 bp=8
+    t1 = _contract_raw(h, Lt, Ld, [1, 2, 3], A, Ad, [1, 4, 5], (wl, a, d, b), [2, 3, 4, 5], prec)
+    t2 = _contract_raw(h, t1, (wl, a, d, b), [2, 3, 4, 5], W, Wd, [2, 6, 4, 7], (a, b, d, x),
+                       [3, 5, 6, 7], prec)
+    Ln = _contract_raw(h, t2, (a, b, d, x), [3, 5, 6, 7], A, Ad, [3, 6, 8], (b, x, b), [5, 7, 8], prec)
+    return Ln, (b, x, b)
+
+
+def _env_right(h, Rt, Rd, A, Ad, W, Wd, prec):
+    """R_new[a, w, a'] = sum A[a,s,b] W[w,s',s,x] R[b,x,b'] A[a',s',b']."""
+    a, d, b = Ad
+    w, _, _, x = Wd
+    # modes: a=1 s=2 b=3 x=4 bp=5 w=6 sp=7 ap=8
+    t1 = _contract_raw(h, A, Ad, [1, 2, 3], Rt, Rd, [3, 4, 5], (a, d, x, b), [1, 2, 4, 5], prec)
+    t2 = _contract_raw(h, t1, (a, d, x, b), [1, 2, 4, 5], W, Wd, [6, 7, 2, 4], (a, b, w, d),
+                       [1, 5, 6, 7], prec)
+    Rn = _contract_raw(h, t2, (a, b, w, d), [1, 5, 6, 7], A, Ad, [8, 7, 5], (a, w, a), [1, 6, 8], prec)
+    return Rn, (a, w, a)
+
+
+def _orthogonalize_left_end(h, ch: _Chain):
+    """Right-orthogonalise sites N-1..1 by QR (orthogonalize!(psi, 1)) and normalise site 0."""
+    for j in range(ch.N - 1, 0, -1):
+        a, d, b = ch.Ad[j]
+        # M = A_j as (a) x (d b); QR of M^T = Q R  ->  A_j = R^T Q^T
+        Mt = _permute_raw(h, ch.A[j], (a, d, b), [1, 2, 3], [2, 3, 1])  # (d, b, a)
+        m, n = d * b, a
+        r = min(m, n)
+        Q = T.empty_dev(m * r)
+        R = T.empty_dev(r * n)
+        h.call("itg_qr", C.c_int64(m), C.c_int64(n), _ptr(Mt), C.c_int64(m), _ptr(Q), _ptr(R))
+        # A_j = Q^T as (r, d, b)
+        ch.A[j] = _permute_raw(h, Q, (d, b, r), [2, 3, 1], [1, 2, 3])
+        ch.Ad[j] = (r, d, b)
+        # A_{j-1}[a', s, r] = sum_a A_{j-1}[a', s, a] R[r, a]
+        pa, pd, _ = ch.Ad[j - 1]
+        ch.A[j - 1] = _contract_raw(h, ch.A[j - 1], ch.Ad[j - 1], [1, 2, 3], R, (r, n), [4, 3],
+                                    (pa, pd, r), [1, 2, 4])
+        ch.Ad[j - 1] = (pa, pd, r)
+    nrm = C.c_double()
+    h.call("itg_nrm2", C.c_int64(ch.A[0].numel()), _ptr(ch.A[0]), C.byref(nrm))
+    h.call("itg_scal", C.c_int64(ch.A[0].numel()), C.c_double(1.0 / nrm.value), _ptr(ch.A[0]))
+
+
+def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int = 2,
+         eigsolve_tol: float = 1e-14, precision: str | int = "fp64", legacy_gpu_truncate: bool = False,
+         outputlevel: int = 0, return_result: bool = False):
+    """Ground state by two-site DMRG.  Returns (energy, psi) like ITensors' dmrg.
+
+    krylovdim / maxiter: Davidson subspace size before a restart and number of
+    restarts per bond.  precision "split" runs the chi^3 contractions of the
+    eigensolver on the tensor cores (FP64 operands split into bf16 slices).
+    """
+    if isinstance(precision, str):
+        precision = {"fp64": PREC_FP64, "split": PREC_SPLIT}[precision.lower()]
+    if any(sweeps.noise(i) > 0 for i in range(sweeps.nsweep)):
+        raise NotImplementedError("noise > 0 (density-matrix perturbation) is not supported")
+    h = T._h()
+    N = len(psi0)
+    if len(H) != N:
+        raise T.DimensionMismatch(2, "dmrg: MPO and MPS lengths differ")
+    if N < 2:
+        raise ValueError("dmrg needs at least two sites")
+    psi0 = T.cu(psi0)
+    H = T.cu(H)
+    ch = _Chain(psi0.copy(), H)
+    _orthogonalize_left_end(h, ch)
+    one = T.empty_dev(1).fill_(1.0)
+    Lenv = [None] * (N + 1)
+    Renv = [None] * (N + 1)
+    Lenv[0] = (one, (1, 1, 1))
+    Renv[N] = (one, (1, 1, 1))
+    for j in range(N - 1, 1, -1):
+        Renv[j] = _env_right(h, Renv[j + 1][0], Renv[j + 1][1], ch.A[j], ch.Ad[j], ch.W[j], ch.Wd[j],
+                             PREC_FP64)
+    energy = 0.0
+    records = []
+    for sw in range(sweeps.nsweep):
+        t0 = time.perf_counter()
+        maxdim, mindim, cutoff = sweeps.maxdim(sw), sweeps.mindim(sw), sweeps.cutoff(sw)
+        maxerr = 0.0
+        nmv_tot = 0
+        for b, ha in sweepnext(N):
+            a, d1, _ = ch.Ad[b]
+            _, d2, c = ch.Ad[b + 1]
+            k_old = ch.Ad[b][2]
+            # phi = A_b * A_{b+1}: (a, d1, d2, c)
+            phi = _contract_raw(h, ch.A[b], (a, d1, k_old), [1, 2, 3], ch.A[b + 1], (k_old, d2, c),
+                                [3, 4, 5], (a, d1, d2, c), [1, 2, 4, 5])
+            Lt, Ld = Lenv[b]
+            Rt, Rd = Renv[b + 2]
+            W1, W1d = ch.W[b], ch.Wd[b]
+            W2, W2d = ch.W[b + 1], ch.Wd[b + 1]
+            e = C.c_double()
+            nmv = C.c_int()
+            h.call("itg_davidson_heff2", C.c_int64(a), C.c_int64(c), C.c_int64(d1), C.c_int64(W1d[0]),
+                   C.c_int64(W1d[3]), C.c_int64(W2d[3]), _ptr(Lt), _ptr(W1), _ptr(W2), _ptr(Rt),
+                   _ptr(phi), int(krylovdim), int(maxiter), C.c_double(eigsolve_tol), int(precision),
+                   C.byref(e), C.byref(nmv))
+            energy = e.value
+            nmv_tot += nmv.value
+            # SVD of phi as (a d1) x (d2 c)
+            m, n = a * d1, d2 * c
+            r = min(m, n)
+            U = T.empty_dev(m * r)
+            S = T.empty_dev(r)
+            V = T.empty_dev(n * r)
+            k = C.c_int64()
+            te = C.c_double()
+            dc = C.c_double()
+            try:
+                h.call("itg_svd_trunc", C.c_int64(m), C.c_int64(n), _ptr(phi), C.c_int64(m),
+                       C.c_int64(maxdim), C.c_int64(mindim), C.c_double(cutoff), 0, 1,
+                       int(legacy_gpu_truncate), _ptr(U), _ptr(S), _ptr(V), C.byref(k), C.byref(te),
+                       C.byref(dc))
+            except NotConverged:
+                pass  # factors are still returned; the rotation limit is generous
+            kk = int(k.value)
+            maxerr = max(maxerr, te.value)
+            Uk = U[: m * kk]
+            Vk = V[: n * kk]
+            Sk = S[:kk]
+            if ha == 1:
+                ch.A[b] = Uk.clone()
+                ch.Ad[b] = (a, d1, kk)
+                # A_{b+1}[k, d2, c] = S[k] V[(d2 c), k]
+                ch.A[b + 1] = _diag_raw(h, Sk, (kk, kk), [1, 2], Vk, (d2, c, kk), [3, 4, 1],
+                                        (kk, d2, c), [2, 3, 4])
+                ch.Ad[b + 1] = (kk, d2, c)
+                Lenv[b + 1] = _env_left(h, Lt, Ld, ch.A[b], ch.Ad[b], W1, W1d, PREC_FP64)
+            else:
+                # A_b[a, d1, k] = U[(a d1), k] S[k];  A_{b+1} = V^T
+                ch.A[b] = _diag_raw(h, Sk, (kk, kk), [1, 2], Uk, (a, d1, kk), [3, 4, 1],
+                                    (a, d1, kk), [3, 4, 2])
+                ch.Ad[b] = (a, d1, kk)
+                ch.A[b + 1] = _permute_raw(h, Vk, (d2, c, kk), [1, 2, 3], [3, 1, 2])
+                ch.Ad[b + 1] = (kk, d2, c)
+                Renv[b + 1] = _env_right(h, Rt, Rd, ch.A[b + 1], ch.Ad[b + 1], W2, W2d, PREC_FP64)
+        h.call("itg_synchronize")
+        rec = SweepRecord(energy, max(x[2] for x in ch.Ad[:-1]), maxerr, time.perf_counter() - t0, nmv_tot)
+        records.append(rec)
+        if outputlevel > 0:
+            print(f"After sweep {sw + 1} energy={energy:.14f} maxlinkdim={rec.maxlinkdim} "
+                  f"maxerr={rec.maxtruncerr:.2e} time={rec.seconds:.3f}", flush=True)
+    # package the result as an MPS with fresh link indices
+    links = [Index(1, "Link,l=0")] + [Index(ch.Ad[j][2], f"Link,l={j + 1}") for j in range(N - 1)] + \
+            [Index(1, f"Link,l={N}")]
+    ts = [ITensor(Dense(ch.A[j]), (links[j], psi0.sites[j], links[j + 1])) for j in range(N)]
+    psi = MPS(ts, psi0.sites, 0, 1)
+    if return_result:
+        return DMRGResult(energy, psi, records)
+    return energy, psi
+
+
+def inner(phi: MPS, psi: MPS) -> float:
+    """<phi|psi> for real MPS with matching site indices (inner, ITensors)."""
+    h = T._h()
+    phi, psi = T.cu(phi), T.cu(psi)
+    E = T.empty_dev(1).fill_(1.0)
+    Ed = (1, 1)
+    for j in range(len(psi)):
+        a, d, b = phi[j].dims
+        a2, d2, b2 = psi[j].dims
+        # E[a, a2] -> t[a2, d, b] = sum_a E[a,a2] phi[a,d,b] -> E'[b, b2] = sum t[a2,d,b] psi[a2,d,b2]
+        t = _contract_raw(h, E, Ed, [1, 2], phi[j].store.data, (a, d, b), [1, 3, 4], (a2, d, b), [2, 3, 4])
+        E = _contract_raw(h, t, (a2, d, b), [2, 3, 4], psi[j].store.data, (a2, d2, b2), [2, 3, 5],
+                          (b, b2), [4, 5])
+        Ed = (b, b2)
+    return float(E[0].item())
+
+
+def expect_energy(H: MPO, psi: MPS) -> float:
+    """<psi|H|psi> / <psi|psi> through left environments."""
+    h = T._h()
+    H, psi = T.cu(H), T.cu(psi)
+    one = T.empty_dev(1).fill_(1.0)
+    Lt, Ld = one, (1, 1, 1)
+    for j in range(len(psi)):
+        Lt, Ld = _env_left(h, Lt, Ld, psi[j].store.data.contiguous(), psi[j].dims,
+                           H[j].store.data.contiguous(), H[j].dims, PREC_FP64)
+    return float(Lt[0].item()) / inner(psi, psi)

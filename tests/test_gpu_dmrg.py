@@ -1,0 +1,161 @@
+"""Two-site DMRG path on the GPU against the oracle and known answers.
+
+* H_eff matvec (itg_heff2_apply) vs the oracle at 1e-12 relative Frobenius;
+* Davidson (itg_davidson_heff2) vs the oracle's restatement of the same solver;
+* dmrg() on the Heisenberg N=20 workload (maxdim [10,20,50,100,100],
+  cutoff 1e-10, Davidson maxiter 2): energy vs the oracle's DMRG and vs exact
+  diagonalisation;
+* the reference's own DMRG known answers (test/dmrg.jl): critical TFIM N=32
+  closed form within 1e-2 relative, S=1 Heisenberg N=10 energy < -12
+  (noise is 0 here: the density-matrix noise term is not implemented);
+* MPS utilities: product states, inner, expectation energy.
+"""
+import ctypes as C
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import itg_oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = json.loads((Path(__file__).parent / "golden" / "reference_known_answers.json").read_text())
+
+
+def relerr(x, y):
+    return np.linalg.norm((np.asarray(x) - np.asarray(y)).ravel()) / np.linalg.norm(np.asarray(y).ravel())
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(O.flat(a).copy()).cuda()
+
+
+def _heff_inputs(chi, chiR=None, d=2, w=5, seed=0):
+    chiR = chiR or chi
+    rng = np.random.default_rng(seed)
+    L = rng.standard_normal((chi, w, chi))
+    R = rng.standard_normal((chiR, w, chiR))
+    W1 = rng.standard_normal((w, d, d, w))
+    W2 = rng.standard_normal((w, d, d, w))
+    psi = rng.standard_normal((chi, d, d, chiR))
+    return L, W1, W2, R, psi
+
+
+@pytest.mark.parametrize("chi,chiR,d,w", [(1, 2, 2, 5), (7, 9, 2, 5), (40, 33, 3, 4), (130, 130, 2, 5)])
+def test_heff_apply_matches_oracle(gpu, chi, chiR, d, w):
+    from itg import _lib
+    L, W1, W2, R, psi = _heff_inputs(chi, chiR, d, w, seed=chi)
+    out = _dev(np.zeros_like(psi))
+    h = _lib.handle(0)
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    Ld, W1d, W2d, Rd, pd = map(_dev, (L, W1, W2, R, psi))
+    h.call("itg_heff2_apply", C.c_int64(chi), C.c_int64(chiR), C.c_int64(d), C.c_int64(w),
+           C.c_int64(w), C.c_int64(w), ptr(Ld), ptr(W1d), ptr(W2d), ptr(Rd), ptr(pd), ptr(out), 0)
+    ref = O.heff_apply(L, W1, W2, R, psi)
+    got = O.unflat(out.cpu().numpy(), psi.shape)
+    assert relerr(got, ref) < 1e-12
+
+
+def test_davidson_matches_oracle(gpu):
+    from itg import _lib
+    chi, d, w = 24, 2, 5
+    L, W1, W2, R, psi = _heff_inputs(chi, d=d, w=w, seed=3)
+    # make H_eff symmetric: symmetrise the environments and the MPO tensors
+    L = L + L.transpose(2, 1, 0)
+    R = R + R.transpose(2, 1, 0)
+    W1 = W1 + W1.transpose(0, 2, 1, 3)
+    W2 = W2 + W2.transpose(0, 2, 1, 3)
+    mv = lambda v: O.flat(O.heff_apply(L, W1, W2, R, O.unflat(v, psi.shape)))
+    dg = O.flat(O.heff_diag(L, W1, W2, R))
+    for kd, mi in ((3, 2), (6, 10)):
+        th_o, x_o, nmv_o = O.davidson(mv, O.flat(psi), dg, kd, mi, 1e-14)
+        h = _lib.handle(0)
+        ptr = lambda t: C.c_void_p(t.data_ptr())
+        Ld, W1d, W2d, Rd, pd = map(_dev, (L, W1, W2, R, psi))
+        e = C.c_double()
+        nmv = C.c_int()
+        h.call("itg_davidson_heff2", C.c_int64(chi), C.c_int64(chi), C.c_int64(d), C.c_int64(w),
+               C.c_int64(w), C.c_int64(w), ptr(Ld), ptr(W1d), ptr(W2d), ptr(Rd), ptr(pd), kd, mi,
+               C.c_double(1e-14), 0, C.byref(e), C.byref(nmv))
+        assert nmv.value == nmv_o
+        assert abs(e.value - th_o) < 1e-10 * abs(th_o)
+        x = pd.cpu().numpy()
+        assert min(np.linalg.norm(x - x_o), np.linalg.norm(x + x_o)) < 1e-8
+
+
+def _run_dmrg_pair(gpu, N, d, mpo_gpu, mpo_oracle, linkdim, seed, maxdims, cutoffs, nsweep, **kw):
+    sites = gpu.siteinds("S=1/2" if d == 2 else "S=1", N)
+    H = gpu.cuMPO(mpo_gpu(sites))
+    psi0 = gpu.randomCuMPS(sites, linkdim, seed=seed)
+    sw = gpu.Sweeps(nsweep, maxdim=maxdims, cutoff=cutoffs, mindim=kw.pop("mindim", [1]))
+    res = gpu.dmrg(H, psi0, sw, return_result=True, **kw)
+    e_o, _, hist = O.dmrg(mpo_oracle(N), O.random_mps([d] * N, linkdim, seed), maxdims, cutoffs, nsweep,
+                          return_sweeps=True)
+    return res, e_o, hist
+
+
+def test_dmrg_heisenberg_n20_matches_oracle_and_ed(gpu):
+    """The plain-method Heisenberg N=20 workload end to end."""
+    N = 20
+    res, e_o, hist = _run_dmrg_pair(gpu, N, 2, gpu.heisenberg_mpo, lambda n: O.heisenberg_mpo(n), 10,
+                                    1234 + 0, [10, 20, 50, 100, 100], [1e-10], 5)
+    e_ed = GOLD["ed"]["heisenberg_N20"]
+    assert abs(res.energy - e_o) < 1e-9, (res.energy, e_o)
+    assert abs(res.energy - e_ed) < 1e-7
+    assert res.psi.maxlinkdim() <= 100
+    # per-sweep energies track the oracle
+    for rec, (eo, _, _) in zip(res.sweeps, hist):
+        assert abs(rec.energy - eo) < 1e-6
+
+
+def test_dmrg_heisenberg_n12_exact(gpu):
+    """No truncation needed at N=12: the energy must reach ED at 1e-10."""
+    N = 12
+    res, e_o, _ = _run_dmrg_pair(gpu, N, 2, gpu.heisenberg_mpo, lambda n: O.heisenberg_mpo(n), 10, 77,
+                                 [10, 20, 50, 100], [1e-14], 6)
+    assert abs(res.energy - GOLD["ed"]["heisenberg_N12"]) < 1e-10
+    assert abs(res.energy - e_o) < 1e-10
+
+
+def test_dmrg_tfim_closed_form(gpu):
+    g = GOLD["dmrg"]["tfim"]
+    N = g["N"]
+    sites = gpu.siteinds("S=1/2", N)
+    H = gpu.cuMPO(gpu.tfim_mpo(sites, h=g["h"], J=g["J"]))
+    psi0 = gpu.randomCuMPS(sites, 1, seed=g["seed"])
+    sw = gpu.Sweeps(g["nsweep"], maxdim=g["maxdim"], cutoff=[g["cutoff"]])
+    energy, psi = gpu.dmrg(H, psi0, sw)
+    exact = O.tfim_closed_form(N)
+    assert abs((energy - exact) / exact) < g["rel_tol"]
+    assert abs(energy - exact) < 1e-6
+    e_o, _ = O.dmrg(O.tfim_mpo(N, h=g["h"], J=g["J"]), O.random_mps([2] * N, 1, g["seed"]), g["maxdim"],
+                    [g["cutoff"]], g["nsweep"])
+    assert abs(energy - e_o) < 1e-9
+    assert abs(gpu.expect_energy(H, psi) - energy) < 1e-9
+
+
+def test_dmrg_spin1_bound(gpu):
+    g = GOLD["dmrg"]["spin1_heisenberg"]
+    sites = gpu.siteinds("S=1", g["N"])
+    H = gpu.cuMPO(gpu.heisenberg_mpo(sites))
+    psi0 = gpu.randomCuMPS(sites, 1, seed=11)
+    sw = gpu.Sweeps(g["nsweep"], maxdim=g["maxdim"], mindim=g["mindim"], cutoff=[g["cutoff"]])
+    energy, psi = gpu.dmrg(H, psi0, sw)
+    assert energy < g["energy_below"]
+
+
+def test_product_state_and_inner(gpu):
+    N = 6
+    sites = gpu.siteinds("S=1/2", N)
+    up = gpu.productCuMPS(sites, ["Up"] * N)
+    neel = gpu.productCuMPS(sites, ["Up", "Dn"] * (N // 2))
+    assert gpu.inner(up, up) == pytest.approx(1.0)
+    assert gpu.inner(up, neel) == pytest.approx(0.0)
+    H = gpu.cuMPO(gpu.heisenberg_mpo(sites))
+    # <up|H|up> = (N-1)/4 ; <neel|H|neel> = -(N-1)/4
+    assert gpu.expect_energy(H, up) == pytest.approx((N - 1) / 4, abs=1e-14)
+    assert gpu.expect_energy(H, neel) == pytest.approx(-(N - 1) / 4, abs=1e-14)
+    psi = gpu.cpu(gpu.randomCuMPS(sites, 4, seed=3))
+    assert not psi.is_cuda and gpu.cuMPS(psi).is_cuda

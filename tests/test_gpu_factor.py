@@ -1,0 +1,147 @@
+"""Truncation, SVD, eigen and QR on the GPU against the oracle.
+
+* truncate: the reference golden vectors (test/test_cutruncate.jl:9-17) through
+  itg_truncate with legacy_gpu = 1, and random spectra bit-exact against both
+  oracle rules (integer keep count exact, sums identical);
+* svd: A = U S V^T and orthogonality at 1e-14 (test/test_cuitensor.jl:105-112),
+  singular values against LAPACK at 1e-13 relative to sigma_max;
+* qr: reconstruction and orthogonality at 1e-14 (test/test_cuitensor.jl:125-130);
+* eigen: descending eigenvalues against LAPACK, truncation.
+"""
+import ctypes as C
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import itg_oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = json.loads((Path(__file__).parent / "golden" / "reference_known_answers.json").read_text())
+
+
+def _truncate_gpu(P, legacy, **kw):
+    import torch
+    from itg import _lib
+    from itg.tensor import _ptr
+    h = _lib.handle(0)
+    Pd = torch.tensor(np.asarray(P, dtype=np.float64), device="cuda")
+    n = C.c_int64()
+    te = C.c_double()
+    dc = C.c_double()
+    h.call("itg_truncate", _ptr(Pd), C.c_int64(len(P)), C.c_int64(int(kw.get("maxdim", 0))),
+           C.c_int64(int(kw.get("mindim", 1))), C.c_double(kw.get("cutoff", 0.0)),
+           int(kw.get("absoluteCutoff", False)), int(kw.get("doRelCutoff", True)), int(legacy),
+           C.byref(n), C.byref(te), C.byref(dc))
+    return n.value, te.value, dc.value
+
+
+@pytest.mark.parametrize("case", GOLD["truncate"], ids=lambda c: c["source"])
+def test_truncate_reference_golden_on_gpu(gpu, case):
+    kw = case["kwargs"]
+    n, te, dc = _truncate_gpu(case["P"], True, cutoff=kw.get("cutoff", 0.0),
+                              absoluteCutoff=kw.get("absoluteCutoff", False))
+    P = np.asarray(case["P"])
+    kept = [0.0] if P.max() == 0 else list(P[:n])
+    assert kept == case["kept"]
+    assert te == pytest.approx(case["truncerr"], rel=1.5e-8, abs=1e-300)
+    assert dc == pytest.approx(case["docut"], rel=1.5e-8, abs=1e-300)
+
+
+@pytest.mark.parametrize("legacy", [False, True])
+def test_truncate_random_spectra_bit_exact(gpu, legacy):
+    rng = np.random.default_rng(11)
+    f = O.truncate_legacy_gpu if legacy else O.truncate_cpu
+    for t in range(60):
+        n = int(rng.integers(1, 300))
+        P = np.sort(rng.exponential(size=n) * 10.0 ** rng.uniform(-12, 0, size=n))[::-1].copy()
+        kw = dict(maxdim=int(rng.integers(0, n + 3)), mindim=int(rng.integers(1, 4)),
+                  cutoff=float(10.0 ** rng.uniform(-14, -1)), absoluteCutoff=bool(rng.integers(0, 2)),
+                  doRelCutoff=bool(rng.integers(0, 2)))
+        got = _truncate_gpu(P, legacy, **kw)
+        ref = f(P, **kw)
+        assert got[0] == ref[0], (t, kw)
+        assert got[1] == ref[1] and got[2] == ref[2], (t, kw, got, ref)
+
+
+@pytest.mark.parametrize("m,n", [(7, 5), (5, 7), (64, 64), (300, 180), (180, 300), (520, 400)])
+def test_svd_reconstruction_and_orthogonality(gpu, m, n):
+    I = gpu.Index
+    i, j = I(m), I(n)
+    A = gpu.randomCuITensor(i, j, seed=m * 1000 + n)
+    U, S, V, spec = gpu.svd(A, i)
+    u = U.inds[-1]
+    Ah = A.array()
+    Uh, Sh, Vh = U.array(i, u), S.store.data.cpu().numpy(), V.array(j, V.inds[-1])
+    assert np.allclose(Uh @ np.diag(Sh) @ Vh.T, Ah, rtol=0, atol=1e-13 * np.abs(Ah).max() * max(m, n))
+    r = min(m, n)
+    assert np.abs(Uh.T @ Uh - np.eye(r)).max() < 1e-13
+    assert np.abs(Vh.T @ Vh - np.eye(r)).max() < 1e-13
+    sref = np.linalg.svd(Ah, compute_uv=False)
+    assert np.abs(Sh - sref).max() < 1e-13 * sref[0]
+    assert np.all(np.diff(Sh) <= 0)
+    # ITensor-level identity A = U * S * V
+    R = U * S * V
+    assert np.abs(R.array(i, j) - Ah).max() < 1e-12 * np.abs(Ah).max()
+
+
+def test_svd_truncation_matches_oracle(gpu):
+    rng = np.random.default_rng(5)
+    m = n = 256
+    Q1, _ = np.linalg.qr(rng.standard_normal((m, m)))
+    Q2, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.exp(-np.arange(n) / 20.0)
+    M = (Q1 * s) @ Q2.T
+    I = gpu.Index
+    i, j = I(m), I(n)
+    A = gpu.cuITensor(M, i, j)
+    for kw in (dict(cutoff=1e-10), dict(maxdim=50), dict(cutoff=1e-6, maxdim=200),
+               dict(cutoff=1e-4, absoluteCutoff=True)):
+        U, S, V, spec = gpu.svd(A, i, **kw)
+        Uo, So, Vo, te, _ = O.svd_trunc(M, **kw)
+        assert len(S.store.data) == len(So), kw
+        assert np.abs(S.store.data.cpu().numpy() - So).max() < 1e-13
+        assert spec.truncerr == pytest.approx(te, rel=1e-9, abs=1e-16)
+
+
+def test_qr(gpu):
+    I = gpu.Index
+    i, j, k, l = I(2), I(3), I(4), I(5)
+    A = gpu.randomCuITensor(i, j, k, l, seed=21)
+    Q, R = gpu.qr(A, i, l)
+    q = Q.inds[-1]
+    assert np.abs((Q * R).array(i, j, k, l) - A.array()).max() < 1e-13
+    Qm = Q.array(i, l, q).reshape(10, -1, order="F")
+    assert np.abs(Qm.T @ Qm - np.eye(Qm.shape[1])).max() < 1e-14
+    # tall and wide matrices
+    for (m, n) in ((200, 50), (40, 90)):
+        a, b = I(m), I(n)
+        M = gpu.randomCuITensor(a, b, seed=m + n)
+        Q, R = gpu.qr(M, a)
+        assert np.abs((Q * R).array(a, b) - M.array()).max() < 1e-12
+        Qh = Q.array(a, Q.inds[-1])
+        assert np.abs(Qh.T @ Qh - np.eye(Qh.shape[1])).max() < 1e-13
+
+
+def test_eigen_hermitian(gpu):
+    I = gpu.Index
+    n = 150
+    i = I(n)
+    ip = i.prime()
+    rng = np.random.default_rng(8)
+    X = rng.standard_normal((n, n))
+    M = X @ X.T / n
+    A = gpu.cuITensor(M, i, ip)
+    D, U, spec = gpu.eigen(A, [i], [ip])
+    w = D.store.data.cpu().numpy()
+    wref = np.linalg.eigvalsh(M)[::-1]
+    assert np.abs(w - wref).max() < 1e-12 * wref[0]
+    Uh = U.array(ip, U.inds[-1])
+    assert np.abs(Uh.T @ Uh - np.eye(n)).max() < 1e-12
+    assert np.abs(Uh @ np.diag(w) @ Uh.T - M).max() < 1e-12 * wref[0]
+    # truncated, indefinite matrix
+    S = X + X.T
+    D, U, spec = gpu.eigen(gpu.cuITensor(S, i, ip), [i], [ip], maxdim=20)
+    wref = np.linalg.eigvalsh(S)[::-1]
+    assert np.abs(D.store.data.cpu().numpy() - wref[:20]).max() < 1e-11 * np.abs(wref).max()
