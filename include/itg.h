@@ -225,6 +225,13 @@ ITG_API int itg_heff2_apply(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d
                     const double* L, const double* W1, const double* W2, const double* R,
                     const double* psi, double* out, int precision);
 
+/* diag[a, s1, s2, b] = H_eff[(a,s1,s2,b),(a,s1,s2,b)] for the operator of
+ * itg_heff2_apply (the Davidson diagonal preconditioner), O(chi^2) work. */
+ITG_API int itg_heff2_diag(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d,
+                           int64_t wL, int64_t wM, int64_t wR,
+                           const double* L, const double* W1, const double* W2, const double* R,
+                           double* diag);
+
 /* Lowest eigenpair of the two-site effective Hamiltonian by Davidson with the
  * diagonal preconditioner.  psi (device) is the start vector and is overwritten
  * with the normalised eigenvector; energy (host) receives the eigenvalue.

@@ -18,20 +18,7 @@
 #include <algorithm>
 #include <sstream>
 
-struct ContractPlan {
-  int64_t M = 0, N = 0, K = 0;
-  int64_t* tables = nullptr;  // offAm[M] offCm[M] offBn[N] offCn[N] offAk[K] offBk[K]
-  bool a_kmaj = false, b_kmaj = false;
-  const int64_t* offAm() const { return tables; }
-  const int64_t* offCm() const { return tables + M; }
-  const int64_t* offBn() const { return tables + 2 * M; }
-  const int64_t* offCn() const { return tables + 2 * M + N; }
-  const int64_t* offAk() const { return tables + 2 * M + 2 * N; }
-  const int64_t* offBk() const { return tables + 2 * M + 2 * N + K; }
-  ~ContractPlan() {
-    if (tables) cudaFree(tables);
-  }
-};
+
 
 void itg_release_plans(itg_handle* h) { h->plans.clear(); }
 
@@ -218,9 +205,16 @@ struct ModeInfo {
   int64_t strA, strB, strC;  // -1 when absent
 };
 
-int build_plan(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA, int rankB,
-               const int64_t* dimsB, const int32_t* modesB, int rankC, const int64_t* dimsC,
-               const int32_t* modesC, std::shared_ptr<ContractPlan>& out) {
+}  // namespace
+
+namespace itg {
+
+// Host half of planning: validates the modes and fills the offset tables
+// (offAm, offCm, offBn, offCn, offAk, offBk) into `tab`; no device work.
+int plan_tables_host(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA,
+                     int rankB, const int64_t* dimsB, const int32_t* modesB, int rankC,
+                     const int64_t* dimsC, const int32_t* modesC, ContractPlan& pl,
+                     std::vector<int64_t>& tab) {
   auto strides = [](int r, const int64_t* d, int64_t* s) {
     int64_t x = 1;
     for (int i = 0; i < r; ++i) { s[i] = x; x *= d[i]; }
@@ -280,7 +274,7 @@ int build_plan(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* mo
     std::stable_sort(contr.begin(), contr.end(),
                      [](const ModeInfo& x, const ModeInfo& y) { return x.strB < y.strB; });
 
-  auto p = std::make_shared<ContractPlan>();
+  ContractPlan* p = &pl;
   auto prod = [](const std::vector<ModeInfo>& v) {
     int64_t x = 1;
     for (auto& m : v) x *= m.dim;
@@ -290,7 +284,7 @@ int build_plan(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* mo
   p->N = prod(freeB);
   p->K = prod(contr);
   // Tables.
-  std::vector<int64_t> tab(2 * p->M + 2 * p->N + 2 * p->K);
+  tab.assign(2 * p->M + 2 * p->N + 2 * p->K, 0);
   auto fill = [](const std::vector<ModeInfo>& v, int64_t count, int which1, int which2,
                  int64_t* o1, int64_t* o2) {
     // which: 0 = strA, 1 = strB, 2 = strC
@@ -317,6 +311,20 @@ int build_plan(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* mo
   fill(contr, p->K, 0, 1, t + 2 * p->M + 2 * p->N, t + 2 * p->M + 2 * p->N + p->K);
   p->a_kmaj = p->K > 1 && (t[2 * p->M + 2 * p->N + 1] - t[2 * p->M + 2 * p->N] == 1);
   p->b_kmaj = p->K > 1 && (t[2 * p->M + 2 * p->N + p->K + 1] - t[2 * p->M + 2 * p->N + p->K] == 1);
+  return ITG_OK;
+}
+
+}  // namespace itg
+
+namespace {
+
+int build_plan(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA, int rankB,
+               const int64_t* dimsB, const int32_t* modesB, int rankC, const int64_t* dimsC,
+               const int32_t* modesC, std::shared_ptr<ContractPlan>& out) {
+  auto p = std::make_shared<ContractPlan>();
+  std::vector<int64_t> tab;
+  ITG_TRY(itg::plan_tables_host(h, rankA, dimsA, modesA, rankB, dimsB, modesB, rankC, dimsC, modesC,
+                                *p, tab));
   if (!tab.empty()) {
     cudaError_t e = cudaMalloc((void**)&p->tables, tab.size() * sizeof(int64_t));
     if (e != cudaSuccess)

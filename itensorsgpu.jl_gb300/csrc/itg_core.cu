@@ -44,7 +44,7 @@ extern "C" int itg_create(int device, itg_handle** out) {
   itg_handle* h = new itg_handle();
   h->device = device;
   cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device);
-  if (cudaMallocHost((void**)&h->pinned, 64 * sizeof(double)) != cudaSuccess) {
+  if (cudaMallocHost((void**)&h->pinned, ITG_PINNED_DOUBLES * sizeof(double)) != cudaSuccess) {
     delete h;
     return ITG_ERR_ALLOC;
   }
@@ -66,6 +66,7 @@ extern "C" int itg_destroy(itg_handle* h) {
   cudaStreamSynchronize(h->stream);
   itg_release_plans(h);
   if (h->scratch) cudaFree(h->scratch);
+  if (h->split_ws) cudaFree(h->split_ws);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->dev_status) cudaFree(h->dev_status);
   delete h;

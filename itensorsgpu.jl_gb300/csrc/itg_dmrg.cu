@@ -238,15 +238,31 @@ __global__ void k_precond(int64_t n, const double* __restrict__ r, const double*
   }
 }
 
-// y = a*x + b*y with host scalars (x, y length n)
+// y = a*x + b*y with host scalars (x, y length n); b == 0 ignores y's old contents.
 __global__ void k_lincomb(int64_t n, double a, const double* __restrict__ x, double b,
                           double* __restrict__ y) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = a * x[i] + b * y[i];
+    y[i] = (b == 0.0) ? a * x[i] : a * x[i] + b * y[i];
 }
 
 }  // namespace
+
+namespace itg {
+// Pieces of the H_eff chain for entry points that bring their own buffers.
+int heff_form_weff(itg_handle* h, int64_t d, int64_t wL, int64_t wM, int64_t wR, const double* W1,
+                   const double* W2, double* Weff) {
+  HeffDims D{1, 1, d, wL, wM, wR};
+  return form_weff(h, D, W1, W2, Weff);
+}
+int heff_mid(itg_handle* h, int64_t rows, int nc, int nj, const double* T1, const double* Weff,
+             double* T3) {
+  k_heff_mid<<<itg_blocks_for(rows, 256, h->num_sms * 8), 256, sizeof(double) * nc * nj, h->stream>>>(
+      T1, Weff, T3, rows, nc, nj);
+  ITG_CHECK_LAUNCH(h);
+  return ITG_OK;
+}
+}  // namespace itg
 
 extern "C" int itg_heff2_apply(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d, int64_t wL,
                                int64_t wM, int64_t wR, const double* L, const double* W1,
@@ -260,6 +276,19 @@ extern "C" int itg_heff2_apply(itg_handle* h, int64_t chiL, int64_t chiR, int64_
   HeffWork w = heff_carve(D, (char*)h->scratch);
   ITG_TRY(form_weff(h, D, W1, W2, w.Weff));
   return heff_apply(h, D, L, R, psi, out, w, precision);
+}
+
+extern "C" int itg_heff2_diag(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d, int64_t wL,
+                              int64_t wM, int64_t wR, const double* L, const double* W1,
+                              const double* W2, const double* R, double* diag) {
+  if (!h || !L || !W1 || !W2 || !R || !diag) return ITG_ERR_INVALID;
+  HeffDims D{chiL, chiR, d, wL, wM, wR};
+  ITG_TRY(heff_validate(h, D));
+  const int nwd = (int)(D.wL * D.d * D.d * D.wR);
+  k_heff_diag<<<itg_blocks_for(D.n(), 256, h->num_sms * 8), 256, sizeof(double) * nwd, h->stream>>>(
+      L, W1, W2, R, chiL, chiR, (int)d, (int)wL, (int)wM, (int)wR, diag);
+  ITG_CHECK_LAUNCH(h);
+  return ITG_OK;
 }
 
 extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d, int64_t wL,

@@ -307,6 +307,26 @@ __global__ void k_col_norms(const double* __restrict__ W, int64_t m, double* __r
   }
 }
 
+// Rescale every column of V (n x ncols) to unit norm: the accumulated plane
+// rotations drift column norms by O(sweeps * n * eps).
+__global__ void k_unit_cols(double* __restrict__ V, int64_t n) {
+  __shared__ double sh[32];
+  __shared__ double f;
+  double* v = V + (int64_t)blockIdx.x * n;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s = fma(v[i], v[i], s);
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh[i];
+    f = t > 0.0 ? 1.0 / sqrt(t) : 1.0;
+  }
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) v[i] *= f;
+}
+
 // Stable descending rank of each value (ties by index): order[rank] = j.
 __global__ void k_rank_desc(const double* __restrict__ sig, int n, double shift,
                             int* __restrict__ order, double* __restrict__ S,
@@ -453,6 +473,7 @@ extern "C" int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* 
   int sweeps = 0;
   int st = jacobi_run(h, W, mm, nn, Vw, flag, &sweeps);
   if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED) return st;
+  k_unit_cols<<<(unsigned)nn, 256, 0, h->stream>>>(Vw, nn);
   k_col_norms<<<(unsigned)nn, 256, 0, h->stream>>>(W, mm, sig);
   k_rank_desc<<<itg_blocks_for(nn, 256, 1024), 256, 0, h->stream>>>(sig, (int)nn, 0.0, order, S, P, 1);
   ITG_CHECK_LAUNCH(h);
@@ -511,6 +532,7 @@ extern "C" int itg_eigh_trunc(itg_handle* h, int64_t n, const double* A, int64_t
   int sweeps = 0;
   int st = jacobi_run(h, W, n, n, Vw, flag, &sweeps);
   if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED) return st;
+  k_unit_cols<<<(unsigned)n, 256, 0, h->stream>>>(Vw, n);
   k_col_norms<<<(unsigned)n, 256, 0, h->stream>>>(W, n, sig);
   k_rank_desc<<<itg_blocks_for(n, 256, 1024), 256, 0, h->stream>>>(sig, (int)n, shift, order, D, P, 0);
   ITG_CHECK_LAUNCH(h);

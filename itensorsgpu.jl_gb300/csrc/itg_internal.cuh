@@ -15,9 +15,24 @@
 #include "../../include/itg.h"
 
 #define ITG_MAX_RANK 16
+#define ITG_PINNED_DOUBLES 4096  // host staging for small results (Davidson subspace <= 32x32)
 
-struct ContractPlan;  // itg_contract.cu
-struct SplitPlan;     // itg_split.cu
+// A lowered contraction C[m,n] = sum_k A[m,k] B[k,n] with every operand
+// addressed through offset tables (see itg_contract.cu).
+struct ContractPlan {
+  int64_t M = 0, N = 0, K = 0;
+  int64_t* tables = nullptr;  // offAm[M] offCm[M] offBn[N] offCn[N] offAk[K] offBk[K]
+  bool a_kmaj = false, b_kmaj = false;
+  const int64_t* offAm() const { return tables; }
+  const int64_t* offCm() const { return tables + M; }
+  const int64_t* offBn() const { return tables + 2 * M; }
+  const int64_t* offCn() const { return tables + 2 * M + N; }
+  const int64_t* offAk() const { return tables + 2 * M + 2 * N; }
+  const int64_t* offBk() const { return tables + 2 * M + 2 * N + K; }
+  ~ContractPlan() {
+    if (tables) cudaFree(tables);
+  }
+};
 
 struct itg_handle {
   int device = 0;
@@ -29,6 +44,11 @@ struct itg_handle {
   // kernels using it were enqueued before the new ones.
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
+  // Workspace of the split-precision path (slices, exponents, accumulators);
+  // separate from `scratch` because split contractions run inside callers
+  // (the H_eff chain, Davidson) that hold regions of `scratch`.
+  void* split_ws = nullptr;
+  size_t split_ws_bytes = 0;
   // Small pinned host buffer for scalar results (dot, truncation outputs).
   double* pinned = nullptr;
   // Persistent device buffers of the contraction plans, keyed by shape.

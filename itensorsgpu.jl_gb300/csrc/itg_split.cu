@@ -1,15 +1,737 @@
-// Split-precision contraction path (ITG_PREC_SPLIT).
+// Split-precision contraction path (ITG_PREC_SPLIT): FP64 GEMM through exact
+// integer products of bf16 slices on the tcgen05 tensor cores.
+//
+// Method (error-free splitting after Ozaki, Ogita, Oishi & Rump, "Error-free
+// transformations of matrix multiplication by using fast routines of matrix
+// multiplication and its applications", Numer. Algorithms 59 (2012); integer
+// slices with exact low-precision accumulation as in Ootomo, Ozaki & Yokota,
+// "DGEMM on integer matrix multiplication unit", IJHPCA 2024):
+//
+//   Row m of A is scaled by 2^-e_m (|A[m,k]| < 2^e_m) and written in balanced
+//   base-2^7 digits:  A[m,k] ~ 2^e_m sum_{p<S} a_p[m,k] 2^-7(p+1)
+//   with |a_0| <= 128 and |a_p| <= 64 (p >= 1); every digit is an exact bf16.
+//   Column n of B likewise with exponent f_n and digits b_q.
+//   C[m,n] ~ 2^(e_m+f_n-14) sum_{L<S} 2^-7L sum_{p+q=L} (a_p b_q)[m,n].
+//
+// Each a_p b_q product is an integer GEMM run by tcgen05.mma (kind::f16, bf16
+// in, FP32 accumulate in TMEM).  Products of one level L are accumulated in a
+// TMEM buffer only while the sum of |a||b| bounds stays <= 2^24, so every FP32
+// partial sum is an exact integer.  The buffer is then drained by the
+// epilogue warps into an exact int64 fixed-point accumulator (2^F scaling),
+// while the MMA warp fills the other TMEM buffer.  The final drain converts the
+// int64 accumulator to FP64 with integer instructions (round to nearest) and
+// scatters C through the contraction plan's offset tables.  No FP64 arithmetic
+// runs in the inner loops (GB300's FP64 rate is a small fraction of its
+// tensor rate).
+//
+// Kernel roles (one CTA per 128 x BN output tile, 6 warps):
+//   warp 0    TMA producer: A/B slice tiles (64 bf16 of K per stage, 128B
+//             swizzle) into a 4-stage shared-memory ring, mbarrier complete_tx
+//   warp 1    TMEM allocator and single-thread tcgen05.mma issuer
+//   warps 2-5 TMEM drain / epilogue (warp w reads TMEM lanes 32*(w%4)..+31)
+// Every mbarrier wait is bounded (globaltimer, ~4 s); on timeout the kernel
+// records ITG_ERR_TIMEOUT, stops issuing work, waits (bounded) for its own
+// copies and MMAs, frees TMEM and returns.
 #include "itg_internal.cuh"
 
-struct ContractPlan;
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+
+
+
+namespace split {
+
+constexpr int S_SLICES = 7;    // digits per operand (7 bits each)
+constexpr int BM = 128;        // tile rows (TMEM lanes)
+constexpr int BK = 64;         // K per pipeline stage (128 bytes of bf16)
+constexpr int STAGES = 4;
+constexpr int NUM_THREADS = 192;
+constexpr uint64_t WAIT_NS = 4000000000ull;  // bounded waits: 4 s
+
+// ------------------------------------------------------------ PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait; returns false (and records the timeout) when it runs out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
+                                          volatile int* abort_flag) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 63) == 63) {
+      if (*abort_flag) return false;
+      if (globaltimer() - t0 > WAIT_NS) {
+        atomicExch(err, ITG_ERR_TIMEOUT);
+        *abort_flag = 1;
+        return false;
+      }
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                            uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_ld_32x32b_x32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// core groups 1024 bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;            // leading-dimension offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride-dimension offset
+  d |= (uint64_t)1 << 46;            // version
+  d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Digit magnitude bounds: 2^7 for the leading digit, 2^6 for the others.
+__host__ __device__ __forceinline__ int digit_log2(int p) { return p == 0 ? 7 : 6; }
+
+// Exact-accumulation schedule shared by every role.  Items are
+// (level L, pair p, k-block kb) in level-major order; a group is a run of
+// items of one level whose summed |product| bound stays <= 2^24.
+struct Sched {
+  int S, nkb;
+  // iteration state
+  int L, p, kb;
+  int group;     // group index of the current item
+  int64_t used;  // bound used in the current group (log-domain sums as integers)
+  bool first_in_group;
+  __host__ __device__ void begin(int S_, int nkb_) {
+    S = S_;
+    nkb = nkb_;
+    L = 0;
+    p = 0;
+    kb = 0;
+    group = 0;
+    used = 0;
+    first_in_group = true;
+    used = cost();
+  }
+  __host__ __device__ int q() const { return L - p; }
+  __host__ __device__ int64_t cost() const {
+    return (int64_t)BK << (digit_log2(p) + digit_log2(L - p));
+  }
+  __host__ __device__ bool valid() const { return L < S; }
+  // Advance; reports whether the item just finished closed its group.
+  __host__ __device__ bool advance() {
+    int nL = L, np = p, nkb2 = kb + 1;
+    if (nkb2 == nkb) {
+      nkb2 = 0;
+      np = p + 1;
+      if (np > L) {
+        np = 0;
+        nL = L + 1;
+      }
+    }
+    bool closes;
+    if (nL >= S) {
+      closes = true;
+    } else if (nL != L) {
+      closes = true;
+    } else {
+      int64_t c = (int64_t)BK << (digit_log2(np) + digit_log2(nL - np));
+      closes = used + c > ((int64_t)1 << 24);
+    }
+    L = nL;
+    p = np;
+    kb = nkb2;
+    if (closes) {
+      group++;
+      used = 0;
+      first_in_group = true;
+    } else {
+      first_in_group = false;
+    }
+    if (L < S) used += cost();
+    return closes;
+  }
+};
+
+struct GemmArgs {
+  int64_t M, N, K;
+  int Mpad, Npad, Kpad, nkb, S, F, tiles_n;
+  const int* eA;
+  const int* eB;
+  const int64_t* offCm;
+  const int64_t* offCn;
+  double* C;
+  double alpha, beta;
+  long long* acc;
+  int* err;
+};
+
+// v * 2^exp2 rounded to nearest even, built with integer instructions.
+__device__ __forceinline__ double i64_to_double_scaled(long long v, int exp2) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
+  unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+  const int top = 63 - __clzll((long long)u);
+  unsigned long long mant;
+  int e2 = top + exp2;
+  if (top <= 52) {
+    mant = u << (52 - top);
+  } else {
+    const int sh = top - 52;
+    const unsigned long long rem = u & ((1ull << sh) - 1);
+    const unsigned long long half = 1ull << (sh - 1);
+    mant = u >> sh;
+    if (rem > half || (rem == half && (mant & 1ull))) {
+      mant++;
+      if (mant >> 53) {
+        mant >>= 1;
+        e2++;
+      }
+    }
+  }
+  const int be = e2 + 1023;
+  if (be <= 0) return __longlong_as_double((long long)sgn);
+  if (be >= 2047) return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ull));
+  return __longlong_as_double(
+      (long long)(sgn | ((unsigned long long)be << 52) | (mant & ((1ull << 52) - 1))));
+}
+
+template <int BN>
+struct Smem {
+  static constexpr int A_BYTES = BM * BK * 2;
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int TOTAL = 1024 /*align slack*/ + STAGES * STAGE_BYTES + 256;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+             GemmArgs args) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* stage_mem = base;
+  uint64_t* bars = (uint64_t*)(base + STAGES * Smem<BN>::STAGE_BYTES);
+  uint64_t* full = bars;                 // [STAGES]
+  uint64_t* empty = bars + STAGES;       // [STAGES]
+  uint64_t* acc_full = bars + 2 * STAGES;      // [2]
+  uint64_t* acc_empty = bars + 2 * STAGES + 2; // [2]
+  uint64_t* done_bar = bars + 2 * STAGES + 4;  // [1]
+  volatile int* abort_flag = (volatile int*)(bars + 2 * STAGES + 5);
+  uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 6);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = blockIdx.x;
+  const int m_tile = tile / args.tiles_n, n_tile = tile - m_tile * args.tiles_n;
+  const int m0 = m_tile * BM, n0 = n_tile * BN;
+  constexpr uint32_t TMEM_COLS = 2 * BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 4);
+    }
+    mbar_init(done_bar, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      Sched sc;
+      sc.begin(args.S, args.nkb);
+      int it = 0;
+      while (sc.valid() && !*abort_flag) {
+        const int s = it % STAGES;
+        if (it >= STAGES) {
+          if (!mbar_wait(&empty[s], ((it / STAGES) - 1) & 1, args.err, abort_flag)) break;
+        }
+        uint8_t* sa = stage_mem + s * Smem<BN>::STAGE_BYTES;
+        uint8_t* sb = sa + Smem<BN>::A_BYTES;
+        mbar_arrive_expect_tx(&full[s], Smem<BN>::STAGE_BYTES);
+        tma_load_2d(sa, &mapA, sc.kb * BK, sc.p * args.Mpad + m0, &full[s]);
+        tma_load_2d(sb, &mapB, sc.kb * BK, sc.q() * args.Npad + n0, &full[s]);
+        sc.advance();
+        ++it;
+      }
+      // make sure no copy is still landing in shared memory when we leave
+      for (int j = std::max(0, it - STAGES); j < it; ++j)
+        mbar_wait(&full[j % STAGES], (j / STAGES) & 1, args.err, abort_flag);
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------- MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16(BM, BN);
+      Sched sc;
+      sc.begin(args.S, args.nkb);
+      int it = 0;
+      bool ok = true;
+      while (sc.valid() && ok) {
+        const int g = sc.group;
+        const int b = g & 1;
+        if (sc.first_in_group && g >= 2) {
+          ok = mbar_wait(&acc_empty[b], ((g >> 1) - 1) & 1, args.err, abort_flag);
+          tc_fence_after();
+          if (!ok) break;
+        }
+        const int s = it % STAGES;
+        ok = mbar_wait(&full[s], (it / STAGES) & 1, args.err, abort_flag);
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t sa = smem_u32(stage_mem + s * Smem<BN>::STAGE_BYTES);
+        const uint32_t sb = sa + Smem<BN>::A_BYTES;
+        const uint64_t ad = sdesc_sw128(sa), bd = sdesc_sw128(sb);
+        const uint32_t tmem_d = tmem_base + (uint32_t)(b * BN);
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk) {
+          const uint32_t accum = (sc.first_in_group && kk == 0) ? 0u : 1u;
+          tc_mma_bf16(tmem_d, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), idesc, accum);
+        }
+        tc_commit(&empty[s]);
+        const bool closes = sc.advance();
+        if (closes) tc_commit(&acc_full[b]);
+        ++it;
+      }
+      // all MMAs issued by this thread complete before TMEM is released
+      tc_commit(done_bar);
+      mbar_wait(done_bar, 0, args.err, abort_flag);
+    }
+  } else {
+    // ------------------------------------------------------ drain/epilogue
+    const int quarter = warp & 3;
+    const int row = quarter * 32 + lane;
+    const int64_t m = (int64_t)m0 + row;
+    const int em = (m < args.M) ? args.eA[m] - 1022 : 0;
+    long long* acc = args.acc + (size_t)tile * BN * BM;
+    Sched sc;
+    sc.begin(args.S, args.nkb);
+    int g_done = -1;
+    bool first_drain = true;
+    while (sc.valid()) {
+      // walk to the end of the current group
+      const int L = sc.L;
+      const int g = sc.group;
+      bool last;
+      for (;;) {
+        const bool closes = sc.advance();
+        if (closes) break;
+      }
+      last = !sc.valid();
+      const int b = g & 1;
+      if (!mbar_wait(&acc_full[b], (g >> 1) & 1, args.err, abort_flag)) break;
+      tc_fence_after();
+      const int sh = args.F - 7 * L;
+      const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN);
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t r[32];
+        tc_ld_32x32b_x32(tbase + (uint32_t)c0, r);
+        if (last) {
+          // final drain: combine, convert to FP64, scatter through the plan
+          if (m < args.M) {
+            const int64_t cm = args.offCm[m];
+#pragma unroll 4
+            for (int j = 0; j < 32; ++j) {
+              const int64_t n = (int64_t)n0 + c0 + j;
+              if (n >= args.N) break;
+              long long t = (long long)__float2int_rn(__uint_as_float(r[j]));
+              t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
+              const size_t idx = (size_t)(c0 + j) * BM + row;
+              const long long tot = first_drain ? t : acc[idx] + t;
+              const int fn = args.eB[n] - 1022;
+              double v = i64_to_double_scaled(tot, em + fn - 14 - args.F);
+              if (args.alpha != 1.0) v *= args.alpha;
+              double* cp = args.C + cm + args.offCn[n];
+              if (args.beta != 0.0) v = fma(args.beta, *cp, v);
+              *cp = v;
+            }
+          }
+        } else {
+#pragma unroll 8
+          for (int j = 0; j < 32; ++j) {
+            long long t = (long long)__float2int_rn(__uint_as_float(r[j]));
+            t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
+            const size_t idx = (size_t)(c0 + j) * BM + row;
+            acc[idx] = first_drain ? t : acc[idx] + t;
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[b]);
+      first_drain = false;
+      g_done = g;
+      if (*abort_flag) break;
+    }
+    (void)g_done;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "r"(TMEM_COLS));
+  }
+}
+
+// ----------------------------------------------------------- slicing
+// Exponent field (11 bits) of max_k |X[r,k]| for every row r < R.
+template <bool KMAJ>
+__global__ void k_row_expfield(const double* __restrict__ X, const int64_t* __restrict__ offR,
+                               const int64_t* __restrict__ offK, int64_t R, int64_t K,
+                               int* __restrict__ efield) {
+  if (KMAJ) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); r < R; r += warps) {
+      const double* x = X + offR[r];
+      unsigned long long mx = 0;
+      for (int64_t k = lane; k < K; k += 32) {
+        unsigned long long b = (unsigned long long)__double_as_longlong(x[offK[k]]) & 0x7FFFFFFFFFFFFFFFull;
+        mx = b > mx ? b : mx;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = y > mx ? y : mx;
+      }
+      if (lane == 0) efield[r] = (int)((mx >> 52) & 0x7FF);
+    }
+  } else {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < R;
+         r += (int64_t)gridDim.x * blockDim.x) {
+      const double* x = X + offR[r];
+      unsigned long long mx = 0;
+      for (int64_t k = 0; k < K; ++k) {
+        unsigned long long b = (unsigned long long)__double_as_longlong(x[offK[k]]) & 0x7FFFFFFFFFFFFFFFull;
+        mx = b > mx ? b : mx;
+      }
+      efield[r] = (int)((mx >> 52) & 0x7FF);
+    }
+  }
+}
+
+// Balanced base-2^7 digits of X[r,k] * 2^-e_r rounded to 7S fractional bits.
+template <int S>
+__device__ __forceinline__ void make_digits(double x, int efield_r, int (&d)[S]) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const bool neg = bits >> 63;
+  const int E = (int)((bits >> 52) & 0x7FF);
+  unsigned long long M = bits & ((1ull << 52) - 1);
+  if (E) M |= 1ull << 52;
+  const int Ee = E ? E : 1;
+  const int er = efield_r - 1022;
+  const int sh = Ee - 1075 - er + 7 * S;
+  unsigned long long Y;
+  if (M == 0 || E == 2047) {
+    Y = 0;
+  } else if (sh >= 0) {
+    Y = M << sh;
+  } else if (sh <= -60) {
+    Y = 0;
+  } else {
+    Y = (M >> (-sh)) + ((M >> (-sh - 1)) & 1ull);
+  }
+#pragma unroll
+  for (int p = S - 1; p >= 1; --p) {
+    int lo = (int)(Y & 127ull);
+    if (lo >= 64) lo -= 128;
+    d[p] = lo;
+    Y = (Y - (unsigned long long)(long long)lo) >> 7;
+  }
+  d[0] = (int)Y;
+  if (neg) {
+#pragma unroll
+    for (int p = 0; p < S; ++p) d[p] = -d[p];
+  }
+}
+
+// out[p][r][k] (bf16, k contiguous, padded to Rpad x Kpad) for the gathered X.
+template <bool KMAJ, int S>
+__global__ void __launch_bounds__(256)
+k_make_slices(const double* __restrict__ X, const int64_t* __restrict__ offR,
+              const int64_t* __restrict__ offK, int64_t R, int64_t K, int64_t Rpad, int64_t Kpad,
+              const int* __restrict__ efield, __nv_bfloat16* __restrict__ out) {
+  __shared__ double tile[32][65];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 64;
+  const int t = threadIdx.x;
+  if (KMAJ) {
+    const int kk = t & 63;
+    const int64_t k = k0 + kk;
+    const int64_t ok = (k < K) ? offK[k] : 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int rr = (t >> 6) + 4 * i;
+      const int64_t r = r0 + rr;
+      tile[rr][kk] = (r < R && k < K) ? X[offR[r] + ok] : 0.0;
+    }
+  } else {
+    const int rr = t & 31;
+    const int64_t r = r0 + rr;
+    const int64_t orr = (r < R) ? offR[r] : 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int kk = (t >> 5) + 8 * i;
+      const int64_t k = k0 + kk;
+      tile[rr][kk] = (r < R && k < K) ? X[orr + offK[k]] : 0.0;
+    }
+  }
+  __syncthreads();
+  const int kk = t & 63;
+  const size_t plane = (size_t)Rpad * Kpad;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int rr = (t >> 6) + 4 * i;
+    const int64_t r = r0 + rr;
+    int d[S];
+    const int ef = (r < R) ? efield[r] : 0;
+    make_digits<S>(tile[rr][kk], ef, d);
+    const size_t o = (size_t)r * Kpad + k0 + kk;
+#pragma unroll
+    for (int p = 0; p < S; ++p) out[(size_t)p * plane + o] = __float2bfloat16_rn((float)d[p]);
+  }
+}
+
+// --------------------------------------------------------------- host
+PFN_cuTensorMapEncodeTiled_v12000 get_encode(itg_handle* h) {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  (void)h;
+  return fn;
+}
+
+int make_map(itg_handle* h, CUtensorMap* map, void* base, int64_t inner, int64_t outer, int box_rows) {
+  auto enc = get_encode(h);
+  if (!enc) return itg_fail(h, ITG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+  cuuint64_t strides[1] = {(cuuint64_t)(inner * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return itg_fail(h, ITG_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return ITG_OK;
+}
+
+int ws_reserve(itg_handle* h, size_t bytes);
+
+template <int BN>
+int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
+        double alpha, double beta) {
+  constexpr int S = S_SLICES;
+  const int64_t Mpad = (p.M + BM - 1) / BM * BM;
+  const int64_t Npad = (p.N + BN - 1) / BN * BN;
+  const int64_t Kpad = (p.K + BK - 1) / BK * BK;
+  if (Mpad * S > (int64_t)INT32_MAX || Npad * S > (int64_t)INT32_MAX || Kpad > (int64_t)INT32_MAX)
+    return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: problem too large");
+  const int64_t tiles = (Mpad / BM) * (Npad / BN);
+  // F: fixed-point fraction bits of the int64 accumulator (keeps |acc| < 2^62).
+  int lk = 0;
+  while (((int64_t)1 << lk) < p.K) ++lk;
+  const int F = 62 - 15 - lk;
+  if (F < 8) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: contraction depth too large");
+  size_t off = 0;
+  auto take = [&](size_t b) { size_t o = off; off += itg_align256(b); return o; };
+  const size_t oEA = take(sizeof(int) * Mpad), oEB = take(sizeof(int) * Npad);
+  const size_t oSA = take((size_t)2 * S * Mpad * Kpad), oSB = take((size_t)2 * S * Npad * Kpad);
+  const size_t oAcc = take(sizeof(long long) * (size_t)tiles * BN * BM);
+  const size_t oErr = take(sizeof(int));
+  ITG_TRY(ws_reserve(h, off));
+  char* ws = (char*)h->split_ws;
+  int* eA = (int*)(ws + oEA);
+  int* eB = (int*)(ws + oEB);
+  __nv_bfloat16* sA = (__nv_bfloat16*)(ws + oSA);
+  __nv_bfloat16* sB = (__nv_bfloat16*)(ws + oSB);
+  long long* acc = (long long*)(ws + oAcc);
+  int* err = (int*)(ws + oErr);
+  ITG_CUDA(h, cudaMemsetAsync(err, 0, sizeof(int), h->stream));
+  // exponents
+  {
+    const int thr = 256;
+    if (p.a_kmaj)
+      k_row_expfield<true><<<itg_blocks_for(p.M, thr / 32, h->num_sms * 16), thr, 0, h->stream>>>(
+          A, p.offAm(), p.offAk(), p.M, p.K, eA);
+    else
+      k_row_expfield<false><<<itg_blocks_for(p.M, thr, h->num_sms * 16), thr, 0, h->stream>>>(
+          A, p.offAm(), p.offAk(), p.M, p.K, eA);
+    if (p.b_kmaj)
+      k_row_expfield<true><<<itg_blocks_for(p.N, thr / 32, h->num_sms * 16), thr, 0, h->stream>>>(
+          B, p.offBn(), p.offBk(), p.N, p.K, eB);
+    else
+      k_row_expfield<false><<<itg_blocks_for(p.N, thr, h->num_sms * 16), thr, 0, h->stream>>>(
+          B, p.offBn(), p.offBk(), p.N, p.K, eB);
+    ITG_CHECK_LAUNCH(h);
+  }
+  // slices
+  {
+    dim3 gA((unsigned)(Kpad / 64), (unsigned)(Mpad / 32)), gB((unsigned)(Kpad / 64), (unsigned)(Npad / 32));
+    if (gA.y > 65535 || gB.y > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: too many rows");
+    if (p.a_kmaj)
+      k_make_slices<true, S><<<gA, 256, 0, h->stream>>>(A, p.offAm(), p.offAk(), p.M, p.K, Mpad, Kpad, eA, sA);
+    else
+      k_make_slices<false, S><<<gA, 256, 0, h->stream>>>(A, p.offAm(), p.offAk(), p.M, p.K, Mpad, Kpad, eA, sA);
+    if (p.b_kmaj)
+      k_make_slices<true, S><<<gB, 256, 0, h->stream>>>(B, p.offBn(), p.offBk(), p.N, p.K, Npad, Kpad, eB, sB);
+    else
+      k_make_slices<false, S><<<gB, 256, 0, h->stream>>>(B, p.offBn(), p.offBk(), p.N, p.K, Npad, Kpad, eB, sB);
+    ITG_CHECK_LAUNCH(h);
+  }
+  CUtensorMap mA, mB;
+  ITG_TRY(make_map(h, &mA, sA, Kpad, Mpad * S, BM));
+  ITG_TRY(make_map(h, &mB, sB, Kpad, Npad * S, BN));
+  GemmArgs a;
+  a.M = p.M;
+  a.N = p.N;
+  a.K = p.K;
+  a.Mpad = (int)Mpad;
+  a.Npad = (int)Npad;
+  a.Kpad = (int)Kpad;
+  a.nkb = (int)(Kpad / BK);
+  a.S = S;
+  a.F = F;
+  a.tiles_n = (int)(Npad / BN);
+  a.eA = eA;
+  a.eB = eB;
+  a.offCm = p.offCm();
+  a.offCn = p.offCn();
+  a.C = C;
+  a.alpha = alpha;
+  a.beta = beta;
+  a.acc = acc;
+  a.err = err;
+  static bool attr = false;
+  if (!attr) {
+    ITG_CUDA(h, cudaFuncSetAttribute(k_split_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     Smem<BN>::TOTAL));
+    attr = true;
+  }
+  if (tiles > (int64_t)INT32_MAX) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: too many tiles");
+  k_split_gemm<BN><<<(unsigned)tiles, NUM_THREADS, Smem<BN>::TOTAL, h->stream>>>(mA, mB, a);
+  ITG_CHECK_LAUNCH(h);
+  // surface a device-side timeout on the next synchronising call
+  ITG_CUDA(h, cudaMemcpyAsync(h->dev_status, err, sizeof(int), cudaMemcpyDeviceToDevice, h->stream));
+  return ITG_OK;
+}
+
+int ws_reserve(itg_handle* h, size_t bytes) {
+  if (bytes <= h->split_ws_bytes) return ITG_OK;
+  size_t want = itg_align256(bytes + bytes / 8);
+  if (h->split_ws) {
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    cudaFree(h->split_ws);
+    h->split_ws = nullptr;
+    h->split_ws_bytes = 0;
+  }
+  cudaError_t e = cudaMalloc(&h->split_ws, want);
+  if (e != cudaSuccess) {
+    h->split_ws = nullptr;
+    return itg_fail(h, ITG_ERR_ALLOC, "split workspace of %zu bytes: %s", want, cudaGetErrorString(e));
+  }
+  h->split_ws_bytes = want;
+  return ITG_OK;
+}
+
+}  // namespace split
 
 int itg_split_gemm(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
                    double alpha, double beta) {
-  (void)p; (void)A; (void)B; (void)C; (void)alpha; (void)beta;
-  return itg_fail(h, ITG_ERR_UNSUPPORTED, "split-precision contraction not built yet");
+  if (p.N <= 128) return split::run<128>(h, p, A, B, C, alpha, beta);
+  return split::run<256>(h, p, A, B, C, alpha, beta);
 }
 
 extern "C" double itg_split_error_bound(int64_t K) {
-  (void)K;
-  return 0.0;
+  // |C_split - C|_F <= 4 K 2^-7S (1 + (S+1)/4 * 1.02) |A|_F |B|_F + 2^-52 |C|_F
+  // (digit truncation of both operands plus the dropped levels p + q >= S; the
+  // 2^-52 term, bounded by |A|_F |B|_F, covers the final rounding to FP64).
+  const int S = split::S_SLICES;
+  const double k = (double)(K > 0 ? K : 1);
+  return 4.0 * k * std::ldexp(1.0, -7 * S) * (1.0 + 0.255 * (S + 1)) + std::ldexp(1.0, -52);
 }

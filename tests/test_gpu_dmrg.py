@@ -58,6 +58,56 @@ def test_heff_apply_matches_oracle(gpu, chi, chiR, d, w):
     assert relerr(got, ref) < 1e-12
 
 
+def test_heff_diag_matches_oracle(gpu):
+    from itg import _lib
+    for chi, chiR, d, w in ((5, 7, 2, 5), (24, 24, 2, 5), (33, 17, 3, 4)):
+        L, W1, W2, R, psi = _heff_inputs(chi, chiR, d, w, seed=9 + chi)
+        h = _lib.handle(0)
+        ptr = lambda t: C.c_void_p(t.data_ptr())
+        Ld, W1d, W2d, Rd, pd = map(_dev, (L, W1, W2, R, psi))
+        dg = _dev(np.zeros_like(psi))
+        h.call("itg_heff2_diag", C.c_int64(chi), C.c_int64(chiR), C.c_int64(d), C.c_int64(w),
+               C.c_int64(w), C.c_int64(w), ptr(Ld), ptr(W1d), ptr(W2d), ptr(Rd), ptr(dg))
+        ref = O.flat(O.heff_diag(L, W1, W2, R))
+        assert relerr(dg.cpu().numpy(), ref) < 1e-13
+
+
+def test_davidson_pieces_localised(gpu):
+    """The oracle's Davidson driven by the GPU matvec and GPU diagonal must equal
+    the pure oracle (isolates the device kernels from the solver logic)."""
+    from itg import _lib
+    chi, d, w = 24, 2, 5
+    L, W1, W2, R, psi = _heff_inputs(chi, d=d, w=w, seed=3)
+    L = L + L.transpose(2, 1, 0)
+    R = R + R.transpose(2, 1, 0)
+    W1 = W1 + W1.transpose(0, 2, 1, 3)
+    W2 = W2 + W2.transpose(0, 2, 1, 3)
+    h = _lib.handle(0)
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    Ld, W1d, W2d, Rd = map(_dev, (L, W1, W2, R))
+
+    def gpu_mv(v):
+        x = _dev(O.unflat(v, psi.shape))
+        y = torch_empty_like(x)
+        h.call("itg_heff2_apply", C.c_int64(chi), C.c_int64(chi), C.c_int64(d), C.c_int64(w),
+               C.c_int64(w), C.c_int64(w), ptr(Ld), ptr(W1d), ptr(W2d), ptr(Rd), ptr(x), ptr(y), 0)
+        return y.cpu().numpy()
+
+    dgd = _dev(np.zeros_like(psi))
+    h.call("itg_heff2_diag", C.c_int64(chi), C.c_int64(chi), C.c_int64(d), C.c_int64(w),
+           C.c_int64(w), C.c_int64(w), ptr(Ld), ptr(W1d), ptr(W2d), ptr(Rd), ptr(dgd))
+    mv = lambda v: O.flat(O.heff_apply(L, W1, W2, R, O.unflat(v, psi.shape)))
+    dg = O.flat(O.heff_diag(L, W1, W2, R))
+    th_o, _, _ = O.davidson(mv, O.flat(psi), dg, 3, 2, 1e-14)
+    th_g, _, _ = O.davidson(gpu_mv, O.flat(psi), dgd.cpu().numpy(), 3, 2, 1e-14)
+    assert abs(th_g - th_o) < 1e-10 * abs(th_o)
+
+
+def torch_empty_like(x):
+    import torch
+    return torch.empty_like(x)
+
+
 def test_davidson_matches_oracle(gpu):
     from itg import _lib
     chi, d, w = 24, 2, 5

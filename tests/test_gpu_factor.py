@@ -86,6 +86,23 @@ def test_svd_reconstruction_and_orthogonality(gpu, m, n):
     assert np.abs(R.array(i, j) - Ah).max() < 1e-12 * np.abs(Ah).max()
 
 
+def test_svd_reference_case_isapprox(gpu):
+    """test/test_cuitensor.jl:105-112: A(i,j,k,l) with dims 2,3,4,5, svd(A, (j,l));
+    U U' ~ delta and V V' ~ delta at rtol 1e-14 (Julia isapprox, Frobenius norm)."""
+    I = gpu.Index
+    i, j, k, l = I(2), I(3), I(4), I(5)
+    A = gpu.randomCuITensor(i, j, k, l, seed=77)
+    U, S, V, spec = gpu.svd(A, j, l)
+    R = U * S * V
+    assert np.linalg.norm(R.array(i, j, k, l) - A.array()) <= 1.5e-8 * np.linalg.norm(A.array())
+    for F, ind in ((U, U.inds[-1]), (V, V.inds[-1])):
+        rest = [x for x in F.inds if x != ind]
+        M = F.array(*rest, ind).reshape(-1, ind.dim, order="F")
+        G = M.T @ M
+        d = np.eye(ind.dim)
+        assert np.linalg.norm(G - d) <= 1e-14 * max(np.linalg.norm(G), np.linalg.norm(d))
+
+
 def test_svd_truncation_matches_oracle(gpu):
     rng = np.random.default_rng(5)
     m = n = 256
