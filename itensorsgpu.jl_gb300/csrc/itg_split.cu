@@ -399,7 +399,10 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
       }
       last = !sc.valid();
       const int b = g & 1;
-      if (!mbar_wait(&acc_full[b], (g >> 1) & 1, args.err, abort_flag)) break;
+      // every lane polls; the outcome is made warp-uniform because the TMEM
+      // loads below are .sync.aligned
+      const bool ok_lane = mbar_wait(&acc_full[b], (g >> 1) & 1, args.err, abort_flag);
+      if (!__all_sync(0xffffffffu, ok_lane)) break;
       tc_fence_after();
       const int sh = args.F - 7 * L;
       const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN);
@@ -442,7 +445,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
       if (lane == 0) mbar_arrive(&acc_empty[b]);
       first_drain = false;
       g_done = g;
-      if (*abort_flag) break;
+      if (__any_sync(0xffffffffu, *abort_flag != 0)) break;
     }
     (void)g_done;
   }
