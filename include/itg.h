@@ -232,6 +232,23 @@ ITG_API int itg_heff2_diag(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d,
                            const double* L, const double* W1, const double* W2, const double* R,
                            double* diag);
 
+/* itg_heff2_apply without any device allocation by the library.
+ * No counterpart in the reference.  For callers that cannot let a library call
+ * cudaMalloc: applications that own all device memory through their own
+ * fixed-budget pool (the Julia side keeps ITensors' tensors in the CUDA.jl
+ * pool), or that cannot accept the device synchronisation cudaMalloc may cause.
+ * Intermediates live in one file-scope __device__ array of 4 Mi doubles
+ * (32 MiB) that every GPU loading libitg.so holds until exit; problems needing
+ * more return ITG_ERR_UNSUPPORTED (itg_heff2_apply has no such limit; with
+ * d = 2, w = 5 the limit is about chiL * chiR <= 100000).  FP64 arithmetic
+ * only.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  All
+ * calls share the array, so calls that overlap on the GPU race. */
+ITG_API int itg_heff2_apply_noalloc(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d,
+                                    int64_t wL, int64_t wM, int64_t wR,
+                                    const double* L, const double* W1, const double* W2,
+                                    const double* R, const double* psi, double* out);
+
 /* Lowest eigenpair of the two-site effective Hamiltonian by Davidson with the
  * diagonal preconditioner.  psi (device) is the start vector and is overwritten
  * with the normalised eigenvector; energy (host) receives the eigenvalue.

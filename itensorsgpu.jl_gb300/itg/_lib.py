@@ -96,6 +96,8 @@ SIGNATURES = {
     "itg_matmul": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, _P, _P, _P, C.c_int]),
     "itg_heff2_apply": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                   C.c_int64, _P, _P, _P, _P, _P, _P, C.c_int]),
+    "itg_heff2_apply_noalloc": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                          C.c_int64, C.c_int64, _P, _P, _P, _P, _P, _P]),
     "itg_heff2_diag": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                  C.c_int64, _P, _P, _P, _P, _P]),
     "itg_davidson_heff2": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
