@@ -18,8 +18,10 @@ Printed JSON line (one, from rank 0):
 --impl reference times the reference's CPU path for the same matvec: the
 reference (ITensorsGPU.jl, Julia) cannot run here, so this is the oracle's
 NumPy restatement of ITensors' dense contraction on all host cores.
---precision fp64|split selects the arithmetic of the chi^3 contractions
-("split" = the chosen form, "fp64" = the plain form).
+The headline is the chosen form (--chosen split: chi^3 contractions on the
+tcgen05 tensor cores through exact bf16 digit products); the plain FP64 form is
+measured in the same run and reported under "plain", with the ratio and the
+relative difference of the two outputs.
 """
 from __future__ import annotations
 
@@ -43,6 +45,11 @@ CHI = 1024
 D = 2
 W = 5
 SEED = 1234 + 1
+METRIC = "H_eff matvec contraction TFLOP/s at chi=1024 (two-site DMRG)"
+
+
+def base_config(chi):
+    return {"workload": f"heff2_matvec chi={chi} d=2 w=5", "chi": chi}
 
 
 def flops(chi):
@@ -159,11 +166,11 @@ def run_reference(args):
     v = flops(chi) * args.steps / el / 1e12
     cores = os.cpu_count()
     line = {
-        "impl": "reference", "metric": "H_eff matvec contraction TFLOP/s at chi=1024 (two-site DMRG)",
+        "impl": "reference", "metric": METRIC,
         "value": v, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "replicas",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox N(0,1))",
-        "config": {"workload": f"heff2_matvec chi={chi} d=2 w=5", "chi": chi},
+        "config": base_config(chi),
         "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port",
                          "sample": f"{args.steps} matvecs at chi={chi}, NumPy/OpenBLAS restatement of "
                                    "ITensors' dense contraction (Julia reference unavailable)"},
@@ -179,17 +186,17 @@ def run_gpu(args):
     import torch
     import torch.distributed as dist
     from itg import _lib
-    from itg._lib import PREC_FP64, PREC_SPLIT
+    from itg._lib import (KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_SPLIT_PREP, PREC_FP64,
+                          PREC_SPLIT)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     h = _lib.handle(local)
-    prec = PREC_SPLIT if args.precision == "split" else PREC_FP64
     chi = args.chi
     sh = shapes(chi)
     ptr = lambda t: C.c_void_p(t.data_ptr())
@@ -199,79 +206,101 @@ def run_gpu(args):
         t = torch.empty(_n(v), dtype=torch.float64, device=dev)
         h.call("itg_random_normal", C.c_int64(_n(v)), C.c_uint64(SEED), C.c_uint64(i), ptr(t))
         dev_in[k] = t
-    out = torch.empty(_n(sh["psi"]), dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2
 
-    def matvec(o=out, ins=dev_in):
+    def matvec(prec, o, ins=dev_in):
         h.call("itg_heff2_apply", C.c_int64(chi), C.c_int64(chi), C.c_int64(D), C.c_int64(W),
                C.c_int64(W), C.c_int64(W), ptr(ins["L"]), ptr(ins["W1"]), ptr(ins["W2"]),
                ptr(ins["R"]), ptr(ins["psi"]), ptr(o), prec)
 
-    for _ in range(args.warmup):
-        matvec()
-    torch.cuda.synchronize()
+    def read_prof(kind):
+        ms = C.c_double()
+        n = C.c_int64()
+        h.call("itg_profile_read", int(kind), C.byref(ms), C.byref(n))
+        return ms.value, n.value
 
-    # ---- device-resident timed region: K steps, L2 flushed between steps
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        for s in range(args.steps):
-            flush.zero_()
-            starts[s].record()
-            matvec()
-            ends[s].record()
+    def measure(prec, steps, warmup):
+        out = torch.empty(_n(sh["psi"]), dtype=torch.float64, device=dev)
+        for _ in range(warmup):
+            matvec(prec, out)
         torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
-    t_local = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t_local, op=dist.ReduceOp.MAX)
-    ms = float(t_local.item())
-    clocks = clk.summary()
-    value = flops(chi) * args.steps * world / (ms / 1e3) / 1e12
-
-    # ---- kernel-level timing of the chi^3 contraction kernel (steps 1 and 3)
-    from itg.tensor import _ptr
-    lib_dims = {
-        "s1": ([chi, W, chi], [1, 2, 3], [chi, D, D, chi], [1, 4, 5, 6], [chi, chi, W, D, D], [3, 6, 2, 4, 5]),
-        "s3": ([chi, chi, D, D, W], [3, 6, 7, 9, 10], [chi, W, chi], [6, 10, 11], [chi, D, D, chi], [3, 7, 9, 11]),
-    }
-    T1 = torch.empty(chi * chi * W * D * D, dtype=torch.float64, device=dev)
-
-    def contract(which, A, B, Cout):
-        dA, mA, dB, mB, dC, mC = lib_dims[which]
-        h.call("itg_contract", 0, C.c_double(1.0), ptr(A), len(dA), _lib.i64arr(dA), _lib.i32arr(mA),
-               ptr(B), len(dB), _lib.i64arr(dB), _lib.i32arr(mB), C.c_double(0.0), ptr(Cout), len(dC),
-               _lib.i64arr(dC), _lib.i32arr(mC), prec)
-
-    contract("s1", dev_in["L"], dev_in["psi"], T1)
-    contract("s3", T1, dev_in["R"], out)
-    torch.cuda.synchronize()
-    kt = 0.0
-    nk = max(2, min(args.steps, 5))
-    for _ in range(nk):
-        flush.zero_()
-        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-        e0.record()
-        contract("s1", dev_in["L"], dev_in["psi"], T1)
-        e1.record()
-        contract("s3", T1, dev_in["R"], out)
-        e2.record()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        if world > 1:
+            dist.barrier()
         torch.cuda.synchronize()
-        kt += e0.elapsed_time(e2)
-    kernel_ms = kt / (2 * nk)  # per launch
-    kernel_flop = 40 * chi ** 3  # per launch (both launches are 40 chi^3)
+        h.call("itg_profile", 1)
+        with ClockSampler(local) as clk:
+            for s_ in range(steps):
+                flush.zero_()
+                starts[s_].record()
+                matvec(prec, out)
+                ends[s_].record()
+            torch.cuda.synchronize()
+        h.call("itg_profile", 0)
+        if world > 1:
+            dist.barrier()
+        ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+        t_local = torch.tensor([ms], dtype=torch.float64, device=dev)
+        if world > 1:
+            dist.all_reduce(t_local, op=dist.ReduceOp.MAX)
+        prof = {k: read_prof(k) for k in (KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_SPLIT_PREP)}
+        return float(t_local.item()), clk.summary(), prof, out
 
-    # ---- end to end through the C ABI with host buffers
+    peaks, src = measured_peaks()
+    fp64_peak = None
+    pf = REPO / "profiles" / "fp64_peak.json"
+    if pf.exists():
+        fp64_peak = json.loads(pf.read_text()).get("fp64_tflops")
+    flop_step = flops(chi)
+    gemm_flop_step = 80 * chi ** 3  # the two chi^3 contractions, FP64-equivalent
+
+    results = {}
+    for name, prec in (("split", PREC_SPLIT), ("fp64", PREC_FP64)):
+        if args.precision not in ("both", name):
+            continue
+        steps = args.steps if name == args.chosen else max(2, min(args.steps, args.plain_steps))
+        ms, clocks, prof, out = measure(prec, steps, args.warmup)
+        value = flop_step * steps * world / (ms / 1e3) / 1e12
+        if prec == PREC_SPLIT:
+            kms, kn = prof[KERNEL_GEMM_SPLIT]
+            prep_ms, _ = prof[KERNEL_SPLIT_PREP]
+            slices = 7 * 8 // 2
+            achieved = slices * gemm_flop_step * steps / (kms / 1e3) / 1e12 if kms > 0 else None
+            roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                    "frac": (achieved / peaks["bf16_tflops"]) if achieved else None, "traffic": None,
+                    "peak_source": f"MEASURED_PEAKS.json bf16_tflops (burst, {src})",
+                    "kernel": "k_split_gemm", "launches": kn, "kernel_ms_per_launch": kms / max(kn, 1),
+                    "kernel_flop_per_launch": slices * 40 * chi ** 3,
+                    "flop_note": "bf16 tensor flop executed: 28 digit products x 2MNK per chi^3 contraction",
+                    "fp64_equiv_tflops": gemm_flop_step * steps / (kms / 1e3) / 1e12 if kms > 0 else None,
+                    "prep_ms_per_step": prep_ms / steps,
+                    "gemm_share_of_step": kms / ms}
+        else:
+            kms, kn = prof[KERNEL_GEMM_F64]
+            achieved = gemm_flop_step * steps / (kms / 1e3) / 1e12 if kms > 0 else None
+            roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                    "frac": (achieved / fp64_peak) if (achieved and fp64_peak) else None, "traffic": None,
+                    "peak_source": "profiles/fp64_peak.json (project DFMA probe, measured)",
+                    "kernel": "k_gemm_gather_f64", "launches": kn, "kernel_ms_per_launch": kms / max(kn, 1),
+                    "kernel_flop_per_launch": 40 * chi ** 3, "gemm_share_of_step": kms / ms}
+        results[name] = {"value": value, "ms_per_step": ms / steps, "steps": steps, "clocks": clocks,
+                         "roofline": roof, "out": out}
+
+    chosen = results.get(args.chosen) or next(iter(results.values()))
+    chosen_prec = PREC_SPLIT if (args.chosen in results and args.chosen == "split") else PREC_FP64
+    accuracy = None
+    if "split" in results and "fp64" in results:
+        a, b = results["split"]["out"], results["fp64"]["out"]
+        accuracy = (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item()
+
+    # ---- end to end through the C ABI with host buffers (chosen form)
     host_in = {k: torch.empty(_n(v), dtype=torch.float64).pin_memory() for k, v in sh.items()}
     for k in sh:
         host_in[k].copy_(dev_in[k].cpu())
     host_out = torch.empty(_n(sh["psi"]), dtype=torch.float64).pin_memory()
     scratch_in = {k: torch.empty_like(v) for k, v in dev_in.items()}
+    out_e = torch.empty(_n(sh["psi"]), dtype=torch.float64, device=dev)
     h2d = sum(8 * _n(v) for v in sh.values())
     d2h = 8 * _n(sh["psi"])
 
@@ -279,60 +308,50 @@ def run_gpu(args):
         for k in sh:
             h.call("itg_memcpy_h2d", ptr(scratch_in[k]), C.c_void_p(host_in[k].data_ptr()),
                    C.c_size_t(8 * _n(sh[k])))
-        matvec(out, scratch_in)
-        h.call("itg_memcpy_d2h", C.c_void_p(host_out.data_ptr()), ptr(out), C.c_size_t(d2h))
+        matvec(chosen_prec, out_e, scratch_in)
+        h.call("itg_memcpy_d2h", C.c_void_p(host_out.data_ptr()), ptr(out_e), C.c_size_t(d2h))
 
     e2e_step()
     torch.cuda.synchronize()
-    ke = max(2, min(args.steps, 5))
+    ke = max(3, min(args.steps, 10))
     t0 = time.perf_counter()
     for _ in range(ke):
         e2e_step()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / ke
-    e2e_value = flops(chi) / e2e_s / 1e12
-
-    # parity spot check of the measured output against the oracle at this size
-    # is done in the tests; here only a finite-value guard.
-    finite = bool(torch.isfinite(out).all().item())
+    e2e_value = flop_step / e2e_s / 1e12
+    finite = bool(torch.isfinite(chosen["out"]).all().item())
 
     if rank != 0:
         return 0
-    peaks, src = measured_peaks()
-    fp64_peak = None
-    pf = REPO / "profiles" / "fp64_peak.json"
-    if pf.exists():
-        fp64_peak = json.loads(pf.read_text()).get("fp64_tflops")
-    achieved = kernel_flop / (kernel_ms / 1e3) / 1e12
-    if prec == PREC_SPLIT:
-        roof = {"bound": "tensor", "achieved": None, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": None, "traffic": None, "peak_source": src}
-    else:
-        pk = fp64_peak
-        roof = {"bound": "fp64", "achieved": achieved, "peak": pk, "unit": "TFLOP/s",
-                "frac": (achieved / pk) if pk else None, "traffic": None,
-                "peak_source": "profiles/fp64_peak.json (project FP64 FMA probe)" if pk else "unmeasured",
-                "kernel": "k_gemm_gather_f64", "kernel_ms": kernel_ms, "kernel_flop": kernel_flop}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         v, n, el = cpu_matvec_rate(chi, args.cpu_seconds)
         cpu = {"value": v, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{n} matvecs at chi={chi} ({el:.1f} s), NumPy/OpenBLAS oracle on host cores"}
     line = {
-        "metric": "H_eff matvec contraction TFLOP/s at chi=1024 (two-site DMRG)",
-        "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "replicas",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox N(0,1))",
-        "config": {"workload": f"heff2_matvec chi={chi} d=2 w=5", "chi": chi,
-                   "precision": args.precision, "l2": "flushed (256 MB write) between timed steps"},
+        "metric": METRIC,
+        "value": chosen["value"], "unit": "TFLOP/s", "n_gpus": world, "steps": chosen["steps"],
+        "warmup": args.warmup, "ms_per_step": chosen["ms_per_step"], "higher_is_better": True,
+        "scaling": "replicas", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Philox N(0,1))",
+        "config": dict(base_config(chi), form=args.chosen,
+                       l2="flushed (256 MB write) between timed steps"),
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_s * 1e3},
-        "gpu_launches": 4 * args.steps,
-        "roofline": roof,
+        "gpu_launches": (11 if chosen_prec == PREC_SPLIT else 4) * chosen["steps"],
+        "roofline": chosen["roofline"],
         "cpu_baseline": cpu,
-        "clocks": clocks,
+        "clocks": chosen["clocks"],
         "finite": finite,
     }
+    if "fp64" in results and args.chosen != "fp64":
+        pl = results["fp64"]
+        line["plain"] = {"value": pl["value"], "ms_per_step": pl["ms_per_step"], "steps": pl["steps"],
+                         "roofline": pl["roofline"], "clocks": pl["clocks"]}
+        line["chosen_vs_plain"] = chosen["value"] / pl["value"]
+    if accuracy is not None:
+        line["split_vs_fp64_rel_frobenius"] = accuracy
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -345,7 +364,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="itg", choices=["itg", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--precision", default="both", choices=["both", "fp64", "split"])
+    ap.add_argument("--chosen", default="split", choices=["fp64", "split"])
+    ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--chi", type=int, default=CHI)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -74,6 +74,19 @@ ITG_API const char* itg_status_string(int status);
 /* Library version as major*10000 + minor*100 + patch. */
 ITG_API int itg_version(void);
 
+/* Kernel timing (tracing; the reference's analogue is its TimerOutputs
+ * @timeit blocks, src/tensor/culinearalgebra.jl:41,82,91, which time launches
+ * without a device sync).  itg_profile(h, 1) clears and starts recording CUDA
+ * events on the handle's stream around the contraction kernels; 0 stops.
+ * itg_profile_read synchronises the stream and returns the summed device time
+ * and launch count of one kernel class:
+ *   ITG_KERNEL_GEMM_F64   the FP64 gather-GEMM (k_gemm_gather_f64)
+ *   ITG_KERNEL_GEMM_SPLIT the tcgen05 split-precision GEMM (k_split_gemm)
+ *   ITG_KERNEL_SPLIT_PREP the split operand preparation (exponents + digits) */
+enum { ITG_KERNEL_GEMM_F64 = 0, ITG_KERNEL_GEMM_SPLIT = 1, ITG_KERNEL_SPLIT_PREP = 2 };
+ITG_API int itg_profile(itg_handle* h, int enable);
+ITG_API int itg_profile_read(itg_handle* h, int kernel, double* total_ms, int64_t* launches);
+
 /* ---------------------------------------------------------------- memory */
 /* Replace CuVector allocation and the H2D/D2H copies of
  * src/tensor/cudense.jl:4-13 (Dense{T,CuArray}(::Dense{T,Array}), cpu(x)). */

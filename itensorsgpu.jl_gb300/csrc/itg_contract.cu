@@ -185,6 +185,7 @@ int launch_gemm(itg_handle* h, const ContractPlan& p, const double* A, const dou
   int64_t gx = (p.M + GBM - 1) / GBM, gy = (p.N + GBN - 1) / GBN;
   if (gy > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "N=%lld too large", (long long)p.N);
   dim3 grid((unsigned)gx, (unsigned)gy);
+  ProfScope prof(h, ITG_KERNEL_GEMM_F64);
   k_gemm_gather_f64<AK, BK><<<grid, GTHREADS, GEMM_SMEM, h->stream>>>(
       A, B, C, p.offAm(), p.offAk(), p.offBk(), p.offBn(), p.offCm(), p.offCn(), p.M, p.N, p.K,
       alpha, beta);

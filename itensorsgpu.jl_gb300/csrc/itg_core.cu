@@ -58,6 +58,66 @@ extern "C" int itg_create(int device, itg_handle** out) {
   return ITG_OK;
 }
 
+// ---------------------------------------------------------------- timing
+static cudaEvent_t prof_event(itg_handle* h) {
+  if (!h->prof_pool.empty()) {
+    cudaEvent_t e = h->prof_pool.back();
+    h->prof_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+static void prof_clear(itg_handle* h) {
+  for (auto& x : h->prof_events) {
+    h->prof_pool.push_back(x.second.first);
+    h->prof_pool.push_back(x.second.second);
+  }
+  h->prof_events.clear();
+}
+
+ProfScope::ProfScope(itg_handle* hh, int k) : h(hh), kind(k) {
+  if (!h->prof_on) return;
+  e1 = prof_event(h);
+  cudaEventRecord(e1, h->stream);
+}
+
+ProfScope::~ProfScope() {
+  if (!e1) return;
+  cudaEvent_t e2 = prof_event(h);
+  cudaEventRecord(e2, h->stream);
+  h->prof_events.push_back({kind, {e1, e2}});
+}
+
+extern "C" int itg_profile(itg_handle* h, int enable) {
+  if (!h) return ITG_ERR_INVALID;
+  if (enable) {
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    prof_clear(h);
+  }
+  h->prof_on = enable != 0;
+  return ITG_OK;
+}
+
+extern "C" int itg_profile_read(itg_handle* h, int kernel, double* total_ms, int64_t* launches) {
+  if (!h || !total_ms) return ITG_ERR_INVALID;
+  ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  double t = 0.0;
+  int64_t n = 0;
+  for (auto& x : h->prof_events) {
+    if (x.first != kernel) continue;
+    float ms = 0.f;
+    ITG_CUDA(h, cudaEventElapsedTime(&ms, x.second.first, x.second.second));
+    t += ms;
+    n++;
+  }
+  *total_ms = t;
+  if (launches) *launches = n;
+  return ITG_OK;
+}
+
 void itg_release_plans(itg_handle* h);  // itg_contract.cu
 
 extern "C" int itg_destroy(itg_handle* h) {
@@ -65,6 +125,8 @@ extern "C" int itg_destroy(itg_handle* h) {
   cudaSetDevice(h->device);
   cudaStreamSynchronize(h->stream);
   itg_release_plans(h);
+  prof_clear(h);
+  for (auto e : h->prof_pool) cudaEventDestroy(e);
   if (h->scratch) cudaFree(h->scratch);
   if (h->split_ws) cudaFree(h->split_ws);
   if (h->pinned) cudaFreeHost(h->pinned);

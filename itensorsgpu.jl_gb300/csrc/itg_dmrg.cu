@@ -228,12 +228,13 @@ void small_sym_lowest(int k, std::vector<double> G, double& theta, std::vector<d
     for (auto& v : y) v = -v;
 }
 
+// t = r / (diag - theta), the denominator kept at least `guard` in magnitude.
 __global__ void k_precond(int64_t n, const double* __restrict__ r, const double* __restrict__ dg,
-                          double theta, double* __restrict__ t) {
+                          double theta, double guard, double* __restrict__ t) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     double den = dg[i] - theta;
-    if (fabs(den) < 1e-12) den = (den >= 0.0) ? 1e-12 : -1e-12;
+    if (fabs(den) < guard) den = (den >= 0.0) ? guard : -guard;
     t[i] = r[i] / den;
   }
 }
@@ -375,17 +376,30 @@ extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int
       ITG_CHECK_LAUNCH(h);
       ITG_TRY(nrm(Rv, rn));
       if (rn < tol || k == kmax) break;
-      // correction t = (diag - theta)^-1 r, orthogonalised twice against V
+      // correction t = (diag - theta)^-1 r, orthogonalised twice against V.  When
+      // the orthogonalisation cancels all but 1e-6 of it (the preconditioned
+      // residual lies almost in span(V)), the plain residual is used instead.
       double* t = V + (int64_t)k * n;
-      k_precond<<<gb, 256, 0, h->stream>>>(n, Rv, dg, theta, t);
-      ITG_CHECK_LAUNCH(h);
-      for (int pass = 0; pass < 2; ++pass) {
-        ITG_TRY(itg_gemv_t(h, n, k, V, n, t, sm + kmax * kmax + kmax));
-        ITG_TRY(itg_scal(h, k, -1.0, sm + kmax * kmax + kmax));
-        ITG_TRY(itg_gemv_n(h, n, k, V, n, sm + kmax * kmax + kmax, 1.0, t));
-      }
+      const double guard = 1e-8 * (fabs(theta) > 1.0 ? fabs(theta) : 1.0);
       double tn = 0.0;
-      ITG_TRY(nrm(t, tn));
+      for (int attempt = 0; attempt < 2; ++attempt) {
+        if (attempt == 0) {
+          k_precond<<<gb, 256, 0, h->stream>>>(n, Rv, dg, theta, guard, t);
+          ITG_CHECK_LAUNCH(h);
+        } else {
+          ITG_CUDA(h, cudaMemcpyAsync(t, Rv, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+        }
+        double t0 = 0.0;
+        ITG_TRY(nrm(t, t0));
+        for (int pass = 0; pass < 2; ++pass) {
+          ITG_TRY(itg_gemv_t(h, n, k, V, n, t, sm + kmax * kmax + kmax));
+          ITG_TRY(itg_scal(h, k, -1.0, sm + kmax * kmax + kmax));
+          ITG_TRY(itg_gemv_n(h, n, k, V, n, sm + kmax * kmax + kmax, 1.0, t));
+        }
+        ITG_TRY(nrm(t, tn));
+        if (tn > 1e-6 * t0) break;
+        tn = 0.0;
+      }
       if (!(tn > 1e-14)) break;
       ITG_TRY(itg_scal(h, n, 1.0 / tn, t));
       ITG_TRY(matvec(t, AV + (int64_t)k * n));

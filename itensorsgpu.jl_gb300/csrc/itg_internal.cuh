@@ -55,6 +55,19 @@ struct itg_handle {
   std::unordered_map<std::string, std::shared_ptr<ContractPlan>> plans;
   // Device status word for bounded waits (ITG_ERR_TIMEOUT reporting).
   int* dev_status = nullptr;
+  // Kernel timing (itg_profile): event pairs recorded around kernel launches.
+  bool prof_on = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_events;
+  std::vector<cudaEvent_t> prof_pool;
+};
+
+// Record a timing event pair around a launch when profiling is on.
+struct ProfScope {
+  itg_handle* h;
+  int kind;
+  cudaEvent_t e1 = nullptr;
+  ProfScope(itg_handle* hh, int k);
+  ~ProfScope();
 };
 
 // Error helpers ---------------------------------------------------------------

@@ -638,6 +638,7 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   ITG_CUDA(h, cudaMemsetAsync(err, 0, sizeof(int), h->stream));
   // exponents
   {
+    ProfScope prof(h, ITG_KERNEL_SPLIT_PREP);
     const int thr = 256;
     if (p.a_kmaj)
       k_row_expfield<true><<<itg_blocks_for(p.M, thr / 32, h->num_sms * 16), thr, 0, h->stream>>>(
@@ -655,6 +656,7 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   }
   // slices
   {
+    ProfScope prof(h, ITG_KERNEL_SPLIT_PREP);
     dim3 gA((unsigned)(Kpad / 64), (unsigned)(Mpad / 32)), gB((unsigned)(Kpad / 64), (unsigned)(Npad / 32));
     if (gA.y > 65535 || gB.y > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: too many rows");
     if (p.a_kmaj)
@@ -697,7 +699,10 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
     attr = true;
   }
   if (tiles > (int64_t)INT32_MAX) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: too many tiles");
-  k_split_gemm<BN><<<(unsigned)tiles, NUM_THREADS, Smem<BN>::TOTAL, h->stream>>>(mA, mB, a);
+  {
+    ProfScope prof(h, ITG_KERNEL_GEMM_SPLIT);
+    k_split_gemm<BN><<<(unsigned)tiles, NUM_THREADS, Smem<BN>::TOTAL, h->stream>>>(mA, mB, a);
+  }
   ITG_CHECK_LAUNCH(h);
   // surface a device-side timeout on the next synchronising call
   ITG_CUDA(h, cudaMemcpyAsync(h->dev_status, err, sizeof(int), cudaMemcpyDeviceToDevice, h->stream));

@@ -23,6 +23,7 @@ ITG_OK, ITG_ERR_INVALID, ITG_ERR_SHAPE, ITG_ERR_ALLOC, ITG_ERR_CUDA = 0, 1, 2, 3
 ITG_ERR_TIMEOUT, ITG_ERR_NOTCONVERGED, ITG_ERR_UNSUPPORTED = 5, 6, 7
 ITG_F64 = 0
 PREC_FP64, PREC_SPLIT = 0, 1
+KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_SPLIT_PREP = 0, 1, 2
 
 
 class ITGError(RuntimeError):
@@ -54,6 +55,8 @@ SIGNATURES = {
     "itg_last_error": (C.c_char_p, [_P]),
     "itg_status_string": (C.c_char_p, [C.c_int]),
     "itg_version": (C.c_int, []),
+    "itg_profile": (C.c_int, [_P, C.c_int]),
+    "itg_profile_read": (C.c_int, [_P, C.c_int, _DP, _I64P]),
     "itg_malloc": (C.c_int, [_P, C.POINTER(_P), C.c_size_t]),
     "itg_free": (C.c_int, [_P, _P]),
     "itg_memcpy_h2d": (C.c_int, [_P, _P, _P, C.c_size_t]),

@@ -303,12 +303,18 @@ def davidson(matvec, x0: np.ndarray, dg: np.ndarray, krylovdim=3, maxiter=2, tol
             rn = np.linalg.norm(r)
             if rn < tol or k == kmax:
                 break
+            guard = 1e-8 * max(abs(theta), 1.0)
             den = dg - theta
-            den = np.where(np.abs(den) < 1e-12, np.where(den >= 0, 1e-12, -1e-12), den)
-            t = r / den
-            for _ in range(2):
-                t = t - V[:, :k] @ (V[:, :k].T @ t)
-            tn = np.linalg.norm(t)
+            den = np.where(np.abs(den) < guard, np.where(den >= 0, guard, -guard), den)
+            tn = 0.0
+            for t in (r / den, r.copy()):
+                t0 = np.linalg.norm(t)
+                for _ in range(2):
+                    t = t - V[:, :k] @ (V[:, :k].T @ t)
+                tn = np.linalg.norm(t)
+                if tn > 1e-6 * t0:
+                    break
+                tn = 0.0
             if not tn > 1e-14:
                 break
             V[:, k] = t / tn
