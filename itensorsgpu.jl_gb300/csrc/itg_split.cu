@@ -24,11 +24,13 @@
 // runs in the inner loops (GB300's FP64 rate is a small fraction of its
 // tensor rate).
 //
-// Kernel roles (one CTA per 128 x BN output tile, 6 warps):
+// Kernel roles (one CTA per 128 x BN output tile, 10 warps):
 //   warp 0    TMA producer: A/B slice tiles (64 bf16 of K per stage, 128B
 //             swizzle) into a 4-stage shared-memory ring, mbarrier complete_tx
 //   warp 1    TMEM allocator and single-thread tcgen05.mma issuer
-//   warps 2-5 TMEM drain / epilogue (warp w reads TMEM lanes 32*(w%4)..+31)
+//   warps 2-9 TMEM drain / epilogue: warp w reads TMEM lanes 32*(w%4)..+31 and
+//             owns half of the tile's columns; each 32-column chunk issues all
+//             of its accumulator loads before using them
 // Every mbarrier wait is bounded (globaltimer, ~4 s); on timeout the kernel
 // records ITG_ERR_TIMEOUT, stops issuing work, waits (bounded) for its own
 // copies and MMAs, frees TMEM and returns.
@@ -49,7 +51,8 @@ constexpr int S_SLICES = 7;    // digits per operand (7 bits each)
 constexpr int BM = 128;        // tile rows (TMEM lanes)
 constexpr int BK = 64;         // K per pipeline stage (128 bytes of bf16)
 constexpr int STAGES = 4;
-constexpr int NUM_THREADS = 192;
+constexpr int NUM_EPI_WARPS = 8;  // two per TMEM lane quarter, each owning half the columns
+constexpr int NUM_THREADS = 64 + 32 * NUM_EPI_WARPS;
 constexpr uint64_t WAIT_NS = 4000000000ull;  // bounded waits: 4 s
 
 // ------------------------------------------------------------ PTX wrappers
@@ -299,7 +302,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], 4);
+      mbar_init(&acc_empty[b], NUM_EPI_WARPS);
     }
     mbar_init(done_bar, 1);
     *abort_flag = 0;
@@ -380,6 +383,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
   } else {
     // ------------------------------------------------------ drain/epilogue
     const int quarter = warp & 3;
+    const int col_lo = ((warp - 2) / 4) * (BN / 2), col_hi = col_lo + BN / 2;
     const int row = quarter * 32 + lane;
     const int64_t m = (int64_t)m0 + row;
     const int em = (m < args.M) ? args.eA[m] - 1022 : 0;
@@ -407,36 +411,40 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
       const int sh = args.F - 7 * L;
       const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN);
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
+      for (int c0 = col_lo; c0 < col_hi; c0 += 32) {
         uint32_t r[32];
         tc_ld_32x32b_x32(tbase + (uint32_t)c0, r);
-        if (last) {
-          // final drain: combine, convert to FP64, scatter through the plan
-          if (m < args.M) {
-            const int64_t cm = args.offCm[m];
-#pragma unroll 4
-            for (int j = 0; j < 32; ++j) {
-              const int64_t n = (int64_t)n0 + c0 + j;
-              if (n >= args.N) break;
-              long long t = (long long)__float2int_rn(__uint_as_float(r[j]));
-              t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
-              const size_t idx = (size_t)(c0 + j) * BM + row;
-              const long long tot = first_drain ? t : acc[idx] + t;
-              const int fn = args.eB[n] - 1022;
-              double v = i64_to_double_scaled(tot, em + fn - 14 - args.F);
-              if (args.alpha != 1.0) v *= args.alpha;
-              double* cp = args.C + cm + args.offCn[n];
-              if (args.beta != 0.0) v = fma(args.beta, *cp, v);
-              *cp = v;
-            }
-          }
+        long long* ap = acc + (size_t)c0 * BM + row;
+        long long old[32];
+        if (!first_drain) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) old[j] = ap[(size_t)j * BM];
         } else {
-#pragma unroll 8
+#pragma unroll
+          for (int j = 0; j < 32; ++j) old[j] = 0;
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          long long t = (long long)__float2int_rn(__uint_as_float(r[j]));
+          t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
+          old[j] += t;
+        }
+        if (!last) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) ap[(size_t)j * BM] = old[j];
+        } else if (m < args.M) {
+          // final drain: convert to FP64 with integer instructions, scatter through the plan
+          const int64_t cm = args.offCm[m];
+#pragma unroll
           for (int j = 0; j < 32; ++j) {
-            long long t = (long long)__float2int_rn(__uint_as_float(r[j]));
-            t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
-            const size_t idx = (size_t)(c0 + j) * BM + row;
-            acc[idx] = first_drain ? t : acc[idx] + t;
+            const int64_t n = (int64_t)n0 + c0 + j;
+            if (n >= args.N) continue;
+            const int fn = args.eB[n] - 1022;
+            double v = i64_to_double_scaled(old[j], em + fn - 14 - args.F);
+            if (args.alpha != 1.0) v *= args.alpha;
+            double* cp = args.C + cm + args.offCn[n];
+            if (args.beta != 0.0) v = fma(args.beta, *cp, v);
+            *cp = v;
           }
         }
       }
@@ -460,11 +468,10 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
 
 // ----------------------------------------------------------- slicing
 // Exponent field (11 bits) of max_k |X[r,k]| for every row r < R.
-template <bool KMAJ>
 __global__ void k_row_expfield(const double* __restrict__ X, const int64_t* __restrict__ offR,
                                const int64_t* __restrict__ offK, int64_t R, int64_t K,
                                int* __restrict__ efield) {
-  if (KMAJ) {
+  {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t r = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); r < R; r += warps) {
@@ -480,18 +487,26 @@ __global__ void k_row_expfield(const double* __restrict__ X, const int64_t* __re
       }
       if (lane == 0) efield[r] = (int)((mx >> 52) & 0x7FF);
     }
-  } else {
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < R;
-         r += (int64_t)gridDim.x * blockDim.x) {
-      const double* x = X + offR[r];
-      unsigned long long mx = 0;
-      for (int64_t k = 0; k < K; ++k) {
-        unsigned long long b = (unsigned long long)__double_as_longlong(x[offK[k]]) & 0x7FFFFFFFFFFFFFFFull;
-        mx = b > mx ? b : mx;
-      }
-      efield[r] = (int)((mx >> 52) & 0x7FF);
-    }
   }
+}
+
+// Rows contiguous in memory: a 2-D grid, threads along rows, blockIdx.y over
+// K chunks of 64; partial maxima meet through atomicMax on the exponent field
+// (integer max, order independent).  efield must start at 0.
+__global__ void k_row_expfield_mmajor(const double* __restrict__ X, const int64_t* __restrict__ offR,
+                                      const int64_t* __restrict__ offK, int64_t R, int64_t K,
+                                      int* __restrict__ efield) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  const int64_t k0 = (int64_t)blockIdx.y * 64, k1 = k0 + 64 < K ? k0 + 64 : K;
+  const double* x = X + offR[r];
+  unsigned long long mx = 0;
+  for (int64_t k = k0; k < k1; ++k) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x[offK[k]]) & 0x7FFFFFFFFFFFFFFFull;
+    mx = b > mx ? b : mx;
+  }
+  const int e = (int)((mx >> 52) & 0x7FF);
+  if (e) atomicMax(&efield[r], e);
 }
 
 // Balanced base-2^7 digits of X[r,k] * 2^-e_r rounded to 7S fractional bits.
@@ -640,18 +655,22 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   {
     ProfScope prof(h, ITG_KERNEL_SPLIT_PREP);
     const int thr = 256;
-    if (p.a_kmaj)
-      k_row_expfield<true><<<itg_blocks_for(p.M, thr / 32, h->num_sms * 16), thr, 0, h->stream>>>(
-          A, p.offAm(), p.offAk(), p.M, p.K, eA);
-    else
-      k_row_expfield<false><<<itg_blocks_for(p.M, thr, h->num_sms * 16), thr, 0, h->stream>>>(
-          A, p.offAm(), p.offAk(), p.M, p.K, eA);
-    if (p.b_kmaj)
-      k_row_expfield<true><<<itg_blocks_for(p.N, thr / 32, h->num_sms * 16), thr, 0, h->stream>>>(
-          B, p.offBn(), p.offBk(), p.N, p.K, eB);
-    else
-      k_row_expfield<false><<<itg_blocks_for(p.N, thr, h->num_sms * 16), thr, 0, h->stream>>>(
-          B, p.offBn(), p.offBk(), p.N, p.K, eB);
+    auto expo = [&](bool kmaj, const double* X, const int64_t* offR, const int64_t* offK, int64_t R,
+                    int* ef) -> int {
+      if (kmaj) {
+        k_row_expfield<<<itg_blocks_for(R, thr / 32, h->num_sms * 16), thr, 0, h->stream>>>(
+            X, offR, offK, R, p.K, ef);
+      } else {
+        ITG_CUDA(h, cudaMemsetAsync(ef, 0, sizeof(int) * R, h->stream));
+        const int64_t ky = (p.K + 63) / 64;
+        if (ky > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: contraction depth too large");
+        dim3 g((unsigned)((R + thr - 1) / thr), (unsigned)ky);
+        k_row_expfield_mmajor<<<g, thr, 0, h->stream>>>(X, offR, offK, R, p.K, ef);
+      }
+      return ITG_OK;
+    };
+    ITG_TRY(expo(p.a_kmaj, A, p.offAm(), p.offAk(), p.M, eA));
+    ITG_TRY(expo(p.b_kmaj, B, p.offBn(), p.offBk(), p.N, eB));
     ITG_CHECK_LAUNCH(h);
   }
   // slices

@@ -72,66 +72,65 @@ def test_heff_diag_matches_oracle(gpu):
         assert relerr(dg.cpu().numpy(), ref) < 1e-13
 
 
-def test_davidson_pieces_localised(gpu):
-    """The oracle's Davidson driven by the GPU matvec and GPU diagonal must equal
-    the pure oracle (isolates the device kernels from the solver logic)."""
-    from itg import _lib
-    chi, d, w = 24, 2, 5
-    L, W1, W2, R, psi = _heff_inputs(chi, d=d, w=w, seed=3)
+def _sym_heff(chi, d, w, seed):
+    L, W1, W2, R, psi = _heff_inputs(chi, d=d, w=w, seed=seed)
     L = L + L.transpose(2, 1, 0)
     R = R + R.transpose(2, 1, 0)
     W1 = W1 + W1.transpose(0, 2, 1, 3)
     W2 = W2 + W2.transpose(0, 2, 1, 3)
+    return L, W1, W2, R, psi
+
+
+def _gpu_davidson(chi, d, w, L, W1, W2, R, psi, kd, mi, tol):
+    from itg import _lib
     h = _lib.handle(0)
     ptr = lambda t: C.c_void_p(t.data_ptr())
-    Ld, W1d, W2d, Rd = map(_dev, (L, W1, W2, R))
+    Ld, W1d, W2d, Rd, pd = map(_dev, (L, W1, W2, R, psi))
+    e = C.c_double()
+    nmv = C.c_int()
+    h.call("itg_davidson_heff2", C.c_int64(chi), C.c_int64(chi), C.c_int64(d), C.c_int64(w),
+           C.c_int64(w), C.c_int64(w), ptr(Ld), ptr(W1d), ptr(W2d), ptr(Rd), ptr(pd), kd, mi,
+           C.c_double(tol), 0, C.byref(e), C.byref(nmv))
+    return e.value, pd.cpu().numpy(), nmv.value
 
-    def gpu_mv(v):
-        x = _dev(O.unflat(v, psi.shape))
-        y = torch_empty_like(x)
-        h.call("itg_heff2_apply", C.c_int64(chi), C.c_int64(chi), C.c_int64(d), C.c_int64(w),
-               C.c_int64(w), C.c_int64(w), ptr(Ld), ptr(W1d), ptr(W2d), ptr(Rd), ptr(x), ptr(y), 0)
-        return y.cpu().numpy()
 
-    dgd = _dev(np.zeros_like(psi))
-    h.call("itg_heff2_diag", C.c_int64(chi), C.c_int64(chi), C.c_int64(d), C.c_int64(w),
-           C.c_int64(w), C.c_int64(w), ptr(Ld), ptr(W1d), ptr(W2d), ptr(Rd), ptr(dgd))
-    mv = lambda v: O.flat(O.heff_apply(L, W1, W2, R, O.unflat(v, psi.shape)))
+def test_davidson_converges_to_lowest_eigenvalue(gpu):
+    """Converged runs reach the exact lowest eigenvalue of the (dense) operator.
+
+    The operator is a random symmetric H_eff; its Rayleigh quotients start in
+    the interior of diag(H), where a diagonally preconditioned Davidson is
+    sensitive to rounding (1e-16 perturbations change a 5-matvec energy at
+    1e-7), so only converged results are compared here."""
+    chi, d, w = 12, 2, 5
+    L, W1, W2, R, psi = _sym_heff(chi, d, w, seed=3)
+    n = chi * d * d * chi
+    H = np.stack([O.flat(O.heff_apply(L, W1, W2, R, O.unflat(np.eye(n)[:, i], psi.shape)))
+                  for i in range(n)], axis=1)
+    e0 = np.linalg.eigvalsh(0.5 * (H + H.T))[0]
+    e, x, nmv = _gpu_davidson(chi, d, w, L, W1, W2, R, psi, 10, 200, 1e-9)
+    assert abs(e - e0) < 1e-10 * abs(e0)
+    assert np.linalg.norm(H @ x - e * x) < 1e-8 * abs(e0)
+
+
+def test_davidson_matches_oracle_trajectory(gpu):
+    """Well-conditioned start (the ground state plus 1e-3 noise): the GPU solver
+    and the oracle's restatement follow the same iterates (same matvec count,
+    energies within 1e-12 relative)."""
+    chi, d, w = 12, 2, 5
+    L, W1, W2, R, psi = _sym_heff(chi, d, w, seed=4)
+    n = chi * d * d * chi
+    H = np.stack([O.flat(O.heff_apply(L, W1, W2, R, O.unflat(np.eye(n)[:, i], psi.shape)))
+                  for i in range(n)], axis=1)
+    wv, V = np.linalg.eigh(0.5 * (H + H.T))
+    rng = np.random.default_rng(0)
+    start = O.unflat(V[:, 0] + 1e-3 * rng.standard_normal(n), psi.shape)
+    mv = lambda v: H @ v
     dg = O.flat(O.heff_diag(L, W1, W2, R))
-    th_o, _, _ = O.davidson(mv, O.flat(psi), dg, 3, 2, 1e-14)
-    th_g, _, _ = O.davidson(gpu_mv, O.flat(psi), dgd.cpu().numpy(), 3, 2, 1e-14)
-    assert abs(th_g - th_o) < 1e-10 * abs(th_o)
-
-
-def torch_empty_like(x):
-    import torch
-    return torch.empty_like(x)
-
-
-def test_davidson_matches_oracle(gpu):
-    from itg import _lib
-    chi, d, w = 24, 2, 5
-    L, W1, W2, R, psi = _heff_inputs(chi, d=d, w=w, seed=3)
-    # make H_eff symmetric: symmetrise the environments and the MPO tensors
-    L = L + L.transpose(2, 1, 0)
-    R = R + R.transpose(2, 1, 0)
-    W1 = W1 + W1.transpose(0, 2, 1, 3)
-    W2 = W2 + W2.transpose(0, 2, 1, 3)
-    mv = lambda v: O.flat(O.heff_apply(L, W1, W2, R, O.unflat(v, psi.shape)))
-    dg = O.flat(O.heff_diag(L, W1, W2, R))
-    for kd, mi in ((3, 2), (6, 10)):
-        th_o, x_o, nmv_o = O.davidson(mv, O.flat(psi), dg, kd, mi, 1e-14)
-        h = _lib.handle(0)
-        ptr = lambda t: C.c_void_p(t.data_ptr())
-        Ld, W1d, W2d, Rd, pd = map(_dev, (L, W1, W2, R, psi))
-        e = C.c_double()
-        nmv = C.c_int()
-        h.call("itg_davidson_heff2", C.c_int64(chi), C.c_int64(chi), C.c_int64(d), C.c_int64(w),
-               C.c_int64(w), C.c_int64(w), ptr(Ld), ptr(W1d), ptr(W2d), ptr(Rd), ptr(pd), kd, mi,
-               C.c_double(1e-14), 0, C.byref(e), C.byref(nmv))
-        assert nmv.value == nmv_o
-        assert abs(e.value - th_o) < 1e-10 * abs(th_o)
-        x = pd.cpu().numpy()
+    for kd, mi in ((3, 2), (5, 3)):
+        th_o, x_o, nmv_o = O.davidson(mv, O.flat(start), dg, kd, mi, 1e-14)
+        e, x, nmv = _gpu_davidson(chi, d, w, L, W1, W2, R, start, kd, mi, 1e-14)
+        assert nmv == nmv_o
+        assert abs(e - th_o) < 1e-12 * abs(th_o)
         assert min(np.linalg.norm(x - x_o), np.linalg.norm(x + x_o)) < 1e-8
 
 
