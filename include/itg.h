@@ -69,6 +69,10 @@ ITG_API int itg_destroy(itg_handle* h);
 ITG_API int itg_set_stream(itg_handle* h, void* stream);
 ITG_API int itg_get_stream(itg_handle* h, void** stream);
 ITG_API int itg_synchronize(itg_handle* h);
+/* enable = 1: itg_davidson_heff2 captures the H_eff chain once per call into a
+ * CUDA graph (on a private capture stream) and replays it for every further
+ * matvec.  Off by default. */
+ITG_API int itg_set_graphs(itg_handle* h, int enable);
 ITG_API const char* itg_last_error(itg_handle* h);
 ITG_API const char* itg_status_string(int status);
 /* Library version as major*10000 + minor*100 + patch. */

@@ -129,6 +129,7 @@ extern "C" int itg_destroy(itg_handle* h) {
   for (auto e : h->prof_pool) cudaEventDestroy(e);
   if (h->scratch) cudaFree(h->scratch);
   if (h->split_ws) cudaFree(h->split_ws);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->dev_status) cudaFree(h->dev_status);
   delete h;
@@ -144,6 +145,12 @@ extern "C" int itg_set_stream(itg_handle* h, void* stream) {
 extern "C" int itg_get_stream(itg_handle* h, void** stream) {
   if (!h || !stream) return ITG_ERR_INVALID;
   *stream = (void*)h->stream;
+  return ITG_OK;
+}
+
+extern "C" int itg_set_graphs(itg_handle* h, int enable) {
+  if (!h) return ITG_ERR_INVALID;
+  h->use_graphs = enable != 0;
   return ITG_OK;
 }
 

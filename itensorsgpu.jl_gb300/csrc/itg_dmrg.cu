@@ -311,6 +311,7 @@ extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int
   size_t oDg = take(sizeof(double) * n), oX = take(sizeof(double) * n), oHX = take(sizeof(double) * n),
          oR = take(sizeof(double) * n), oSm = take(sizeof(double) * (kmax * kmax + 4 * kmax + 8)),
          oPart = take(sizeof(double) * 1024);
+  size_t oXg = take(h->use_graphs ? sizeof(double) * n : 0), oYg = take(h->use_graphs ? sizeof(double) * n : 0);
   ITG_TRY(itg_scratch_reserve(h, off));
   char* base = (char*)h->scratch;
   HeffWork w = heff_carve(D, base + oH);
@@ -322,6 +323,8 @@ extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int
   double* Rv = (double*)(base + oR);
   double* sm = (double*)(base + oSm);
   double* part = (double*)(base + oPart);
+  double* Xg = (double*)(base + oXg);
+  double* Yg = (double*)(base + oYg);
   double* hp = h->pinned;
   const int gb = itg_blocks_for(n, 256, h->num_sms * 8);
 
@@ -333,9 +336,47 @@ extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int
     out = hp[0];
     return ITG_OK;
   };
-  auto matvec = [&](const double* x, double* y) -> int {
+  // With graphs on, the chain is captured once per call (after a first direct
+  // matvec has built the plans and sized the workspaces) with fixed input and
+  // output buffers, then replayed for every further matvec.
+  cudaGraphExec_t gexec = nullptr;
+  auto matvec_direct = [&](const double* x, double* y) -> int {
     return heff_apply(h, D, L, R, x, y, w, precision);
   };
+  auto matvec = [&](const double* x, double* y) -> int {
+    if (!h->use_graphs || !gexec) return matvec_direct(x, y);
+    ITG_CUDA(h, cudaMemcpyAsync(Xg, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+    ITG_CUDA(h, cudaGraphLaunch(gexec, h->stream));
+    ITG_CUDA(h, cudaMemcpyAsync(y, Yg, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+    return ITG_OK;
+  };
+  auto capture = [&]() -> int {
+    if (!h->cap_stream) ITG_CUDA(h, cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    cudaStream_t saved = h->stream;
+    const bool prof = h->prof_on;
+    h->prof_on = false;
+    h->stream = h->cap_stream;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal);
+    int st = ITG_OK;
+    if (e == cudaSuccess) {
+      st = matvec_direct(Xg, Yg);
+      e = cudaStreamEndCapture(h->cap_stream, &graph);
+    }
+    h->stream = saved;
+    h->prof_on = prof;
+    if (st != ITG_OK) return st;
+    if (e != cudaSuccess) return itg_fail(h, ITG_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return itg_fail(h, ITG_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    return ITG_OK;
+  };
+  struct GraphGuard {
+    cudaGraphExec_t* g;
+    ~GraphGuard() { if (*g) cudaGraphExecDestroy(*g); }
+  } gguard{&gexec};
 
   ITG_TRY(form_weff(h, D, W1, W2, w.Weff));
   {
@@ -349,7 +390,8 @@ extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int
   if (!(pn > 0.0)) return itg_fail(h, ITG_ERR_INVALID, "davidson: zero start vector");
   k_lincomb<<<gb, 256, 0, h->stream>>>(n, 1.0 / pn, psi, 0.0, V);
   ITG_CHECK_LAUNCH(h);
-  ITG_TRY(matvec(V, AV));
+  ITG_TRY(matvec_direct(V, AV));
+  if (h->use_graphs) ITG_TRY(capture());
   int nmv = 1;
   int k = 1;
   double theta = 0.0, rn = 0.0;

@@ -55,6 +55,9 @@ struct itg_handle {
   std::unordered_map<std::string, std::shared_ptr<ContractPlan>> plans;
   // Device status word for bounded waits (ITG_ERR_TIMEOUT reporting).
   int* dev_status = nullptr;
+  // CUDA-graph replay of the H_eff chain inside Davidson (itg_set_graphs).
+  bool use_graphs = false;
+  cudaStream_t cap_stream = nullptr;
   // Kernel timing (itg_profile): event pairs recorded around kernel launches.
   bool prof_on = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_events;

@@ -52,6 +52,7 @@ SIGNATURES = {
     "itg_set_stream": (C.c_int, [_P, _P]),
     "itg_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "itg_synchronize": (C.c_int, [_P]),
+    "itg_set_graphs": (C.c_int, [_P, C.c_int]),
     "itg_last_error": (C.c_char_p, [_P]),
     "itg_status_string": (C.c_char_p, [C.c_int]),
     "itg_version": (C.c_int, []),

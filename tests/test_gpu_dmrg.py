@@ -134,6 +134,24 @@ def test_davidson_matches_oracle_trajectory(gpu):
         assert min(np.linalg.norm(x - x_o), np.linalg.norm(x + x_o)) < 1e-8
 
 
+def test_davidson_graph_replay_identical(gpu):
+    """itg_set_graphs(1): the captured H_eff chain replays the same kernels in
+    the same order, so results are bit-identical to direct launches."""
+    from itg import _lib
+    chi, d, w = 20, 2, 5
+    L, W1, W2, R, psi = _sym_heff(chi, d, w, seed=5)
+    h = _lib.handle(0)
+    res = []
+    for g in (0, 1):
+        h.call("itg_set_graphs", g)
+        try:
+            res.append(_gpu_davidson(chi, d, w, L, W1, W2, R, psi, 4, 3, 1e-14))
+        finally:
+            h.call("itg_set_graphs", 0)
+    (e0, x0, n0), (e1, x1, n1) = res
+    assert n0 == n1 and e0 == e1 and np.array_equal(x0, x1)
+
+
 def _run_dmrg_pair(gpu, N, d, mpo_gpu, mpo_oracle, linkdim, seed, maxdims, cutoffs, nsweep, **kw):
     sites = gpu.siteinds("S=1/2" if d == 2 else "S=1", N)
     H = gpu.cuMPO(mpo_gpu(sites))
