@@ -209,6 +209,23 @@ ITG_API int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* A, 
                   double* U, double* S, double* V,
                   int64_t* k, double* truncerr, double* docut);
 
+/* itg_svd_trunc with an explicit method and GEMM precision.
+ *  ITG_SVD_JACOBI: one-sided FP64 Jacobi (every rotation in FP64).
+ *  ITG_SVD_MIXED : FP32 one-sided Jacobi, then FP64-accurate refinement of the
+ *                  right singular vectors as eigenvectors of A^T A (matrix
+ *                  products through the contraction engine at `precision`),
+ *                  U = A V / sigma and one Newton-Schulz orthonormalisation.
+ *                  Singular values to ~eps * sigma_max absolute.
+ *  ITG_SVD_AUTO  : Jacobi for min(m, n) <= 192, mixed above (itg_svd_trunc
+ *                  uses AUTO with ITG_PREC_FP64). */
+enum { ITG_SVD_AUTO = 0, ITG_SVD_JACOBI = 1, ITG_SVD_MIXED = 2 };
+ITG_API int itg_svd_trunc_ex(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
+                             int64_t maxdim, int64_t mindim, double cutoff,
+                             int absoluteCutoff, int doRelCutoff, int legacy_gpu,
+                             double* U, double* S, double* V,
+                             int64_t* k, double* truncerr, double* docut,
+                             int method, int precision);
+
 /* Eigendecomposition of the symmetric n x n matrix A: A = U diag(D) U^T with D
  * descending, then truncation of D as a spectrum.  U holds n*n doubles.
  * Replaces eigen(::Hermitian{CuDenseTensor}) (src/tensor/culinearalgebra.jl:74-108). */

@@ -29,19 +29,15 @@ constexpr int GBM = 128, GBN = 128, GBK = 16, GTHREADS = 256;
 constexpr int SPAD = 4;  // shared-memory row padding (doubles)
 
 template <bool AK, bool BK>
-__global__ void __launch_bounds__(GTHREADS)
-k_gemm_gather_f64(const double* __restrict__ A, const double* __restrict__ B,
+__device__ __forceinline__ void gemm_tile_f64(const double* __restrict__ A, const double* __restrict__ B,
                   double* __restrict__ C, const int64_t* __restrict__ offAm,
                   const int64_t* __restrict__ offAk, const int64_t* __restrict__ offBk,
                   const int64_t* __restrict__ offBn, const int64_t* __restrict__ offCm,
                   const int64_t* __restrict__ offCn, int64_t M, int64_t N, int64_t K,
-                  double alpha, double beta) {
-  extern __shared__ double smem[];
+                  double alpha, double beta, int64_t m0, int64_t n0, double* smem) {
   double* As = smem;                              // [2][GBK][GBM+SPAD]
   double* Bs = smem + 2 * GBK * (GBM + SPAD);     // [2][GBK][GBN+SPAD]
   const int t = threadIdx.x;
-  const int64_t m0 = (int64_t)blockIdx.x * GBM;
-  const int64_t n0 = (int64_t)blockIdx.y * GBN;
 
   // Load mapping.
   // AK: kk = t&15, rows mm = (t>>4) + 16r.   !AK: mm = t&127, kk = (t>>7) + 2r.
@@ -168,6 +164,55 @@ k_gemm_gather_f64(const double* __restrict__ A, const double* __restrict__ B,
       if (beta != 0.0) v = fma(beta, *c, v);
       *c = v;
     }
+  }
+}
+
+template <bool AK, bool BK>
+__global__ void __launch_bounds__(GTHREADS)
+k_gemm_gather_f64(const double* __restrict__ A, const double* __restrict__ B,
+                  double* __restrict__ C, const int64_t* __restrict__ offAm,
+                  const int64_t* __restrict__ offAk, const int64_t* __restrict__ offBk,
+                  const int64_t* __restrict__ offBn, const int64_t* __restrict__ offCm,
+                  const int64_t* __restrict__ offCn, int64_t M, int64_t N, int64_t K,
+                  double alpha, double beta) {
+  extern __shared__ double smem[];
+  gemm_tile_f64<AK, BK>(A, B, C, offAm, offAk, offBk, offBn, offCm, offCn, M, N, K, alpha, beta,
+                        (int64_t)blockIdx.x * GBM, (int64_t)blockIdx.y * GBN, smem);
+}
+
+// Grouped launch: many contractions of one mode structure with different
+// sizes.  CTA b finds its problem by binary search over tile_start.
+struct GroupProb {
+  const double* A;
+  const double* B;
+  double* C;
+  const int64_t* tables;
+  int64_t M, N, K;
+  int64_t tile_start, tiles_n;
+  int flags;  // bit 0: A K-major, bit 1: B K-major
+};
+
+__global__ void __launch_bounds__(GTHREADS)
+k_gemm_gather_f64_grouped(const GroupProb* __restrict__ probs, int count, double alpha, double beta) {
+  extern __shared__ double smem[];
+  const int64_t b = blockIdx.x;
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (probs[mid].tile_start <= b) lo = mid; else hi = mid - 1;
+  }
+  const GroupProb& p = probs[lo];
+  const int64_t local = b - p.tile_start;
+  const int64_t tm = local / p.tiles_n, tn = local - tm * p.tiles_n;
+  const int64_t* T = p.tables;
+  const int64_t *offAm = T, *offCm = T + p.M, *offBn = T + 2 * p.M, *offCn = T + 2 * p.M + p.N;
+  const int64_t *offAk = T + 2 * p.M + 2 * p.N, *offBk = offAk + p.K;
+  const int64_t m0 = tm * GBM, n0 = tn * GBN;
+  switch (p.flags) {
+    case 3: gemm_tile_f64<true, true>(p.A, p.B, p.C, offAm, offAk, offBk, offBn, offCm, offCn, p.M, p.N, p.K, alpha, beta, m0, n0, smem); break;
+    case 1: gemm_tile_f64<true, false>(p.A, p.B, p.C, offAm, offAk, offBk, offBn, offCm, offCn, p.M, p.N, p.K, alpha, beta, m0, n0, smem); break;
+    case 2: gemm_tile_f64<false, true>(p.A, p.B, p.C, offAm, offAk, offBk, offBn, offCm, offCn, p.M, p.N, p.K, alpha, beta, m0, n0, smem); break;
+    default: gemm_tile_f64<false, false>(p.A, p.B, p.C, offAm, offAk, offBk, offBn, offCm, offCn, p.M, p.N, p.K, alpha, beta, m0, n0, smem); break;
   }
 }
 
@@ -429,6 +474,75 @@ extern "C" int itg_contract(itg_handle* h, int dtype, double alpha, const void* 
     if (dimsC[i] < 0) return itg_fail(h, ITG_ERR_SHAPE, "negative dimension");
   return itg::contract_f64(h, alpha, (const double*)A, rankA, dimsA, modesA, (const double*)B, rankB,
                            dimsB, modesB, beta, (double*)C, rankC, dimsC, modesC, precision);
+}
+
+namespace itg {
+// Grouped FP64 contraction: `count` problems sharing ranks and mode labels,
+// each with its own dims and pointers (dims arrays are concatenated per problem).
+int contract_grouped_f64(itg_handle* h, int count, double alpha, const double* const* A, int rankA,
+                         const int64_t* dimsA, const int32_t* modesA, const double* const* B, int rankB,
+                         const int64_t* dimsB, const int32_t* modesB, double beta, double* const* C,
+                         int rankC, const int64_t* dimsC, const int32_t* modesC) {
+  if (count <= 0) return ITG_OK;
+  std::vector<GroupProb> probs;
+  probs.reserve(count);
+  int64_t tiles = 0;
+  for (int i = 0; i < count; ++i) {
+    std::shared_ptr<ContractPlan> pl;
+    ITG_TRY(get_plan(h, rankA, dimsA + (int64_t)i * rankA, modesA, rankB, dimsB + (int64_t)i * rankB,
+                     modesB, rankC, dimsC + (int64_t)i * rankC, modesC, pl));
+    if (pl->M == 0 || pl->N == 0 || pl->K == 0)
+      return itg_fail(h, ITG_ERR_UNSUPPORTED, "grouped contraction with an empty problem");
+    GroupProb g;
+    g.A = A[i];
+    g.B = B[i];
+    g.C = C[i];
+    g.tables = pl->tables;
+    g.M = pl->M;
+    g.N = pl->N;
+    g.K = pl->K;
+    g.tiles_n = (pl->N + GBN - 1) / GBN;
+    g.tile_start = tiles;
+    g.flags = (pl->a_kmaj ? 1 : 0) | (pl->b_kmaj ? 2 : 0);
+    tiles += ((pl->M + GBM - 1) / GBM) * g.tiles_n;
+    probs.push_back(g);
+  }
+  if (tiles > (int64_t)INT32_MAX) return itg_fail(h, ITG_ERR_UNSUPPORTED, "grouped: too many tiles");
+  const size_t bytes = sizeof(GroupProb) * probs.size();
+  ITG_TRY(itg_scratch_reserve(h, bytes));
+  // the descriptor array lives at the end of nothing else: callers of the
+  // grouped path do not hold scratch regions
+  ITG_CUDA(h, cudaMemcpyAsync(h->scratch, probs.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+  static bool attr = false;
+  if (!attr) {
+    ITG_CUDA(h, cudaFuncSetAttribute(k_gemm_gather_f64_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)GEMM_SMEM));
+    attr = true;
+  }
+  ProfScope prof(h, ITG_KERNEL_GEMM_F64);
+  k_gemm_gather_f64_grouped<<<(unsigned)tiles, GTHREADS, GEMM_SMEM, h->stream>>>(
+      (const GroupProb*)h->scratch, count, alpha, beta);
+  ITG_CHECK_LAUNCH(h);
+  return ITG_OK;
+}
+}  // namespace itg
+
+extern "C" int itg_contract_grouped(itg_handle* h, int count, double alpha, const void* const* A,
+                                    int rankA, const int64_t* dimsA, const int32_t* modesA,
+                                    const void* const* B, int rankB, const int64_t* dimsB,
+                                    const int32_t* modesB, double beta, void* const* C, int rankC,
+                                    const int64_t* dimsC, const int32_t* modesC) {
+  if (!h || count < 0 || (count > 0 && (!A || !B || !C || !dimsA || !dimsB || !dimsC)))
+    return ITG_ERR_INVALID;
+  if (rankA > ITG_MAX_RANK || rankB > ITG_MAX_RANK || rankC > ITG_MAX_RANK || rankA < 0 || rankB < 0 ||
+      rankC < 0)
+    return itg_fail(h, ITG_ERR_UNSUPPORTED, "rank outside 0..%d", ITG_MAX_RANK);
+  for (int i = 0; i < count; ++i)
+    if (!A[i] || !B[i] || !C[i] || C[i] == A[i] || C[i] == B[i])
+      return itg_fail(h, ITG_ERR_INVALID, "grouped problem %d: null or aliased pointer", i);
+  return itg::contract_grouped_f64(h, count, alpha, (const double* const*)A, rankA, dimsA, modesA,
+                                   (const double* const*)B, rankB, dimsB, modesB, beta,
+                                   (double* const*)C, rankC, dimsC, modesC);
 }
 
 extern "C" int itg_matmul(itg_handle* h, int64_t m, int64_t n, int64_t k, const double* A,

@@ -434,10 +434,48 @@ int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* f
 
 }  // namespace
 
+namespace itg {
+int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, int precision,
+                   double* X, double* lam, double* Uw, double* ws, float* ws32, int* flag,
+                   int* sweeps_out);
+size_t svd_mixed_ws_doubles(int64_t mm, int64_t nn);
+}  // namespace itg
+
+__global__ void k_sqrt_clamp(const double* __restrict__ lam, int n, double* __restrict__ sig) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    sig[i] = sqrt(fmax(lam[i], 0.0));
+}
+
+static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
+                          int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
+                          int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
+                          int64_t* k, double* truncerr, double* docut, int method, int precision);
+
 extern "C" int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
                              int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
                              int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
                              int64_t* k, double* truncerr, double* docut) {
+  return svd_trunc_impl(h, m, n, A, lda, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff,
+                        legacy_gpu, U, S, V, k, truncerr, docut, ITG_SVD_AUTO, ITG_PREC_FP64);
+}
+
+extern "C" int itg_svd_trunc_ex(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
+                                int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
+                                int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
+                                int64_t* k, double* truncerr, double* docut, int method,
+                                int precision) {
+  if (method != ITG_SVD_AUTO && method != ITG_SVD_JACOBI && method != ITG_SVD_MIXED)
+    return itg_fail(h, ITG_ERR_INVALID, "unknown SVD method %d", method);
+  if (precision != ITG_PREC_FP64 && precision != ITG_PREC_SPLIT)
+    return itg_fail(h, ITG_ERR_INVALID, "unknown precision %d", precision);
+  return svd_trunc_impl(h, m, n, A, lda, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff,
+                        legacy_gpu, U, S, V, k, truncerr, docut, method, precision);
+}
+
+static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
+                          int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
+                          int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
+                          int64_t* k, double* truncerr, double* docut, int method, int precision) {
   if (!h || m < 0 || n < 0 || lda < m || !A || !U || !S || !V) return ITG_ERR_INVALID;
   if (m == 0 || n == 0) {
     if (k) *k = 0;
@@ -451,9 +489,17 @@ extern "C" int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* 
   // scratch: W (mm*nn) | Vw (nn*nn) | sig (nn) | S,P (2 nn) | order (nn ints) | out3 | flag
   size_t off = 0;
   auto take = [&](size_t bytes) { size_t o = off; off += itg_align256(bytes); return o; };
+  const bool mixed = method == ITG_SVD_MIXED || (method == ITG_SVD_AUTO && nn > ONECTA_MAX_N);
   size_t oW = take(sizeof(double) * mm * nn), oV = take(sizeof(double) * nn * nn),
          oSig = take(sizeof(double) * nn), oP = take(sizeof(double) * nn),
          oOrd = take(sizeof(int) * nn), oOut = take(4 * sizeof(double)), oFlag = take(sizeof(int));
+  size_t oLam = 0, oUw = 0, oWs = 0, oWs32 = 0;
+  if (mixed) {
+    oLam = take(sizeof(double) * nn);
+    oUw = take(sizeof(double) * mm * nn);
+    oWs = take(sizeof(double) * itg::svd_mixed_ws_doubles(mm, nn));
+    oWs32 = take(sizeof(float) * (mm * nn + nn * nn));
+  }
   ITG_TRY(itg_scratch_reserve(h, off));
   char* base = (char*)h->scratch;
   double* W = (double*)(base + oW);
@@ -471,20 +517,35 @@ extern "C" int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* 
     ITG_TRY(itg::transpose(h, m, n, A, lda, W));
   }
   int sweeps = 0;
-  int st = jacobi_run(h, W, mm, nn, Vw, flag, &sweeps);
-  if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED) return st;
-  k_unit_cols<<<(unsigned)nn, 256, 0, h->stream>>>(Vw, nn);
-  k_col_norms<<<(unsigned)nn, 256, 0, h->stream>>>(W, mm, sig);
-  k_rank_desc<<<itg_blocks_for(nn, 256, 1024), 256, 0, h->stream>>>(sig, (int)nn, 0.0, order, S, P, 1);
-  ITG_CHECK_LAUNCH(h);
-  ITG_TRY(itg::truncate_dev(h, P, nn, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, out3));
-  // Left factor of the working problem = W[:, order] / sig; right = Vw[:, order].
+  int st = ITG_OK;
   double* Uw_dst = tr ? V : U;  // rows mm
   double* Vw_dst = tr ? U : V;  // rows nn
   dim3 g1(itg_blocks_for(mm, 256, 64), (unsigned)nn), g2(itg_blocks_for(nn, 256, 64), (unsigned)nn);
-  k_gather_cols<<<g1, 256, 0, h->stream>>>(W, mm, order, sig, 1, (int)nn, Uw_dst, mm);
-  k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, nn, order, sig, 0, (int)nn, Vw_dst, nn);
-  ITG_CHECK_LAUNCH(h);
+  if (mixed) {
+    double* lam = (double*)(base + oLam);
+    double* Uw = (double*)(base + oUw);
+    ITG_TRY(itg::svd_mixed_core(h, W, mm, nn, precision, Vw, lam, Uw, (double*)(base + oWs),
+                                (float*)(base + oWs32), flag, &sweeps));
+    k_sqrt_clamp<<<itg_blocks_for(nn, 256, 64), 256, 0, h->stream>>>(lam, (int)nn, sig);
+    k_rank_desc<<<itg_blocks_for(nn, 256, 1024), 256, 0, h->stream>>>(sig, (int)nn, 0.0, order, S, P, 1);
+    ITG_CHECK_LAUNCH(h);
+    ITG_TRY(itg::truncate_dev(h, P, nn, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, out3));
+    k_gather_cols<<<g1, 256, 0, h->stream>>>(Uw, mm, order, sig, 0, (int)nn, Uw_dst, mm);
+    k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, nn, order, sig, 0, (int)nn, Vw_dst, nn);
+    ITG_CHECK_LAUNCH(h);
+  } else {
+    st = jacobi_run(h, W, mm, nn, Vw, flag, &sweeps);
+    if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED) return st;
+    k_unit_cols<<<(unsigned)nn, 256, 0, h->stream>>>(Vw, nn);
+    k_col_norms<<<(unsigned)nn, 256, 0, h->stream>>>(W, mm, sig);
+    k_rank_desc<<<itg_blocks_for(nn, 256, 1024), 256, 0, h->stream>>>(sig, (int)nn, 0.0, order, S, P, 1);
+    ITG_CHECK_LAUNCH(h);
+    ITG_TRY(itg::truncate_dev(h, P, nn, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, out3));
+    // Left factor of the working problem = W[:, order] / sig; right = Vw[:, order].
+    k_gather_cols<<<g1, 256, 0, h->stream>>>(W, mm, order, sig, 1, (int)nn, Uw_dst, mm);
+    k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, nn, order, sig, 0, (int)nn, Vw_dst, nn);
+    ITG_CHECK_LAUNCH(h);
+  }
   ITG_TRY(read_out3(h, out3, k, truncerr, docut));
   if (st == ITG_ERR_NOTCONVERGED)
     return itg_fail(h, ITG_ERR_NOTCONVERGED, "Jacobi SVD did not converge in %d sweeps", sweeps);

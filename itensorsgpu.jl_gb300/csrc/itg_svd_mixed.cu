@@ -1,0 +1,293 @@
+// Large-matrix SVD by FP32 one-sided Jacobi plus FP64-accurate refinement.
+//
+// GB300 runs FP32 about 60x faster than FP64, so the O(n^3) scalar work of
+// Jacobi is done in FP32 and every later O(n^3) step is a matrix product run by
+// the contraction engine (FP64 gather-GEMM, or the split-precision tensor-core
+// path, which is FP64-accurate):
+//
+//  1. W32 = float(A); one-sided Jacobi sweeps in FP32 (same round-robin pairs
+//     and rotation formula as the FP64 kernels) until |w_p.w_q| <= 1e-5 |w_p||w_q|.
+//  2. Refine X = double(V32) as eigenvectors of G = A^T A.  Per iteration
+//       R = I - X^T X,  S = X^T (G X),  l_i = s_ii / (1 - r_ii),
+//       e_ij = (s_ij + l_j r_ij) / (l_j - l_i)  (i != j, |l_j - l_i| > delta),
+//       e_ij = r_ij / 2                          (diagonal and clustered pairs),
+//       X <- X + X E.
+//     These are the first-order conditions for X(I+E) to be orthonormal
+//     (E + E^T = R) and to diagonalise S (s_ij + e_ji l_j + l_i e_ij = 0), the
+//     scheme of Ogita & Aishima, "Iterative refinement for symmetric eigenvalue
+//     decomposition", Japan J. Indust. Appl. Math. 35 (2018).  Convergence is
+//     quadratic; clustered (degenerate) pairs only get their orthogonality
+//     restored, which leaves any basis of a degenerate subspace.
+//  3. sigma_i = sqrt(max(l_i, 0)), U = A X diag(1/sigma), then one Newton-
+//     Schulz step U <- U + U (I - U^T U)/2 to restore orthonormality.
+// Singular values are accurate to ~eps * sigma_max absolute (the spectrum
+// P = sigma^2 that truncation uses to ~eps * P_max), which is what DMRG
+// truncation needs.
+#include "itg_internal.cuh"
+
+#include <cmath>
+
+namespace itg {
+int contract_f64(itg_handle* h, double alpha, const double* A, int rankA, const int64_t* dimsA,
+                 const int32_t* modesA, const double* B, int rankB, const int64_t* dimsB,
+                 const int32_t* modesB, double beta, double* C, int rankC, const int64_t* dimsC,
+                 const int32_t* modesC, int precision);
+}
+
+namespace {
+
+__device__ __forceinline__ int rr_player32(int pos, int step, int np) {
+  if (pos == 0) return 0;
+  return ((pos - 1 + step) % (np - 1)) + 1;
+}
+
+__device__ __forceinline__ float warp_sumf(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// One round-robin step of FP32 one-sided Jacobi: one CTA per column pair.
+__global__ void __launch_bounds__(256)
+k_jacobi32_step(float* __restrict__ W, int64_t m, int n, float* __restrict__ V, float tol, int step,
+                int* __restrict__ rotated) {
+  __shared__ float sh[3][8];
+  const int np = n + (n & 1);
+  int p = rr_player32(blockIdx.x, step, np), q = rr_player32(np - 1 - blockIdx.x, step, np);
+  if (p >= n || q >= n) return;
+  if (p > q) { int t = p; p = q; q = t; }
+  float* wp = W + (int64_t)p * m;
+  float* wq = W + (int64_t)q * m;
+  float a = 0.f, b = 0.f, g = 0.f;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+    float x = wp[i], y = wq[i];
+    a = fmaf(x, x, a);
+    b = fmaf(y, y, b);
+    g = fmaf(x, y, g);
+  }
+  a = warp_sumf(a); b = warp_sumf(b); g = warp_sumf(g);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { sh[0][warp] = a; sh[1][warp] = b; sh[2][warp] = g; }
+  __syncthreads();
+  a = 0.f; b = 0.f; g = 0.f;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a += sh[0][w]; b += sh[1][w]; g += sh[2][w]; }
+  if (a == 0.f || b == 0.f || fabsf(g) <= tol * sqrtf(a) * sqrtf(b)) return;
+  const float zeta = (b - a) / (2.f * g);
+  const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+  const float c = 1.f / sqrtf(1.f + t * t), s = c * t;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+    float x = wp[i], y = wq[i];
+    wp[i] = c * x - s * y;
+    wq[i] = s * x + c * y;
+  }
+  float* vp = V + (int64_t)p * n;
+  float* vq = V + (int64_t)q * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    float x = vp[i], y = vq[i];
+    vp[i] = c * x - s * y;
+    vq[i] = s * x + c * y;
+  }
+  if (threadIdx.x == 0) *rotated = 1;
+}
+
+__global__ void k_to_float(const double* __restrict__ A, int64_t lda, int64_t m, int64_t n, bool transpose,
+                           float* __restrict__ W) {
+  const int64_t total = m * n;  // W is (rows x cols) = transpose ? (n x m) : (m x n)
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    if (!transpose) {
+      int64_t j = t / m, i = t - j * m;
+      W[t] = (float)A[i + j * lda];
+    } else {
+      int64_t j = t / n, i = t - j * n;  // W[i, j] = A[j, i], W rows = n
+      W[t] = (float)A[j + i * lda];
+    }
+  }
+}
+
+__global__ void k_identity32(int n, float* __restrict__ V) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn;
+       i += (int64_t)gridDim.x * blockDim.x)
+    V[i] = (i % (n + 1) == 0) ? 1.f : 0.f;
+}
+
+__global__ void k_to_double(const float* __restrict__ x, int64_t n, double* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+
+// lam[i] = s_ii / (1 - r_ii) with R = I - P (P = X^T X), S given.
+__global__ void k_refine_lambda(const double* __restrict__ P, const double* __restrict__ S, int n,
+                                double* __restrict__ lam) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double rii = 1.0 - P[i + (int64_t)i * n];
+    lam[i] = S[i + (int64_t)i * n] / (1.0 - rii);
+  }
+}
+
+// E (n x n) from P = X^T X and S = X^T G X; delta = cluster threshold (absolute).
+__global__ void k_refine_E(const double* __restrict__ P, const double* __restrict__ S,
+                           const double* __restrict__ lam, int n, double delta, double* __restrict__ E) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nn;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(t / n), i = (int)(t - (int64_t)j * n);
+    const double rij = (i == j ? 1.0 : 0.0) - P[t];
+    double e;
+    if (i == j) {
+      e = 0.5 * rij;
+    } else {
+      const double d = lam[j] - lam[i];
+      e = (fabs(d) > delta) ? (S[t] + lam[j] * rij) / d : 0.5 * rij;
+    }
+    E[t] = e;
+  }
+}
+
+// Q = I - P  (for Newton-Schulz: U <- U + U (I - U^T U)/2, written as 0.5*(I-P))
+__global__ void k_half_identity_minus(const double* __restrict__ P, int n, double* __restrict__ Q) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nn;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(t / n), i = (int)(t - (int64_t)j * n);
+    Q[t] = 0.5 * ((i == j ? 1.0 : 0.0) - P[t]);
+  }
+}
+
+// inv[j] = 1/sigma_j, 0 when sigma is numerically zero.
+__global__ void k_inv_sigma(const double* __restrict__ lam, int n, double floor_sig,
+                            double* __restrict__ inv) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double s = sqrt(fmax(lam[i], 0.0));
+    inv[i] = (s > floor_sig) ? 1.0 / s : 0.0;
+  }
+}
+
+// U[:, j] *= inv[j].
+__global__ void k_scale_cols(double* __restrict__ U, int64_t m, int n, const double* __restrict__ inv) {
+  const int64_t total = m * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x)
+    U[t] *= inv[t / m];
+}
+
+__global__ void k_max_abs(const double* __restrict__ x, int n, double* __restrict__ out) {
+  __shared__ double sh[32];
+  double mx = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, fabs(x[i]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) b = fmax(b, sh[i]);
+    *out = b;
+  }
+}
+
+// C (rows x cols) = alpha * op(A) * B + beta * C for column-major square-ish blocks:
+// tA = 1 uses A^T.  A is (ka x ra) when transposed, B is (k x cb).
+int gemm(itg_handle* h, bool tA, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
+         const double* B, double beta, double* C, int precision) {
+  const int64_t dA[2] = {tA ? K : M, tA ? M : K};
+  const int32_t mA[2] = {tA ? 3 : 1, tA ? 1 : 3};
+  const int64_t dB[2] = {K, N};
+  const int32_t mB[2] = {3, 2};
+  const int64_t dC[2] = {M, N};
+  const int32_t mC[2] = {1, 2};
+  return itg::contract_f64(h, alpha, A, 2, dA, mA, B, 2, dB, mB, beta, C, 2, dC, mC, precision);
+}
+
+}  // namespace
+
+namespace itg {
+
+// Mixed-precision SVD of the working matrix (rows mm >= cols nn).  Outputs the
+// unsorted right vectors X (nn x nn), lam (nn, = sigma^2) and the left vectors
+// Uw (mm x nn).  `Awork` is the FP64 working matrix (mm x nn, ld = mm).
+int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, int precision,
+                   double* X, double* lam, double* Uw, double* ws, float* ws32, int* flag,
+                   int* sweeps_out) {
+  const int n = (int)nn;
+  // 1. FP32 Jacobi
+  float* W32 = ws32;
+  float* V32 = ws32 + mm * nn;
+  k_to_float<<<itg_blocks_for(mm * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(Awork, mm, mm, nn, false, W32);
+  k_identity32<<<itg_blocks_for(nn * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(n, V32);
+  ITG_CHECK_LAUNCH(h);
+  const int np = n + (n & 1);
+  int* hp = (int*)h->pinned;
+  int sweeps = 0;
+  for (; sweeps < 40; ++sweeps) {
+    ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+    for (int step = 0; step < np - 1; ++step)
+      k_jacobi32_step<<<np / 2, 256, 0, h->stream>>>(W32, mm, n, V32, 1e-5f, step, flag);
+    ITG_CHECK_LAUNCH(h);
+    ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hp[0] == 0) break;
+  }
+  *sweeps_out = sweeps + 1;
+  // 2. refinement of X on G = A^T A
+  // G P Q E Xn (nn^2 each) | S (max(mm*nn, nn^2), also the copy of U) | max slot
+  double* G = ws;
+  double* P = G + nn * nn;
+  double* Q = P + nn * nn;
+  double* E = Q + nn * nn;
+  double* Xn = E + nn * nn;
+  double* S = Xn + nn * nn;
+  double* mx = S + ((mm * nn > nn * nn) ? mm * nn : nn * nn);
+  k_to_double<<<itg_blocks_for(nn * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(V32, nn * nn, X);
+  ITG_CHECK_LAUNCH(h);
+  ITG_TRY(gemm(h, true, nn, nn, mm, 1.0, Awork, Awork, 0.0, G, precision));  // G = A^T A
+  const int gb = itg_blocks_for(nn * nn, 256, h->num_sms * 16);
+  for (int it = 0; it < 3; ++it) {
+    ITG_TRY(gemm(h, true, nn, nn, nn, 1.0, X, X, 0.0, P, precision));   // P = X^T X
+    ITG_TRY(gemm(h, false, nn, nn, nn, 1.0, G, X, 0.0, Q, precision));  // Q = G X
+    ITG_TRY(gemm(h, true, nn, nn, nn, 1.0, X, Q, 0.0, S, precision));   // S = X^T G X
+    k_refine_lambda<<<itg_blocks_for(nn, 256, 64), 256, 0, h->stream>>>(P, S, n, lam);
+    k_max_abs<<<1, 1024, 0, h->stream>>>(lam, n, mx);
+    ITG_CHECK_LAUNCH(h);
+    ITG_CUDA(h, cudaMemcpyAsync(h->pinned, mx, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    const double lmax = h->pinned[0] > 0.0 ? h->pinned[0] : 1.0;
+    k_refine_E<<<gb, 256, 0, h->stream>>>(P, S, lam, n, 1e-9 * lmax, E);
+    ITG_CHECK_LAUNCH(h);
+    ITG_CUDA(h, cudaMemcpyAsync(Xn, X, sizeof(double) * nn * nn, cudaMemcpyDeviceToDevice, h->stream));
+    ITG_TRY(gemm(h, false, nn, nn, nn, 1.0, X, E, 1.0, Xn, precision));  // X <- X + X E
+    ITG_CUDA(h, cudaMemcpyAsync(X, Xn, sizeof(double) * nn * nn, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  // final eigenvalues from the refined X
+  ITG_TRY(gemm(h, true, nn, nn, nn, 1.0, X, X, 0.0, P, precision));
+  ITG_TRY(gemm(h, false, nn, nn, nn, 1.0, G, X, 0.0, Q, precision));
+  ITG_TRY(gemm(h, true, nn, nn, nn, 1.0, X, Q, 0.0, S, precision));
+  k_refine_lambda<<<itg_blocks_for(nn, 256, 64), 256, 0, h->stream>>>(P, S, n, lam);
+  k_max_abs<<<1, 1024, 0, h->stream>>>(lam, n, mx);
+  ITG_CHECK_LAUNCH(h);
+  ITG_CUDA(h, cudaMemcpyAsync(h->pinned, mx, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  const double smax = sqrt(h->pinned[0] > 0.0 ? h->pinned[0] : 0.0);
+  // 3. U = A X diag(1/sigma), one Newton-Schulz step
+  ITG_TRY(gemm(h, false, mm, nn, nn, 1.0, Awork, X, 0.0, Uw, precision));
+  double* inv = E;  // E is free after the refinement
+  k_inv_sigma<<<itg_blocks_for(nn, 256, 64), 256, 0, h->stream>>>(lam, n, 1e-14 * smax, inv);
+  k_scale_cols<<<itg_blocks_for(mm * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(Uw, mm, n, inv);
+  ITG_CHECK_LAUNCH(h);
+  ITG_TRY(gemm(h, true, nn, nn, mm, 1.0, Uw, Uw, 0.0, P, precision));  // P = U^T U
+  k_half_identity_minus<<<gb, 256, 0, h->stream>>>(P, n, Q);
+  ITG_CHECK_LAUNCH(h);
+  // Uw <- Uw + Uw Q  (through a copy: the product must not alias its operand)
+  double* Ucp = S;  // S is free now; needs mm x nn: ensured by the caller's sizing
+  ITG_CUDA(h, cudaMemcpyAsync(Ucp, Uw, sizeof(double) * mm * nn, cudaMemcpyDeviceToDevice, h->stream));
+  ITG_TRY(gemm(h, false, mm, nn, nn, 1.0, Ucp, Q, 1.0, Uw, precision));
+  return ITG_OK;
+}
+
+size_t svd_mixed_ws_doubles(int64_t mm, int64_t nn) {
+  const int64_t sq = nn * nn;
+  const int64_t s_slot = (mm * nn > sq) ? mm * nn : sq;
+  return (size_t)(5 * sq + s_slot + 64);
+}
+
+}  // namespace itg

@@ -24,6 +24,7 @@ ITG_ERR_TIMEOUT, ITG_ERR_NOTCONVERGED, ITG_ERR_UNSUPPORTED = 5, 6, 7
 ITG_F64 = 0
 PREC_FP64, PREC_SPLIT = 0, 1
 KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_SPLIT_PREP = 0, 1, 2
+SVD_AUTO, SVD_JACOBI, SVD_MIXED = 0, 1, 2
 
 
 class ITGError(RuntimeError):
@@ -93,6 +94,9 @@ SIGNATURES = {
     "itg_svd_trunc": (C.c_int, [_P, C.c_int64, C.c_int64, _P, C.c_int64,
                                 C.c_int64, C.c_int64, C.c_double, C.c_int, C.c_int, C.c_int,
                                 _P, _P, _P, _I64P, _DP, _DP]),
+    "itg_svd_trunc_ex": (C.c_int, [_P, C.c_int64, C.c_int64, _P, C.c_int64,
+                                   C.c_int64, C.c_int64, C.c_double, C.c_int, C.c_int, C.c_int,
+                                   _P, _P, _P, _I64P, _DP, _DP, C.c_int, C.c_int]),
     "itg_eigh_trunc": (C.c_int, [_P, C.c_int64, _P, C.c_int64,
                                  C.c_int64, C.c_int64, C.c_double, C.c_int, C.c_int, C.c_int,
                                  _P, _P, _I64P, _DP, _DP]),

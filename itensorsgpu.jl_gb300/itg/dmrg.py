@@ -6,9 +6,10 @@ test/dmrg.jl:27,75 of the reference) sweeps bonds b = 1..N-1 and back
 lowest eigenvector of the ProjMPO effective Hamiltonian, factorises it with a
 truncated SVD (``replacebond!``/``factorize``) and updates the projected
 environments.  This module does the same with every tensor operation in
-libitg.so: Davidson with the fused H_eff chain (itg_davidson_heff2), Jacobi SVD
-with on-device truncation (itg_svd_trunc), gather/scale Diag kernels for S and
-gather-GEMM contractions for the environments.  The host only orchestrates.
+libitg.so: Davidson with the H_eff chain (itg_davidson_heff2), the truncated
+SVD with on-device truncation (itg_svd_trunc_ex), gather/scale Diag kernels for
+S and gather-GEMM contractions for the environments, all at the run's
+precision.  The host only orchestrates.
 """
 from __future__ import annotations
 
@@ -189,12 +190,16 @@ def _orthogonalize_left_end(h, ch: _Chain):
 
 def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int = 2,
          eigsolve_tol: float = 1e-14, precision: str | int = "fp64", legacy_gpu_truncate: bool = False,
+         svd_method: int = 0,
          outputlevel: int = 0, return_result: bool = False):
     """Ground state by two-site DMRG.  Returns (energy, psi) like ITensors' dmrg.
 
     krylovdim / maxiter: Davidson subspace size before a restart and number of
     restarts per bond.  precision "split" runs the chi^3 contractions of the
-    eigensolver on the tensor cores (FP64 operands split into bf16 slices).
+    eigensolver and the matrix products of the large-matrix SVD on the tensor
+    cores (FP64 operands split into exact bf16 digit products).  svd_method:
+    0 auto (Jacobi up to 192 columns, mixed FP32-Jacobi + refinement above),
+    1 FP64 Jacobi, 2 mixed.
     """
     if isinstance(precision, str):
         precision = {"fp64": PREC_FP64, "split": PREC_SPLIT}[precision.lower()]
@@ -217,7 +222,7 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
     Renv[N] = (one, (1, 1, 1))
     for j in range(N - 1, 1, -1):
         Renv[j] = _env_right(h, Renv[j + 1][0], Renv[j + 1][1], ch.A[j], ch.Ad[j], ch.W[j], ch.Wd[j],
-                             PREC_FP64)
+                             precision)
     energy = 0.0
     records = []
     for sw in range(sweeps.nsweep):
@@ -254,10 +259,10 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
             te = C.c_double()
             dc = C.c_double()
             try:
-                h.call("itg_svd_trunc", C.c_int64(m), C.c_int64(n), _ptr(phi), C.c_int64(m),
+                h.call("itg_svd_trunc_ex", C.c_int64(m), C.c_int64(n), _ptr(phi), C.c_int64(m),
                        C.c_int64(maxdim), C.c_int64(mindim), C.c_double(cutoff), 0, 1,
                        int(legacy_gpu_truncate), _ptr(U), _ptr(S), _ptr(V), C.byref(k), C.byref(te),
-                       C.byref(dc))
+                       C.byref(dc), int(svd_method), int(precision))
             except NotConverged:
                 pass  # factors are still returned; the rotation limit is generous
             kk = int(k.value)
@@ -272,7 +277,7 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
                 ch.A[b + 1] = _diag_raw(h, Sk, (kk, kk), [1, 2], Vk, (d2, c, kk), [3, 4, 1],
                                         (kk, d2, c), [2, 3, 4])
                 ch.Ad[b + 1] = (kk, d2, c)
-                Lenv[b + 1] = _env_left(h, Lt, Ld, ch.A[b], ch.Ad[b], W1, W1d, PREC_FP64)
+                Lenv[b + 1] = _env_left(h, Lt, Ld, ch.A[b], ch.Ad[b], W1, W1d, precision)
             else:
                 # A_b[a, d1, k] = U[(a d1), k] S[k];  A_{b+1} = V^T
                 ch.A[b] = _diag_raw(h, Sk, (kk, kk), [1, 2], Uk, (a, d1, kk), [3, 4, 1],
@@ -280,7 +285,7 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
                 ch.Ad[b] = (a, d1, kk)
                 ch.A[b + 1] = _permute_raw(h, Vk, (d2, c, kk), [1, 2, 3], [3, 1, 2])
                 ch.Ad[b + 1] = (kk, d2, c)
-                Renv[b + 1] = _env_right(h, Rt, Rd, ch.A[b + 1], ch.Ad[b + 1], W2, W2d, PREC_FP64)
+                Renv[b + 1] = _env_right(h, Rt, Rd, ch.A[b + 1], ch.Ad[b + 1], W2, W2d, precision)
         h.call("itg_synchronize")
         rec = SweepRecord(energy, max(x[2] for x in ch.Ad[:-1]), maxerr, time.perf_counter() - t0, nmv_tot)
         records.append(rec)

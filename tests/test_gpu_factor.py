@@ -122,6 +122,43 @@ def test_svd_truncation_matches_oracle(gpu):
         assert spec.truncerr == pytest.approx(te, rel=1e-9, abs=1e-16)
 
 
+@pytest.mark.parametrize("n,prec", [(300, 0), (512, 1), (1024, 1)])
+def test_svd_mixed_haar_exp_spectrum(gpu, n, prec):
+    """The Jacobi-SVD microbench matrix: A = U diag(exp(-k/20)) V^T with Haar U, V;
+    mixed path (FP32 Jacobi + refinement, products at FP64 or split precision)."""
+    from itg import _lib
+    import torch
+    rng = np.random.default_rng(n)
+    Q1, R1 = np.linalg.qr(rng.standard_normal((n, n)))
+    Q1 *= np.sign(np.diag(R1))
+    Q2, R2 = np.linalg.qr(rng.standard_normal((n, n)))
+    Q2 *= np.sign(np.diag(R2))
+    s = np.exp(-np.arange(n) / 20.0)
+    M = (Q1 * s) @ Q2.T
+    h = _lib.handle(0)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    A = torch.from_numpy(O.flat(M).copy()).cuda()
+    U = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    S = torch.empty(n, dtype=torch.float64, device="cuda")
+    V = torch.empty_like(U)
+    k, te, dc = C.c_int64(), C.c_double(), C.c_double()
+    h.call("itg_svd_trunc_ex", C.c_int64(n), C.c_int64(n), p(A), C.c_int64(n), C.c_int64(0), C.c_int64(1),
+           C.c_double(1e-12), 0, 1, 0, p(U), p(S), p(V), C.byref(k), C.byref(te), C.byref(dc), 2, prec)
+    kk = k.value
+    Uo, So, Vo, teo, _ = O.svd_trunc(M, cutoff=1e-12)
+    assert kk == len(So)
+    Sh = S.cpu().numpy()[:kk]
+    assert np.abs(Sh - So).max() < 1e-13
+    Uh = O.unflat(U.cpu().numpy()[: n * kk], (n, kk))
+    Vh = O.unflat(V.cpu().numpy()[: n * kk], (n, kk))
+    assert np.abs(Uh.T @ Uh - np.eye(kk)).max() < 1e-12
+    assert np.abs(Vh.T @ Vh - np.eye(kk)).max() < 1e-12
+    Mk = (Uh * Sh) @ Vh.T
+    Mo = (Uo * So) @ Vo.T
+    assert np.abs(Mk - Mo).max() < 1e-12
+    assert te.value == pytest.approx(teo, rel=1e-6, abs=1e-20)
+
+
 def test_qr(gpu):
     I = gpu.Index
     i, j, k, l = I(2), I(3), I(4), I(5)
