@@ -215,9 +215,11 @@ ITG_API int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* A, 
  *                  right singular vectors as eigenvectors of A^T A (matrix
  *                  products through the contraction engine at `precision`),
  *                  U = A V / sigma and one Newton-Schulz orthonormalisation.
- *                  Singular values to ~eps * sigma_max absolute.
- *  ITG_SVD_AUTO  : Jacobi for min(m, n) <= 192, mixed above (itg_svd_trunc
- *                  uses AUTO with ITG_PREC_FP64). */
+ *                  P = sigma^2 to ~eps * P_max absolute (sigma_j to
+ *                  ~eps * sigma_max^2 / sigma_j): exact for truncation, and
+ *                  full accuracy for sigma_j above ~1e-4 sigma_max.
+ *  ITG_SVD_AUTO  : Jacobi for min(m, n) <= 192, mixed above.
+ * itg_svd_trunc always uses ITG_SVD_JACOBI (LAPACK-level accuracy). */
 enum { ITG_SVD_AUTO = 0, ITG_SVD_JACOBI = 1, ITG_SVD_MIXED = 2 };
 ITG_API int itg_svd_trunc_ex(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
                              int64_t maxdim, int64_t mindim, double cutoff,
@@ -296,6 +298,73 @@ ITG_API int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int64_
                        const double* L, const double* W1, const double* W2, const double* R,
                        double* psi, int krylovdim, int maxiter, double tol, int precision,
                        double* energy, int* nmatvec);
+
+/* ----------------------------------------- learned Davidson preconditioner */
+/* A per-element MLP (F inputs -> 128 -> 128 -> 1, ReLU, BF16 weights, FP32
+ * accumulation; FP32 master weights with Adam) with hand-written forward,
+ * backward and optimizer kernels.  No counterpart in the reference: it stands
+ * in for the diagonal preconditioner of the eigensolver.  X is element-major
+ * (n x F floats). */
+ITG_API int itg_mlp_create(itg_handle* h, int in_dim, uint64_t seed, void** mlp);
+ITG_API int itg_mlp_destroy(itg_handle* h, void* mlp);
+ITG_API int itg_mlp_num_params(void* mlp, int64_t* n);
+ITG_API int itg_mlp_get_params(itg_handle* h, void* mlp, float* host);
+ITG_API int itg_mlp_set_params(itg_handle* h, void* mlp, const float* host);
+/* g[e] = network(X[e, :]) */
+ITG_API int itg_mlp_forward(itg_handle* h, void* mlp, int64_t n, const float* X, float* g);
+/* loss = mean_e (g[e] mult[e] - target[e])^2; writes the gradient w.r.t. the
+ * master parameters to grad (device, num_params floats, may be NULL), the loss
+ * to *loss (host, may be NULL), then takes one Adam step when lr > 0. */
+ITG_API int itg_mlp_train_step(itg_handle* h, void* mlp, int64_t n, const float* X, const float* mult,
+                               const float* target, float lr, float* grad, float* loss);
+/* Features of the learned preconditioner for the residual r of the two-site
+ * problem (F = 5): normalised residual, (diag - theta)/scale, clipped inverse,
+ * left / right Schmidt values of each element's link indices (lamL: chiL
+ * values, lamR: chiR values, either may be NULL).  mult = normalised residual. */
+ITG_API int itg_heff2_features(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d,
+                               const double* r, const double* diag, double theta,
+                               const double* lamL, const double* lamR, float* X, float* mult);
+/* itg_davidson_heff2 with the learned preconditioner: corrections are
+ * t = network(features) * r_hat; convergence is still judged by the exact
+ * residual norm, and when a learned correction fails to reduce the residual by
+ * 10% the diagonal preconditioner takes over for the rest of the solve
+ * (*fallbacks counts those hand-overs, may be NULL). */
+ITG_API int itg_davidson_heff2_learned(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d,
+                                       int64_t wL, int64_t wM, int64_t wR,
+                                       const double* L, const double* W1, const double* W2, const double* R,
+                                       double* psi, int krylovdim, int maxiter, double tol, int precision,
+                                       void* mlp, const double* lamL, const double* lamR,
+                                       double* energy, int* nmatvec, int* fallbacks);
+
+/* ------------------------------------------- many independent instances */
+/* Grouped FP64 contraction: `count` contractions with the same ranks and mode
+ * labels but their own dims and pointers (dims arrays concatenated per problem),
+ * C_i = alpha A_i B_i + beta C_i, all tiles of all problems in one launch. */
+ITG_API int itg_contract_grouped(itg_handle* h, int count, double alpha,
+                                 const void* const* A, int rankA, const int64_t* dimsA, const int32_t* modesA,
+                                 const void* const* B, int rankB, const int64_t* dimsB, const int32_t* modesB,
+                                 double beta,
+                                 void* const* C, int rankC, const int64_t* dimsC, const int32_t* modesC);
+
+/* Truncated SVDs of `count` matrices (each min(m, n) <= 512), one CTA per
+ * matrix running FP64 one-sided Jacobi, on-device truncation per instance.
+ * U_i, S_i, V_i sized as for itg_svd_trunc; k and truncerr are host arrays. */
+ITG_API int itg_svd_trunc_batched(itg_handle* h, int count, const int64_t* m, const int64_t* n,
+                                  const double* const* A, const int64_t* maxdim, int64_t mindim,
+                                  double cutoff, int absoluteCutoff, int doRelCutoff, int legacy_gpu,
+                                  double* const* U, double* const* S, double* const* V,
+                                  int64_t* k, double* truncerr);
+
+/* itg_davidson_heff2 for `count` instances sharing d and the MPO bond
+ * dimensions (the same bond of equally long chains), each with its own chiL,
+ * chiR and tensors.  The H_eff chain runs as grouped launches over all
+ * instances; energy and nmatvec are host arrays of length count. */
+ITG_API int itg_davidson_heff2_batched(itg_handle* h, int count, const int64_t* chiL, const int64_t* chiR,
+                                       int64_t d, int64_t wL, int64_t wM, int64_t wR,
+                                       const double* const* L, const double* const* W1,
+                                       const double* const* W2, const double* const* R,
+                                       double* const* psi, int krylovdim, int maxiter, double tol,
+                                       double* energy, int* nmatvec);
 
 #ifdef __cplusplus
 }

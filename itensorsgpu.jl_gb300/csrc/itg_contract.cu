@@ -509,10 +509,21 @@ int contract_grouped_f64(itg_handle* h, int count, double alpha, const double* c
   }
   if (tiles > (int64_t)INT32_MAX) return itg_fail(h, ITG_ERR_UNSUPPORTED, "grouped: too many tiles");
   const size_t bytes = sizeof(GroupProb) * probs.size();
-  ITG_TRY(itg_scratch_reserve(h, bytes));
-  // the descriptor array lives at the end of nothing else: callers of the
-  // grouped path do not hold scratch regions
-  ITG_CUDA(h, cudaMemcpyAsync(h->scratch, probs.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+  if (bytes > h->group_desc_bytes) {
+    if (h->group_desc) {
+      ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+      cudaFree(h->group_desc);
+      h->group_desc = nullptr;
+      h->group_desc_bytes = 0;
+    }
+    const size_t want = itg_align256(bytes * 2);
+    if (cudaMalloc(&h->group_desc, want) != cudaSuccess)
+      return itg_fail(h, ITG_ERR_ALLOC, "grouped descriptor allocation failed");
+    h->group_desc_bytes = want;
+  }
+  // Pageable source: the copy is staged before the call returns, so `probs`
+  // may go out of scope; the stream orders it before the kernel.
+  ITG_CUDA(h, cudaMemcpyAsync(h->group_desc, probs.data(), bytes, cudaMemcpyHostToDevice, h->stream));
   static bool attr = false;
   if (!attr) {
     ITG_CUDA(h, cudaFuncSetAttribute(k_gemm_gather_f64_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -521,7 +532,7 @@ int contract_grouped_f64(itg_handle* h, int count, double alpha, const double* c
   }
   ProfScope prof(h, ITG_KERNEL_GEMM_F64);
   k_gemm_gather_f64_grouped<<<(unsigned)tiles, GTHREADS, GEMM_SMEM, h->stream>>>(
-      (const GroupProb*)h->scratch, count, alpha, beta);
+      (const GroupProb*)h->group_desc, count, alpha, beta);
   ITG_CHECK_LAUNCH(h);
   return ITG_OK;
 }

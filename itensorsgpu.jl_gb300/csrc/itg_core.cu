@@ -130,6 +130,7 @@ extern "C" int itg_destroy(itg_handle* h) {
   if (h->scratch) cudaFree(h->scratch);
   if (h->split_ws) cudaFree(h->split_ws);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+  if (h->group_desc) cudaFree(h->group_desc);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->dev_status) cudaFree(h->dev_status);
   delete h;

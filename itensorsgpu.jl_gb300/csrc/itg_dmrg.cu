@@ -239,6 +239,54 @@ __global__ void k_precond(int64_t n, const double* __restrict__ r, const double*
   }
 }
 
+// Per-element features of the learned preconditioner (F = 5, float, element-major):
+//   f0 = r_e sqrt(n) / |r|                      (normalised residual; also the multiplier)
+//   f1 = (diag_e - theta) / scale               (scale = mean |diag - theta|)
+//   f2 = clamp(scale / (diag_e - theta), -10, 10) / 10
+//   f3 = log10(max(lamL[a], 1e-12)) / 12 + 0.5  (left Schmidt value of the element's a)
+//   f4 = log10(max(lamR[b], 1e-12)) / 12 + 0.5  (right Schmidt value of its b)
+__global__ void k_features(int64_t n, int64_t chiL, int64_t dd, const double* __restrict__ r,
+                           const double* __restrict__ dg, double theta, double rscale, double dscale,
+                           const double* __restrict__ lamL, const double* __restrict__ lamR,
+                           float* __restrict__ X, float* __restrict__ mult) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = e % chiL, b = e / (chiL * dd);
+    const double dv = dg[e] - theta;
+    double inv = dscale / (fabs(dv) > 1e-300 ? dv : 1e-300);
+    inv = inv > 10.0 ? 10.0 : (inv < -10.0 ? -10.0 : inv);
+    const float f0 = (float)(r[e] * rscale);
+    X[e * 5 + 0] = f0;
+    X[e * 5 + 1] = (float)(dv / dscale);
+    X[e * 5 + 2] = (float)(inv / 10.0);
+    X[e * 5 + 3] = lamL ? (float)(log10(fmax(lamL[a], 1e-12)) / 12.0 + 0.5) : 0.f;
+    X[e * 5 + 4] = lamR ? (float)(log10(fmax(lamR[b], 1e-12)) / 12.0 + 0.5) : 0.f;
+    mult[e] = f0;
+  }
+}
+
+// t = g * mult (the learned correction, in FP64)
+__global__ void k_learned_corr(int64_t n, const float* __restrict__ g, const float* __restrict__ mult,
+                               double* __restrict__ t) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    t[e] = (double)g[e] * (double)mult[e];
+}
+
+// out[0] = sum |diag - theta| (block partial sums, reduced on the host side)
+__global__ void k_abs_diff_sum(int64_t n, const double* __restrict__ dg, double theta, double* __restrict__ part) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    s += fabs(dg[e] - theta);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh[i];
+    part[blockIdx.x] = t;
+  }
+}
+
 // y = a*x + b*y with host scalars (x, y length n); b == 0 ignores y's old contents.
 __global__ void k_lincomb(int64_t n, double a, const double* __restrict__ x, double b,
                           double* __restrict__ y) {
@@ -292,11 +340,66 @@ extern "C" int itg_heff2_diag(itg_handle* h, int64_t chiL, int64_t chiR, int64_t
   return ITG_OK;
 }
 
+namespace itg {
+int mlp_forward(itg_handle* h, void* mlp, int64_t n, const float* X, float* g);
+}
+
+static int davidson_impl(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d, int64_t wL, int64_t wM,
+                         int64_t wR, const double* L, const double* W1, const double* W2, const double* R,
+                         double* psi, int krylovdim, int maxiter, double tol, int precision, void* mlp,
+                         const double* lamL, const double* lamR, double* energy, int* nmatvec,
+                         int* fallbacks);
+
 extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d, int64_t wL,
                                   int64_t wM, int64_t wR, const double* L, const double* W1,
                                   const double* W2, const double* R, double* psi, int krylovdim,
                                   int maxiter, double tol, int precision, double* energy,
                                   int* nmatvec) {
+  return davidson_impl(h, chiL, chiR, d, wL, wM, wR, L, W1, W2, R, psi, krylovdim, maxiter, tol, precision,
+                       nullptr, nullptr, nullptr, energy, nmatvec, nullptr);
+}
+
+extern "C" int itg_davidson_heff2_learned(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d, int64_t wL,
+                                          int64_t wM, int64_t wR, const double* L, const double* W1,
+                                          const double* W2, const double* R, double* psi, int krylovdim,
+                                          int maxiter, double tol, int precision, void* mlp,
+                                          const double* lamL, const double* lamR, double* energy,
+                                          int* nmatvec, int* fallbacks) {
+  if (!mlp) return itg_fail(h, ITG_ERR_INVALID, "learned davidson needs a network");
+  return davidson_impl(h, chiL, chiR, d, wL, wM, wR, L, W1, W2, R, psi, krylovdim, maxiter, tol, precision,
+                       mlp, lamL, lamR, energy, nmatvec, fallbacks);
+}
+
+extern "C" int itg_heff2_features(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d, const double* r,
+                                  const double* diag, double theta, const double* lamL, const double* lamR,
+                                  float* X, float* mult) {
+  if (!h || !r || !diag || !X || !mult || chiL <= 0 || chiR <= 0 || d <= 0) return ITG_ERR_INVALID;
+  const int64_t n = chiL * d * d * chiR;
+  ITG_TRY(itg_scratch_reserve(h, sizeof(double) * 600));
+  double* part = (double*)h->scratch;
+  const int nb = itg_blocks_for(n, 256, 512);
+  k_abs_diff_sum<<<nb, 256, 0, h->stream>>>(n, diag, theta, part);
+  ITG_CHECK_LAUNCH(h);
+  std::vector<double> hp(nb);
+  ITG_CUDA(h, cudaMemcpyAsync(hp.data(), part, sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));
+  double rn = 0.0;
+  ITG_TRY(itg_nrm2(h, n, r, &rn));
+  double ds = 0.0;
+  for (double x : hp) ds += x;
+  ds = ds / (double)n;
+  if (!(ds > 0.0)) ds = 1.0;
+  const double rs = rn > 0.0 ? std::sqrt((double)n) / rn : 0.0;
+  k_features<<<itg_blocks_for(n, 256, h->num_sms * 8), 256, 0, h->stream>>>(n, chiL, d * d, r, diag, theta, rs,
+                                                                           ds, lamL, lamR, X, mult);
+  ITG_CHECK_LAUNCH(h);
+  return ITG_OK;
+}
+
+static int davidson_impl(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d, int64_t wL, int64_t wM,
+                         int64_t wR, const double* L, const double* W1, const double* W2, const double* R,
+                         double* psi, int krylovdim, int maxiter, double tol, int precision, void* mlp,
+                         const double* lamL, const double* lamR, double* energy, int* nmatvec,
+                         int* fallbacks) {
   if (!h || !L || !W1 || !W2 || !R || !psi || !energy) return ITG_ERR_INVALID;
   HeffDims D{chiL, chiR, d, wL, wM, wR};
   ITG_TRY(heff_validate(h, D));
@@ -312,6 +415,8 @@ extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int
          oR = take(sizeof(double) * n), oSm = take(sizeof(double) * (kmax * kmax + 4 * kmax + 8)),
          oPart = take(sizeof(double) * 1024);
   size_t oXg = take(h->use_graphs ? sizeof(double) * n : 0), oYg = take(h->use_graphs ? sizeof(double) * n : 0);
+  size_t oFx = take(mlp ? sizeof(float) * n * 5 : 0), oFm = take(mlp ? sizeof(float) * n : 0),
+         oFg = take(mlp ? sizeof(float) * n : 0), oFp = take(mlp ? sizeof(double) * 600 : 0);
   ITG_TRY(itg_scratch_reserve(h, off));
   char* base = (char*)h->scratch;
   HeffWork w = heff_carve(D, base + oH);
@@ -325,6 +430,14 @@ extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int
   double* part = (double*)(base + oPart);
   double* Xg = (double*)(base + oXg);
   double* Yg = (double*)(base + oYg);
+  float* Fx = (float*)(base + oFx);
+  float* Fm = (float*)(base + oFm);
+  float* Fg = (float*)(base + oFg);
+  double* Fp = (double*)(base + oFp);
+  bool use_learned = mlp != nullptr;
+  int nfallback = 0;
+  double rn_prev = -1.0;
+  bool last_was_learned = false;
   double* hp = h->pinned;
   const int gb = itg_blocks_for(n, 256, h->num_sms * 8);
 
@@ -417,6 +530,14 @@ extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int
       k_lincomb<<<gb, 256, 0, h->stream>>>(n, -theta, X, 1.0, Rv);
       ITG_CHECK_LAUNCH(h);
       ITG_TRY(nrm(Rv, rn));
+      // stall rule: a learned correction that did not cut the residual by 10%
+      // hands the rest of this solve to the diagonal preconditioner
+      if (last_was_learned && rn_prev > 0.0 && rn > 0.9 * rn_prev) {
+        use_learned = false;
+        nfallback++;
+      }
+      rn_prev = rn;
+      last_was_learned = false;
       if (rn < tol || k == kmax) break;
       // correction t = (diag - theta)^-1 r, orthogonalised twice against V.  When
       // the orthogonalisation cancels all but 1e-6 of it (the preconditioned
@@ -425,10 +546,29 @@ extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int
       const double guard = 1e-8 * (fabs(theta) > 1.0 ? fabs(theta) : 1.0);
       double tn = 0.0;
       for (int attempt = 0; attempt < 2; ++attempt) {
-        if (attempt == 0) {
+        if (attempt == 0 && use_learned) {
+          // learned correction t = g(features) * r_hat
+          const int nb = itg_blocks_for(n, 256, 512);
+          k_abs_diff_sum<<<nb, 256, 0, h->stream>>>(n, dg, theta, Fp);
+          ITG_CHECK_LAUNCH(h);
+          ITG_CUDA(h, cudaMemcpyAsync(hp, Fp, sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));
+          ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+          double ds = 0.0;
+          for (int q = 0; q < nb; ++q) ds += hp[q];
+          ds /= (double)n;
+          if (!(ds > 0.0)) ds = 1.0;
+          const double rs = rn > 0.0 ? std::sqrt((double)n) / rn : 0.0;
+          k_features<<<gb, 256, 0, h->stream>>>(n, chiL, d * d, Rv, dg, theta, rs, ds, lamL, lamR, Fx, Fm);
+          ITG_CHECK_LAUNCH(h);
+          ITG_TRY(itg::mlp_forward(h, mlp, n, Fx, Fg));
+          k_learned_corr<<<gb, 256, 0, h->stream>>>(n, Fg, Fm, t);
+          ITG_CHECK_LAUNCH(h);
+          last_was_learned = true;
+        } else if (attempt == 0) {
           k_precond<<<gb, 256, 0, h->stream>>>(n, Rv, dg, theta, guard, t);
           ITG_CHECK_LAUNCH(h);
         } else {
+          last_was_learned = false;
           ITG_CUDA(h, cudaMemcpyAsync(t, Rv, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
         }
         double t0 = 0.0;
@@ -463,5 +603,6 @@ extern "C" int itg_davidson_heff2(itg_handle* h, int64_t chiL, int64_t chiR, int
   ITG_CUDA(h, cudaStreamSynchronize(h->stream));
   *energy = theta;
   if (nmatvec) *nmatvec = nmv;
+  if (fallbacks) *fallbacks = nfallback;
   return ITG_OK;
 }

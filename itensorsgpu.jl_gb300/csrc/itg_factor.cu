@@ -456,7 +456,7 @@ extern "C" int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* 
                              int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
                              int64_t* k, double* truncerr, double* docut) {
   return svd_trunc_impl(h, m, n, A, lda, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff,
-                        legacy_gpu, U, S, V, k, truncerr, docut, ITG_SVD_AUTO, ITG_PREC_FP64);
+                        legacy_gpu, U, S, V, k, truncerr, docut, ITG_SVD_JACOBI, ITG_PREC_FP64);
 }
 
 extern "C" int itg_svd_trunc_ex(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,

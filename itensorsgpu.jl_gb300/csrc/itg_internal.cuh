@@ -55,6 +55,10 @@ struct itg_handle {
   std::unordered_map<std::string, std::shared_ptr<ContractPlan>> plans;
   // Device status word for bounded waits (ITG_ERR_TIMEOUT reporting).
   int* dev_status = nullptr;
+  // Descriptor array of grouped launches (separate from scratch: grouped calls
+  // run inside callers that hold scratch regions).
+  void* group_desc = nullptr;
+  size_t group_desc_bytes = 0;
   // CUDA-graph replay of the H_eff chain inside Davidson (itg_set_graphs).
   bool use_graphs = false;
   cudaStream_t cap_stream = nullptr;

@@ -20,9 +20,13 @@
 //     restored, which leaves any basis of a degenerate subspace.
 //  3. sigma_i = sqrt(max(l_i, 0)), U = A X diag(1/sigma), then one Newton-
 //     Schulz step U <- U + U (I - U^T U)/2 to restore orthonormality.
-// Singular values are accurate to ~eps * sigma_max absolute (the spectrum
-// P = sigma^2 that truncation uses to ~eps * P_max), which is what DMRG
-// truncation needs.
+// Accuracy: P = sigma^2 (what truncation uses) to ~eps * P_max absolute, so
+// sigma_j to ~eps * sigma_max^2 / sigma_j: full FP64 accuracy for the
+// singular values above ~1e-4 sigma_max, degrading below sqrt(eps) sigma_max.
+// DMRG keeps sigma_j^2 >= cutoff * sum(P) (sigma_j >= 1e-6 sigma_max at
+// cutoff 1e-12), where the error is <= 1e-10 sigma_max.  itg_svd_trunc keeps
+// the FP64 Jacobi path for callers that need LAPACK-level accuracy on tiny
+// singular values.
 #include "itg_internal.cuh"
 
 #include <cmath>
@@ -87,6 +91,60 @@ k_jacobi32_step(float* __restrict__ W, int64_t m, int n, float* __restrict__ V, 
     vq[i] = s * x + c * y;
   }
   if (threadIdx.x == 0) *rotated = 1;
+}
+
+// All sweeps in one CTA (n <= 512): warps take column pairs of each
+// round-robin step; __syncthreads between steps.
+__global__ void __launch_bounds__(1024)
+k_jacobi32_onecta(float* __restrict__ W, int64_t m, int n, float* __restrict__ V, float tol, int max_sweeps,
+                  int* __restrict__ sweeps_out) {
+  __shared__ int rotated;
+  const int np = n + (n & 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (threadIdx.x == 0) rotated = 0;
+    __syncthreads();
+    for (int step = 0; step < np - 1; ++step) {
+      for (int pi = warp; pi < np / 2; pi += nw) {
+        int p = rr_player32(pi, step, np), q = rr_player32(np - 1 - pi, step, np);
+        if (p >= n || q >= n) continue;
+        if (p > q) { const int t = p; p = q; q = t; }
+        float* wp = W + (int64_t)p * m;
+        float* wq = W + (int64_t)q * m;
+        float a = 0.f, b = 0.f, g = 0.f;
+        for (int64_t i = lane; i < m; i += 32) {
+          const float x = wp[i], y = wq[i];
+          a = fmaf(x, x, a);
+          b = fmaf(y, y, b);
+          g = fmaf(x, y, g);
+        }
+        a = warp_sumf(a); b = warp_sumf(b); g = warp_sumf(g);
+        if (a == 0.f || b == 0.f || fabsf(g) <= tol * sqrtf(a) * sqrtf(b)) continue;
+        const float zeta = (b - a) / (2.f * g);
+        const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+        const float c = 1.f / sqrtf(1.f + t * t), s = c * t;
+        for (int64_t i = lane; i < m; i += 32) {
+          const float x = wp[i], y = wq[i];
+          wp[i] = c * x - s * y;
+          wq[i] = s * x + c * y;
+        }
+        float* vp = V + (int64_t)p * n;
+        float* vq = V + (int64_t)q * n;
+        for (int i = lane; i < n; i += 32) {
+          const float x = vp[i], y = vq[i];
+          vp[i] = c * x - s * y;
+          vq[i] = s * x + c * y;
+        }
+        if (lane == 0) rotated = 1;
+      }
+      __syncthreads();
+    }
+    const int r = rotated;
+    __syncthreads();
+    if (!r) break;
+  }
+  if (threadIdx.x == 0) *sweeps_out = sweep;
 }
 
 __global__ void k_to_float(const double* __restrict__ A, int64_t lda, int64_t m, int64_t n, bool transpose,
@@ -219,16 +277,26 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
   const int np = n + (n & 1);
   int* hp = (int*)h->pinned;
   int sweeps = 0;
-  for (; sweeps < 40; ++sweeps) {
-    ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
-    for (int step = 0; step < np - 1; ++step)
-      k_jacobi32_step<<<np / 2, 256, 0, h->stream>>>(W32, mm, n, V32, 1e-5f, step, flag);
+  const float tol32 = 1e-5f;
+  if (n <= 512) {
+    k_jacobi32_onecta<<<1, 1024, 0, h->stream>>>(W32, mm, n, V32, tol32, 30, flag);
     ITG_CHECK_LAUNCH(h);
     ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     ITG_CUDA(h, cudaStreamSynchronize(h->stream));
-    if (hp[0] == 0) break;
+    sweeps = hp[0];
+  } else {
+    for (; sweeps < 30; ++sweeps) {
+      ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+      for (int step = 0; step < np - 1; ++step)
+        k_jacobi32_step<<<np / 2, 256, 0, h->stream>>>(W32, mm, n, V32, tol32, step, flag);
+      ITG_CHECK_LAUNCH(h);
+      ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+      ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+      if (hp[0] == 0) break;
+    }
+    sweeps++;
   }
-  *sweeps_out = sweeps + 1;
+  *sweeps_out = sweeps;
   // 2. refinement of X on G = A^T A
   // G P Q E Xn (nn^2 each) | S (max(mm*nn, nn^2), also the copy of U) | max slot
   double* G = ws;
@@ -252,7 +320,11 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
     ITG_CUDA(h, cudaMemcpyAsync(h->pinned, mx, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     ITG_CUDA(h, cudaStreamSynchronize(h->stream));
     const double lmax = h->pinned[0] > 0.0 ? h->pinned[0] : 1.0;
-    k_refine_E<<<gb, 256, 0, h->stream>>>(P, S, lam, n, 1e-9 * lmax, E);
+    // pairs closer than the current eigenvector error are treated as one
+    // cluster (only their orthogonality is restored): 1e-6 relative after the
+    // FP32 start, then 1e-10
+    const double delta = (it == 0 ? 1e-6 : 1e-10) * lmax;
+    k_refine_E<<<gb, 256, 0, h->stream>>>(P, S, lam, n, delta, E);
     ITG_CHECK_LAUNCH(h);
     ITG_CUDA(h, cudaMemcpyAsync(Xn, X, sizeof(double) * nn * nn, cudaMemcpyDeviceToDevice, h->stream));
     ITG_TRY(gemm(h, false, nn, nn, nn, 1.0, X, E, 1.0, Xn, precision));  // X <- X + X E

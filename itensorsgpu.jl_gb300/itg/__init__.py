@@ -14,5 +14,6 @@ from .mps import (MPO, MPS, cuMPO, cuMPS, heisenberg_mpo, j1j2_mpo, mpo_dense_ma
                   productCuMPS, productMPS_host, randomCuMPS, siteinds, spin_ops, tfim_mpo, xxz_mpo)
 from .dmrg import (DMRGResult, Sweeps, cutoff_, dmrg, expect_energy, inner, maxdim_, mindim_,
                    noise_, sweepnext)
+from .batched import dmrg_batched
 
 __all__ = [n for n in dir() if not n.startswith("_")]

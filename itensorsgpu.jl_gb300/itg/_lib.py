@@ -102,6 +102,26 @@ SIGNATURES = {
                                  _P, _P, _I64P, _DP, _DP]),
     "itg_qr": (C.c_int, [_P, C.c_int64, C.c_int64, _P, C.c_int64, _P, _P]),
     "itg_matmul": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, _P, _P, _P, C.c_int]),
+    "itg_mlp_create": (C.c_int, [_P, C.c_int, C.c_uint64, C.POINTER(_P)]),
+    "itg_mlp_destroy": (C.c_int, [_P, _P]),
+    "itg_mlp_num_params": (C.c_int, [_P, _I64P]),
+    "itg_mlp_get_params": (C.c_int, [_P, _P, _P]),
+    "itg_mlp_set_params": (C.c_int, [_P, _P, _P]),
+    "itg_mlp_forward": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
+    "itg_mlp_train_step": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P, C.c_float, _P, C.POINTER(C.c_float)]),
+    "itg_heff2_features": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, _P, _P, C.c_double, _P, _P, _P,
+                                     _P]),
+    "itg_davidson_heff2_learned": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                             C.c_int64, _P, _P, _P, _P, _P, C.c_int, C.c_int, C.c_double,
+                                             C.c_int, _P, _P, _P, _DP, C.POINTER(C.c_int),
+                                             C.POINTER(C.c_int)]),
+    "itg_contract_grouped": (C.c_int, [_P, C.c_int, C.c_double, _P, C.c_int, _I64P, _I32P,
+                                       _P, C.c_int, _I64P, _I32P, C.c_double, _P, C.c_int, _I64P, _I32P]),
+    "itg_svd_trunc_batched": (C.c_int, [_P, C.c_int, _I64P, _I64P, _P, _I64P, C.c_int64, C.c_double,
+                                        C.c_int, C.c_int, C.c_int, _P, _P, _P, _I64P, _DP]),
+    "itg_davidson_heff2_batched": (C.c_int, [_P, C.c_int, _I64P, _I64P, C.c_int64, C.c_int64, C.c_int64,
+                                             C.c_int64, _P, _P, _P, _P, _P, C.c_int, C.c_int, C.c_double,
+                                             _DP, C.POINTER(C.c_int)]),
     "itg_heff2_apply": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                   C.c_int64, _P, _P, _P, _P, _P, _P, C.c_int]),
     "itg_heff2_apply_noalloc": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64,

@@ -190,7 +190,7 @@ def _orthogonalize_left_end(h, ch: _Chain):
 
 def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int = 2,
          eigsolve_tol: float = 1e-14, precision: str | int = "fp64", legacy_gpu_truncate: bool = False,
-         svd_method: int = 0,
+         svd_method: int = 0, preconditioner=None, bond_hook=None,
          outputlevel: int = 0, return_result: bool = False):
     """Ground state by two-site DMRG.  Returns (energy, psi) like ITensors' dmrg.
 
@@ -200,6 +200,11 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
     cores (FP64 operands split into exact bf16 digit products).  svd_method:
     0 auto (Jacobi up to 192 columns, mixed FP32-Jacobi + refinement above),
     1 FP64 Jacobi, 2 mixed.
+
+    preconditioner: None (the diagonal one) or an itg.learned.LearnedPreconditioner
+    (itg_davidson_heff2_learned; falls back to the diagonal one when it stalls).
+    bond_hook(ctx): called before every eigensolve with a dict of the bond's
+    device tensors and dimensions (used to collect training data).
     """
     if isinstance(precision, str):
         precision = {"fp64": PREC_FP64, "split": PREC_SPLIT}[precision.lower()]
@@ -225,6 +230,8 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
                              precision)
     energy = 0.0
     records = []
+    schmidt = [None] * (N + 1)  # latest singular values on link j (between sites j-1 and j)
+    fallbacks_total = 0
     for sw in range(sweeps.nsweep):
         t0 = time.perf_counter()
         maxdim, mindim, cutoff = sweeps.maxdim(sw), sweeps.mindim(sw), sweeps.cutoff(sw)
@@ -241,12 +248,27 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
             Rt, Rd = Renv[b + 2]
             W1, W1d = ch.W[b], ch.Wd[b]
             W2, W2d = ch.W[b + 1], ch.Wd[b + 1]
+            lamL = schmidt[b] if (schmidt[b] is not None and len(schmidt[b]) == a) else None
+            lamR = schmidt[b + 2] if (schmidt[b + 2] is not None and len(schmidt[b + 2]) == c) else None
+            if bond_hook is not None:
+                bond_hook(dict(b=b, half=ha, sweep=sw, chiL=a, chiR=c, d=d1, wL=W1d[0], wM=W1d[3], wR=W2d[3],
+                               L=Lt, W1=W1, W2=W2, R=Rt, phi=phi, lamL=lamL, lamR=lamR))
             e = C.c_double()
             nmv = C.c_int()
-            h.call("itg_davidson_heff2", C.c_int64(a), C.c_int64(c), C.c_int64(d1), C.c_int64(W1d[0]),
-                   C.c_int64(W1d[3]), C.c_int64(W2d[3]), _ptr(Lt), _ptr(W1), _ptr(W2), _ptr(Rt),
-                   _ptr(phi), int(krylovdim), int(maxiter), C.c_double(eigsolve_tol), int(precision),
-                   C.byref(e), C.byref(nmv))
+            if preconditioner is None:
+                h.call("itg_davidson_heff2", C.c_int64(a), C.c_int64(c), C.c_int64(d1), C.c_int64(W1d[0]),
+                       C.c_int64(W1d[3]), C.c_int64(W2d[3]), _ptr(Lt), _ptr(W1), _ptr(W2), _ptr(Rt),
+                       _ptr(phi), int(krylovdim), int(maxiter), C.c_double(eigsolve_tol), int(precision),
+                       C.byref(e), C.byref(nmv))
+            else:
+                fb = C.c_int()
+                h.call("itg_davidson_heff2_learned", C.c_int64(a), C.c_int64(c), C.c_int64(d1),
+                       C.c_int64(W1d[0]), C.c_int64(W1d[3]), C.c_int64(W2d[3]), _ptr(Lt), _ptr(W1), _ptr(W2),
+                       _ptr(Rt), _ptr(phi), int(krylovdim), int(maxiter), C.c_double(eigsolve_tol),
+                       int(precision), preconditioner.ptr,
+                       _ptr(lamL) if lamL is not None else None, _ptr(lamR) if lamR is not None else None,
+                       C.byref(e), C.byref(nmv), C.byref(fb))
+                fallbacks_total += fb.value
             energy = e.value
             nmv_tot += nmv.value
             # SVD of phi as (a d1) x (d2 c)
@@ -270,6 +292,7 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
             Uk = U[: m * kk]
             Vk = V[: n * kk]
             Sk = S[:kk]
+            schmidt[b + 1] = Sk.clone()
             if ha == 1:
                 ch.A[b] = Uk.clone()
                 ch.Ad[b] = (a, d1, kk)
@@ -298,7 +321,9 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
     ts = [ITensor(Dense(ch.A[j]), (links[j], psi0.sites[j], links[j + 1])) for j in range(N)]
     psi = MPS(ts, psi0.sites, 0, 1)
     if return_result:
-        return DMRGResult(energy, psi, records)
+        res = DMRGResult(energy, psi, records)
+        res.fallbacks = fallbacks_total
+        return res
     return energy, psi
 
 

@@ -536,3 +536,65 @@ def heisenberg_ed_sz0(N: int, J=1.0, Delta=1.0, J2=0.0) -> float:
 def tfim_closed_form(N: int) -> float:
     """test/dmrg.jl:79: E = 0.25 - 0.25 / sin(pi / (2 (2N + 1))) for H = -sum SzSz - 0.5 sum Sx."""
     return 0.25 - 0.25 / math.sin(math.pi / (2 * (2 * N + 1)))
+
+
+# ------------------------------------------------- learned preconditioner MLP
+MLP_W = 128
+
+
+def bf16_round(x) -> np.ndarray:
+    """Round float32 values to bfloat16 (nearest even), returned as float32."""
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def mlp_unpack(params, F):
+    p = np.asarray(params, dtype=np.float32)
+    o = 0
+    W1 = p[o: o + MLP_W * F].reshape(MLP_W, F); o += MLP_W * F
+    b1 = p[o: o + MLP_W]; o += MLP_W
+    W2 = p[o: o + MLP_W * MLP_W].reshape(MLP_W, MLP_W); o += MLP_W * MLP_W
+    b2 = p[o: o + MLP_W]; o += MLP_W
+    w3 = p[o: o + MLP_W]; o += MLP_W
+    b3 = p[o]
+    return W1, b1, W2, b2, w3, b3
+
+
+def mlp_forward(params, F, X):
+    """The library's per-element MLP: BF16 weights, FP32 arithmetic, ReLU."""
+    W1, b1, W2, b2, w3, b3 = mlp_unpack(params, F)
+    W1, W2, w3 = bf16_round(W1), bf16_round(W2), bf16_round(w3)
+    X = np.asarray(X, dtype=np.float32).reshape(-1, F)
+    z1 = X @ W1.T + b1
+    a1 = np.maximum(z1, 0)
+    z2 = a1 @ W2.T + b2
+    a2 = np.maximum(z2, 0)
+    return (a2 @ w3 + b3).astype(np.float32)
+
+
+def mlp_loss_grad(params, F, X, mult, target):
+    """(loss, gradient w.r.t. the master parameters) of mean (g*mult - target)^2."""
+    W1, b1, W2, b2, w3, b3 = mlp_unpack(params, F)
+    W1r, W2r, w3r = bf16_round(W1), bf16_round(W2), bf16_round(w3)
+    X = np.asarray(X, dtype=np.float64).reshape(-1, F)
+    n = X.shape[0]
+    z1 = X @ W1r.T.astype(np.float64) + b1
+    a1 = np.maximum(z1, 0)
+    z2 = a1 @ W2r.T.astype(np.float64) + b2
+    a2 = np.maximum(z2, 0)
+    g = a2 @ w3r.astype(np.float64) + b3
+    diff = g * mult - target
+    loss = float(np.mean(diff ** 2))
+    dg = 2.0 * diff * mult / n
+    dw3 = a2.T @ dg
+    db3 = dg.sum()
+    dz2 = np.outer(dg, w3r) * (z2 > 0)
+    dW2 = dz2.T @ a1
+    db2 = dz2.sum(0)
+    dz1 = (dz2 @ W2r.astype(np.float64)) * (z1 > 0)
+    dW1 = dz1.T @ X
+    db1 = dz1.sum(0)
+    grad = np.concatenate([dW1.ravel(), db1, dW2.ravel(), db2, dw3, [db3]])
+    return loss, grad
