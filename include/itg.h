@@ -91,6 +91,39 @@ enum { ITG_KERNEL_GEMM_F64 = 0, ITG_KERNEL_GEMM_SPLIT = 1, ITG_KERNEL_SPLIT_PREP
 ITG_API int itg_profile(itg_handle* h, int enable);
 ITG_API int itg_profile_read(itg_handle* h, int kernel, double* total_ms, int64_t* launches);
 
+/* Autotuning of kernel variants per contraction shape.  Replaces the
+ * reference's per-(mode, dim) algorithm cache (src/cudense.jl:284-326, cache
+ * declared at src/ITensorsGPU.jl:55), which sweeps cuTENSOR algorithms on the
+ * first use of a shape.  Here the first FP64 contraction of a shape whose
+ * 128x128 tiling leaves the GPU under-filled times the tile variants
+ * (128x128, 128x64, 64x64) on the call's own operands into a throw-away
+ * output, and split contractions time the 256- and 128-wide tcgen05 tiles;
+ * grouped launches choose their tile per shape class.  All variants compute
+ * bit-identical results (the same k order per output element), so tuning only
+ * changes speed.  The choices live in one per-process cache guarded by a
+ * mutex; with the environment variable ITG_TUNE_FILE set they are also read
+ * from and appended to that file.  Launches inside a CUDA-graph capture never
+ * tune (they use the cached choice or the heuristic).
+ * enable: 1 (default unless ITG_AUTOTUNE=0 in the environment) or 0
+ * (heuristic choice only). */
+enum { ITG_TILE_128x128 = 0, ITG_TILE_128x64 = 1, ITG_TILE_64x64 = 2 };
+ITG_API int itg_set_autotune(itg_handle* h, int enable);
+/* entries: size of the process-wide cache; tunings: tuning runs by this handle. */
+ITG_API int itg_autotune_info(itg_handle* h, int64_t* entries, int64_t* tunings);
+/* Empty the process-wide cache and every cached choice of this handle's plans. */
+ITG_API int itg_autotune_clear(itg_handle* h);
+/* The variant a contraction of this shape would use now (without tuning):
+ * *tile = ITG_TILE_* for FP64, *split_bn = 128 or 256 for split. */
+ITG_API int itg_autotune_query(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA,
+                               int rankB, const int64_t* dimsB, const int32_t* modesB, int rankC,
+                               const int64_t* dimsC, const int32_t* modesC, int* tile, int* split_bn);
+/* Pin the variants of one shape (tile: ITG_TILE_*, split_bn: 128 or 256; a
+ * negative / zero value leaves that choice alone); stored in the process-wide
+ * cache like a tuned choice. */
+ITG_API int itg_autotune_force(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA,
+                               int rankB, const int64_t* dimsB, const int32_t* modesB, int rankC,
+                               const int64_t* dimsC, const int32_t* modesC, int tile, int split_bn);
+
 /* ---------------------------------------------------------------- memory */
 /* Replace CuVector allocation and the H2D/D2H copies of
  * src/tensor/cudense.jl:4-13 (Dense{T,CuArray}(::Dense{T,Array}), cpu(x)). */

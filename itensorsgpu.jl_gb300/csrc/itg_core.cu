@@ -1,6 +1,8 @@
 // Handle, memory, level-1 vector kernels and the Philox normal generator.
 #include "itg_internal.cuh"
 
+#include <cstdlib>
+
 #include <cmath>
 
 #define ITG_VERSION 10000  // 1.0.0
@@ -54,6 +56,7 @@ extern "C" int itg_create(int device, itg_handle** out) {
     return ITG_ERR_ALLOC;
   }
   cudaMemset(h->dev_status, 0, 64);
+  if (const char* at = std::getenv("ITG_AUTOTUNE")) h->autotune = std::atoi(at) != 0;
   *out = h;
   return ITG_OK;
 }
@@ -131,6 +134,7 @@ extern "C" int itg_destroy(itg_handle* h) {
   if (h->split_ws) cudaFree(h->split_ws);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   if (h->group_desc) cudaFree(h->group_desc);
+  if (h->tune_buf) cudaFree(h->tune_buf);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->dev_status) cudaFree(h->dev_status);
   delete h;

@@ -398,10 +398,12 @@ __global__ void k_gershgorin(const double* __restrict__ A, int64_t lda, int64_t 
 namespace {
 
 constexpr int JACOBI_MAX_SWEEPS = 60;
+constexpr int JACOBI_AUX_INTS = 8 + JACOBI_MAX_SWEEPS;
 constexpr int64_t ONECTA_MAX_N = 192;
 
 // Runs Jacobi on W (m x n, m >= n) with V = I.  Returns ITG_ERR_NOTCONVERGED
-// (results still usable) when the sweep limit is hit.
+// (results still usable) when the sweep limit is hit.  flag_dev: at least
+// JACOBI_AUX_INTS device ints.
 int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* flag_dev,
                int* sweeps_done) {
   k_identity<<<itg_blocks_for(n * n, 256, h->num_sms * 8), 256, 0, h->stream>>>((int)n, V);
@@ -417,6 +419,12 @@ int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* f
     *sweeps_done = hp[0];
     return hp[0] >= JACOBI_MAX_SWEEPS ? ITG_ERR_NOTCONVERGED : ITG_OK;
   }
+  {
+    const int st = itg::jacobi_persistent<double>(h, W, m, (int)n, V, tol, JACOBI_MAX_SWEEPS, flag_dev,
+                                                  sweeps_done);
+    if (st != ITG_ERR_UNSUPPORTED) return st;
+  }
+  // per-step launches (devices without cooperative launch)
   const int np = (int)(n + (n & 1));
   int* hp = (int*)h->pinned;
   for (int sweep = 0; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
@@ -492,7 +500,7 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
   const bool mixed = method == ITG_SVD_MIXED || (method == ITG_SVD_AUTO && nn > ONECTA_MAX_N);
   size_t oW = take(sizeof(double) * mm * nn), oV = take(sizeof(double) * nn * nn),
          oSig = take(sizeof(double) * nn), oP = take(sizeof(double) * nn),
-         oOrd = take(sizeof(int) * nn), oOut = take(4 * sizeof(double)), oFlag = take(sizeof(int));
+         oOrd = take(sizeof(int) * nn), oOut = take(4 * sizeof(double)), oFlag = take(sizeof(int) * JACOBI_AUX_INTS);
   size_t oLam = 0, oUw = 0, oWs = 0, oWs32 = 0;
   if (mixed) {
     oLam = take(sizeof(double) * nn);
@@ -571,7 +579,7 @@ extern "C" int itg_eigh_trunc(itg_handle* h, int64_t n, const double* A, int64_t
   auto take = [&](size_t bytes) { size_t o = off; off += itg_align256(bytes); return o; };
   size_t oW = take(sizeof(double) * n * n), oV = take(sizeof(double) * n * n),
          oSig = take(sizeof(double) * n), oP = take(sizeof(double) * n),
-         oOrd = take(sizeof(int) * n), oOut = take(4 * sizeof(double)), oFlag = take(sizeof(int)),
+         oOrd = take(sizeof(int) * n), oOut = take(4 * sizeof(double)), oFlag = take(sizeof(int) * JACOBI_AUX_INTS),
          oC = take(sizeof(double));
   ITG_TRY(itg_scratch_reserve(h, off));
   char* base = (char*)h->scratch;

@@ -23,6 +23,11 @@ struct ContractPlan {
   int64_t M = 0, N = 0, K = 0;
   int64_t* tables = nullptr;  // offAm[M] offCm[M] offBn[N] offCn[N] offAk[K] offBk[K]
   bool a_kmaj = false, b_kmaj = false;
+  // Autotuning: the plan's canonical shape key (empty for plans that must not
+  // be tuned) and the chosen variants (-1 / 0: not chosen yet).
+  std::string key;
+  mutable int tile = -1;      // FP64 tile variant (ITG_TILE_*)
+  mutable int split_bn = 0;   // split GEMM tile width (128 or 256)
   const int64_t* offAm() const { return tables; }
   const int64_t* offCm() const { return tables + M; }
   const int64_t* offBn() const { return tables + 2 * M; }
@@ -66,6 +71,11 @@ struct itg_handle {
   bool prof_on = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_events;
   std::vector<cudaEvent_t> prof_pool;
+  // Autotuning (itg_set_autotune): on by default unless ITG_AUTOTUNE=0.
+  bool autotune = true;
+  void* tune_buf = nullptr;   // throw-away outputs of tuning launches
+  size_t tune_buf_bytes = 0;
+  int64_t tune_runs = 0;
 };
 
 // Record a timing event pair around a launch when profiling is on.
@@ -76,6 +86,15 @@ struct ProfScope {
   ProfScope(itg_handle* hh, int k);
   ~ProfScope();
 };
+
+namespace itg {
+// Persistent one-sided Jacobi (itg_jacobi.cu): all sweeps in one cooperative
+// launch; aux holds jacobi_aux_ints(max_sweeps) device ints.
+int jacobi_aux_ints(int max_sweeps);
+template <class T>
+int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, int max_sweeps, int* aux,
+                      int* sweeps);
+}  // namespace itg
 
 // Error helpers ---------------------------------------------------------------
 int itg_fail(itg_handle* h, int code, const char* fmt, ...);

@@ -748,9 +748,11 @@ int ws_reserve(itg_handle* h, size_t bytes) {
 
 }  // namespace split
 
+// bn: tcgen05 tile width, 128 or 256 (0: 128 when N <= 128, else 256).
 int itg_split_gemm(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
-                   double alpha, double beta) {
-  if (p.N <= 128) return split::run<128>(h, p, A, B, C, alpha, beta);
+                   double alpha, double beta, int bn) {
+  if (bn == 0) bn = p.N <= 128 ? 128 : 256;
+  if (bn == 128) return split::run<128>(h, p, A, B, C, alpha, beta);
   return split::run<256>(h, p, A, B, C, alpha, beta);
 }
 

@@ -18,6 +18,7 @@
 //     decomposition", Japan J. Indust. Appl. Math. 35 (2018).  Convergence is
 //     quadratic; clustered (degenerate) pairs only get their orthogonality
 //     restored, which leaves any basis of a degenerate subspace.
+//     Two Newton-Schulz steps then restore X's orthonormality to rounding.
 //  3. sigma_i = sqrt(max(l_i, 0)), U = A X diag(1/sigma), then one Newton-
 //     Schulz step U <- U + U (I - U^T U)/2 to restore orthonormality.
 // Accuracy: P = sigma^2 (what truncation uses) to ~eps * P_max absolute, so
@@ -285,6 +286,12 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
     ITG_CUDA(h, cudaStreamSynchronize(h->stream));
     sweeps = hp[0];
   } else {
+    const int st = itg::jacobi_persistent<float>(h, W32, mm, n, V32, tol32, 30, flag, &sweeps);
+    if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED && st != ITG_ERR_UNSUPPORTED) return st;
+    if (st == ITG_ERR_UNSUPPORTED) sweeps = 0;
+  }
+  if (n > 512 && sweeps == 0) {
+    // per-step launches (devices without cooperative launch)
     for (; sweeps < 30; ++sweeps) {
       ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
       for (int step = 0; step < np - 1; ++step)
@@ -328,6 +335,18 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
     ITG_CHECK_LAUNCH(h);
     ITG_CUDA(h, cudaMemcpyAsync(Xn, X, sizeof(double) * nn * nn, cudaMemcpyDeviceToDevice, h->stream));
     ITG_TRY(gemm(h, false, nn, nn, nn, 1.0, X, E, 1.0, Xn, precision));  // X <- X + X E
+    ITG_CUDA(h, cudaMemcpyAsync(X, Xn, sizeof(double) * nn * nn, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  // Two Newton-Schulz steps X <- X + X (I - X^T X)/2: pairs whose gap is
+  // below the products' rounding (eigenvalues under ~1e-8 lambda_max) leave
+  // first-order errors in E's antisymmetric part, hence second-order loss of
+  // orthogonality (up to ~1e-5); each step squares it.
+  for (int it = 0; it < 2; ++it) {
+    ITG_TRY(gemm(h, true, nn, nn, nn, 1.0, X, X, 0.0, P, precision));
+    k_half_identity_minus<<<gb, 256, 0, h->stream>>>(P, n, Q);
+    ITG_CHECK_LAUNCH(h);
+    ITG_CUDA(h, cudaMemcpyAsync(Xn, X, sizeof(double) * nn * nn, cudaMemcpyDeviceToDevice, h->stream));
+    ITG_TRY(gemm(h, false, nn, nn, nn, 1.0, X, Q, 1.0, Xn, precision));
     ITG_CUDA(h, cudaMemcpyAsync(X, Xn, sizeof(double) * nn * nn, cudaMemcpyDeviceToDevice, h->stream));
   }
   // final eigenvalues from the refined X

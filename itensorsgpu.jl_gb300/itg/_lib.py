@@ -102,6 +102,13 @@ SIGNATURES = {
                                  _P, _P, _I64P, _DP, _DP]),
     "itg_qr": (C.c_int, [_P, C.c_int64, C.c_int64, _P, C.c_int64, _P, _P]),
     "itg_matmul": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, _P, _P, _P, C.c_int]),
+    "itg_set_autotune": (C.c_int, [_P, C.c_int]),
+    "itg_autotune_info": (C.c_int, [_P, _I64P, _I64P]),
+    "itg_autotune_clear": (C.c_int, [_P]),
+    "itg_autotune_query": (C.c_int, [_P, C.c_int, _I64P, _I32P, C.c_int, _I64P, _I32P, C.c_int, _I64P, _I32P,
+                                     C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "itg_autotune_force": (C.c_int, [_P, C.c_int, _I64P, _I32P, C.c_int, _I64P, _I32P, C.c_int, _I64P, _I32P,
+                                     C.c_int, C.c_int]),
     "itg_mlp_create": (C.c_int, [_P, C.c_int, C.c_uint64, C.POINTER(_P)]),
     "itg_mlp_destroy": (C.c_int, [_P, _P]),
     "itg_mlp_num_params": (C.c_int, [_P, _I64P]),

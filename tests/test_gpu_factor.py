@@ -150,7 +150,8 @@ def test_svd_mixed_haar_exp_spectrum(gpu, n, prec):
     # truncation is exact; singular values accurate above ~1e-4 sigma_max
     assert kk == len(So)
     Sh = S.cpu().numpy()[:kk]
-    assert np.abs(Sh ** 2 - So ** 2).max() < 1e-14 * So[0] ** 2
+    # P = S^2 to a few hundred ulps of P_max (the split products add ~1e-14)
+    assert np.abs(Sh ** 2 - So ** 2).max() < 3e-14 * So[0] ** 2
     big = So > 1e-4 * So[0]
     assert np.abs(Sh[big] - So[big]).max() < 1e-12 * So[0]
     Uh = O.unflat(U.cpu().numpy()[: n * kk], (n, kk))
