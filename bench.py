@@ -322,6 +322,10 @@ def run_gpu(args):
     e2e_value = flop_step / e2e_s / 1e12
     finite = bool(torch.isfinite(chosen["out"]).all().item())
 
+    # ---- one DMRG sweep at bond dimension chi, chosen vs plain (rank 0, N=1)
+    sweep = None
+    if args.sweep_n > 0 and world == 1:
+        sweep = measure_sweeps(args.sweep_n, chi, 1, 0.0)
     if rank != 0:
         return 0
     cpu = None
@@ -352,6 +356,8 @@ def run_gpu(args):
         line["chosen_vs_plain"] = chosen["value"] / pl["value"]
     if accuracy is not None:
         line["split_vs_fp64_rel_frobenius"] = accuracy
+    if sweep is not None:
+        line["sweep"] = sweep
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -359,40 +365,167 @@ def run_gpu(args):
 
 
 # ------------------------------------------------------ DMRG sweep workload
-def run_dmrg(args):
-    """DMRG sweep time at bond dimension chi, chosen (split) vs plain (FP64) form.
+def measure_sweeps(N, chi, nsweep, cutoff, seed=1236):
+    """One DMRG run per form from the same initial state; per-sweep times and phases.
 
-    S=1/2 Heisenberg chain of N sites, random initial MPS with link dimensions
-    min(chi, 2^b, 2^(N-b)) from the Philox stream (seed 1236), sweeps at maxdim chi,
-    cutoff 1e-12, Davidson krylovdim 3 / maxiter 2.  Every bond in the middle of the
-    chain runs at the full bond dimension, so the per-sweep time is the cost of
-    chi-sized two-site updates (SVD of 2chi x 2chi, H_eff matvecs, environments).
+    S=1/2 Heisenberg chain of N sites (MPO bond dimension 5), random initial MPS
+    with link dimensions min(chi, 2^b, 2^(N-b)) from the Philox stream, sweeps at
+    maxdim chi and the given cutoff (0 keeps chi on every bulk bond), Davidson
+    krylovdim 3 / maxiter 2.  Forms:
+      chosen: split-precision contractions, mixed SVD (FP32 Jacobi + FP64-accurate
+              refinement through split products);
+      plain:  FP64 contractions, FP64 one-sided Jacobi SVD.
     """
     import torch
     import itg
-    N, chi = args.dmrg_n, args.chi
     sites = itg.siteinds("S=1/2", N)
     H = itg.cuMPO(itg.heisenberg_mpo(sites))
-    psi0 = itg.randomCuMPS(sites, chi, seed=1236)
+    psi0 = itg.randomCuMPS(sites, chi, seed=seed)
     out = {}
-    for form in ("split", "fp64"):
-        sw = itg.Sweeps(args.dmrg_sweeps, maxdim=[chi], cutoff=[1e-12])
+    for form, prec, svd in (("chosen", "split", 2), ("plain", "fp64", 1)):
+        sw = itg.Sweeps(nsweep, maxdim=[chi], cutoff=[cutoff])
         torch.cuda.synchronize()
         with ClockSampler(0) as clk:
-            res = itg.dmrg(H, psi0, sw, precision=form, return_result=True)
+            res = itg.dmrg(H, psi0, sw, precision=prec, svd_method=svd, phase_timing=True, return_result=True)
         out[form] = {"sweep_seconds": [r.seconds for r in res.sweeps],
                      "energies": [r.energy for r in res.sweeps],
+                     "phases": [r.phases for r in res.sweeps],
                      "maxlinkdim": res.sweeps[-1].maxlinkdim, "matvecs": [r.matvecs for r in res.sweeps],
+                     "precision": prec, "svd": "mixed" if svd == 2 else "fp64 jacobi",
                      "clocks": clk.summary()}
-    sp, pl = out["split"], out["fp64"]
+    ch, pl = out["chosen"], out["plain"]
+    return {"N": N, "chi": chi, "sweeps": nsweep, "cutoff": cutoff,
+            "chosen_seconds": min(ch["sweep_seconds"]), "plain_seconds": min(pl["sweep_seconds"]),
+            "chosen_vs_plain_speedup": min(pl["sweep_seconds"]) / min(ch["sweep_seconds"]),
+            "energy_diff_last_sweep": abs(ch["energies"][-1] - pl["energies"][-1]),
+            "detail": out}
+
+
+def run_dmrg(args):
+    """DMRG sweep time at bond dimension chi, chosen vs plain form (see measure_sweeps)."""
+    N, chi = args.dmrg_n, args.chi
+    r = measure_sweeps(N, chi, args.dmrg_sweeps, args.dmrg_cutoff)
     line = {"metric": f"DMRG sweep time at chi={chi} (Heisenberg N={N}), chosen vs plain",
-            "value": min(sp["sweep_seconds"]), "unit": "s", "higher_is_better": False,
-            "plain_value": min(pl["sweep_seconds"]),
-            "chosen_vs_plain_speedup": min(pl["sweep_seconds"]) / min(sp["sweep_seconds"]),
-            "energy_diff_last_sweep": abs(sp["energies"][-1] - pl["energies"][-1]),
+            "value": r["chosen_seconds"], "unit": "s", "higher_is_better": False,
+            "plain_value": r["plain_seconds"], "chosen_vs_plain_speedup": r["chosen_vs_plain_speedup"],
+            "energy_diff_last_sweep": r["energy_diff_last_sweep"],
             "config": {"workload": f"dmrg heisenberg N={N} chi={chi}", "sweeps": args.dmrg_sweeps,
-                       "cutoff": 1e-12, "krylovdim": 3, "maxiter": 2},
-            "dtype": "f64", "data": "synthetic (seeded Philox initial MPS)", "detail": out}
+                       "cutoff": args.dmrg_cutoff, "krylovdim": 3, "maxiter": 2},
+            "dtype": "f64", "data": "synthetic (seeded Philox initial MPS)", "detail": r["detail"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------ many instances (batched)
+def run_batched(args):
+    """Many independent disordered XXZ chains advanced in lockstep vs looping the plain path.
+
+    `count` chains of N sites, J_i, Delta_i ~ U[0.5, 1.5] per bond (seeded), maxdim per
+    instance drawn from {32, 64, 96, 128}, cutoff 1e-10, random initial MPS of link
+    dimension 8.  The lockstep run (itg.dmrg_batched: grouped contractions, batched
+    Davidson, batched Jacobi SVD) is timed whole; the looped plain path
+    (itg.dmrg per instance, FP64 Jacobi SVD) is timed on the first `loop_sample`
+    instances and scaled by count / loop_sample.
+    """
+    import numpy as np
+    import torch
+    import itg
+    cnt, N, nsw = args.batch_count, args.batch_n, args.batch_sweeps
+    rng = np.random.default_rng(1234 + 4)
+    Hs, psis, mds = [], [], []
+    for i in range(cnt):
+        sites = itg.siteinds("S=1/2", N)
+        J = rng.uniform(0.5, 1.5, N - 1)
+        D = rng.uniform(0.5, 1.5, N - 1)
+        Hs.append(itg.cuMPO(itg.xxz_mpo(sites, J=J, Delta=D)))
+        psis.append(itg.randomCuMPS(sites, 8, seed=5000 + i))
+        mds.append(int(rng.choice([32, 64, 96, 128])))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with ClockSampler(0) as clk:
+        E, _, secs = itg.dmrg_batched(Hs, psis, nsw, mds, 1e-10)
+    torch.cuda.synchronize()
+    t_batched = time.perf_counter() - t0
+    ns = min(args.loop_sample, cnt)
+    t0 = time.perf_counter()
+    e_loop = []
+    for i in range(ns):
+        sw = itg.Sweeps(nsw, maxdim=[mds[i]], cutoff=[1e-10])
+        e, _ = itg.dmrg(Hs[i], psis[i], sw, svd_method=1)
+        e_loop.append(e)
+    torch.cuda.synchronize()
+    t_loop_sample = time.perf_counter() - t0
+    t_loop = t_loop_sample * cnt / ns
+    line = {"metric": f"DMRG of {cnt} disordered XXZ chains (N={N}, {nsw} sweeps): lockstep vs looped",
+            "value": t_batched, "unit": "s", "higher_is_better": False,
+            "looped_value": t_loop, "looped_note": f"{ns} instances timed, scaled by {cnt}/{ns}",
+            "batched_vs_looped_speedup": t_loop / t_batched,
+            "max_energy_diff_vs_looped": max(abs(E[i] - e_loop[i]) for i in range(ns)),
+            "sweep_seconds": secs, "clocks": clk.summary(),
+            "config": {"workload": f"batched xxz count={cnt} N={N}", "sweeps": nsw, "cutoff": 1e-10,
+                       "maxdim_choices": [32, 64, 96, 128], "init_linkdim": 8},
+            "dtype": "f64", "data": "synthetic (seeded couplings and Philox initial MPS)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------ learned preconditioner
+def run_learned(args):
+    """Learned Davidson preconditioner on the J1-J2 chain (train J2 = 0.2, 0.3, 0.4; test 0.5).
+
+    Training samples: plain DMRG runs at the training couplings (maxdim
+    `learn_train_maxdim`, 2 sweeps) with itg.learned.SampleCollector; the network is
+    trained on the GPU with the library's own kernels.  Evaluation at J2 = 0.5:
+    DMRG with the diagonal and with the learned preconditioner from the same
+    initial state (maxdim `learn_maxdim`, cutoff 1e-10, Davidson krylovdim 3,
+    maxiter 4, residual tolerance 1e-9): matvecs per bond, sweep time, energies.
+    """
+    import torch
+    import itg
+    from itg.learned import LearnedPreconditioner, SampleCollector
+    N = args.learn_n
+    sites = itg.siteinds("S=1/2", N)
+    col = SampleCollector(max_elements=args.learn_samples)
+    t0 = time.perf_counter()
+    for j2 in (0.2, 0.3, 0.4):
+        H = itg.cuMPO(itg.j1j2_mpo(sites, J1=1.0, J2=j2))
+        sw = itg.Sweeps(2, maxdim=[args.learn_train_maxdim], cutoff=[1e-10])
+        itg.dmrg(H, itg.randomCuMPS(sites, 8, seed=int(j2 * 100)), sw, bond_hook=col)
+    X, M, Y = col.data()
+    t_collect = time.perf_counter() - t0
+    net = LearnedPreconditioner(seed=11)
+    l0 = net.step(X, M, Y, 0.0)
+    t0 = time.perf_counter()
+    net.train((X, M, Y), steps=args.learn_steps, lr=1e-3, batch=65536)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    l1 = net.step(X, M, Y, 0.0)
+    H = itg.cuMPO(itg.j1j2_mpo(sites, J1=1.0, J2=0.5))
+    psi0 = itg.randomCuMPS(sites, 8, seed=505)
+    res = {}
+    for name, pc in (("diag", None), ("learned", net)):
+        sw = itg.Sweeps(args.learn_sweeps, maxdim=[args.learn_maxdim], cutoff=[1e-10])
+        torch.cuda.synchronize()
+        r = itg.dmrg(H, psi0, sw, krylovdim=3, maxiter=4, eigsolve_tol=1e-9, preconditioner=pc,
+                     return_result=True)
+        nb = 2 * (N - 1)
+        res[name] = {"energies": [x.energy for x in r.sweeps], "sweep_seconds": [x.seconds for x in r.sweeps],
+                     "matvecs_per_bond": [x.matvecs / nb for x in r.sweeps],
+                     "maxlinkdim": r.sweeps[-1].maxlinkdim, "fallbacks": getattr(r, "fallbacks", 0)}
+    d, l = res["diag"], res["learned"]
+    line = {"metric": f"learned vs diagonal Davidson preconditioner, J1-J2 N={N} J2=0.5 (held out)",
+            "value": sum(l["matvecs_per_bond"]) / len(l["matvecs_per_bond"]), "unit": "matvecs/bond",
+            "higher_is_better": False,
+            "diag_value": sum(d["matvecs_per_bond"]) / len(d["matvecs_per_bond"]),
+            "energy_diff_final": abs(l["energies"][-1] - d["energies"][-1]),
+            "sweep_seconds_learned": l["sweep_seconds"], "sweep_seconds_diag": d["sweep_seconds"],
+            "train": {"samples": int(M.numel()), "loss_before": l0, "loss_after": l1, "steps": args.learn_steps,
+                      "collect_s": t_collect, "train_s": t_train},
+            "detail": res,
+            "config": {"workload": f"j1j2 N={N} maxdim={args.learn_maxdim}", "train_J2": [0.2, 0.3, 0.4],
+                       "test_J2": 0.5, "cutoff": 1e-10, "krylovdim": 3, "maxiter": 4, "tol": 1e-9},
+            "dtype": "f64 (network bf16/fp32)", "data": "synthetic (seeded Philox initial MPS)"}
+    net.close()
     print(json.dumps(line), flush=True)
     return 0
 
@@ -409,12 +542,29 @@ def main():
     ap.add_argument("--chi", type=int, default=CHI)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="heff", choices=["heff", "dmrg"])
+    ap.add_argument("--workload", default="heff", choices=["heff", "dmrg", "batched", "learned"])
     ap.add_argument("--dmrg-n", type=int, default=24)
     ap.add_argument("--dmrg-sweeps", type=int, default=2)
+    ap.add_argument("--dmrg-cutoff", type=float, default=0.0)
+    ap.add_argument("--sweep-n", type=int, default=24,
+                    help="chain length of the sweep measurement in the default run (0: skip)")
+    ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--batch-n", type=int, default=32)
+    ap.add_argument("--batch-sweeps", type=int, default=8)
+    ap.add_argument("--loop-sample", type=int, default=16)
+    ap.add_argument("--learn-n", type=int, default=64)
+    ap.add_argument("--learn-maxdim", type=int, default=512)
+    ap.add_argument("--learn-train-maxdim", type=int, default=64)
+    ap.add_argument("--learn-samples", type=int, default=4_000_000)
+    ap.add_argument("--learn-steps", type=int, default=600)
+    ap.add_argument("--learn-sweeps", type=int, default=4)
     args = ap.parse_args()
     if args.workload == "dmrg":
         return run_dmrg(args)
+    if args.workload == "batched":
+        return run_batched(args)
+    if args.workload == "learned":
+        return run_learned(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -260,6 +260,35 @@ ITG_API int itg_svd_trunc_ex(itg_handle* h, int64_t m, int64_t n, const double* 
                              double* U, double* S, double* V,
                              int64_t* k, double* truncerr, double* docut,
                              int method, int precision);
+/* Truncated factorisation A ~ L C with one exactly orthonormal factor, the
+ * two-site bond split of the DMRG sweep: ITensors' factorize(phi, inds;
+ * ortho, maxdim, mindim, cutoff) as called by replacebond! inside dmrg
+ * (ITensors 0.2, external; used at examples/dmrg.jl:25, test/dmrg.jl:27,75),
+ * built on the SVD that src/tensor/culinearalgebra.jl:33-72 provides.
+ *  ortho = ITG_ORTHO_LEFT : L (m x k) has orthonormal columns, C = L^T A (k x n) = S V^T.
+ *  ortho = ITG_ORTHO_RIGHT: L (n x k) has orthonormal columns, C = A L   (m x k) = U S.
+ * The orthonormal factor is the one built from rotations (or refined
+ * eigenvectors), never from a division by S, so it stays orthonormal for
+ * kept singular values of any size; C is a matrix product at `precision`.
+ * S (min(m,n)) holds the singular values, k/truncerr/docut as itg_svd_trunc.
+ * L and C each hold max(m,n)*min(m,n) doubles (C's slot is also scratch). */
+enum { ITG_ORTHO_LEFT = 0, ITG_ORTHO_RIGHT = 1 };
+ITG_API int itg_factorize_trunc(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
+                                int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
+                                int doRelCutoff, int legacy_gpu, int ortho, int method, int precision,
+                                double* L, double* S, double* C, int64_t* k, double* truncerr,
+                                double* docut);
+/* Jacobi sweeps run by the last itg_svd_trunc / itg_svd_trunc_ex / itg_eigh_trunc
+ * call on this handle (FP32 sweeps for the mixed method). */
+ITG_API int itg_svd_info(itg_handle* h, int* sweeps);
+/* SVD options of this handle.  qr_precondition = 1 (default): for
+ * min(m, n) > 192 the working matrix is first factored A = Q R by Householder
+ * reflections and the Jacobi iteration runs on R^T (far fewer sweeps on
+ * graded spectra; A = (Q V_B) S U_B^T from R^T = U_B S V_B^T).  jacobi_mode:
+ * 0 (default) or 1: one launch per round-robin step (queued back to back);
+ * 2: all sweeps in one cooperative launch with a grid barrier between steps
+ * (measured slower on GB300; kept for comparison). */
+ITG_API int itg_set_svd_options(itg_handle* h, int qr_precondition, int jacobi_mode);
 
 /* Eigendecomposition of the symmetric n x n matrix A: A = U diag(D) U^T with D
  * descending, then truncation of D as a spectrum.  U holds n*n doubles.

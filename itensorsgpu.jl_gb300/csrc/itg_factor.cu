@@ -397,6 +397,87 @@ __global__ void k_gershgorin(const double* __restrict__ A, int64_t lda, int64_t 
 
 namespace {
 
+// ------------------------------------------------ QR preconditioning
+// One-sided Jacobi converges in far fewer sweeps on R^T, where A = Q R, than on
+// A itself when A's singular values are graded (the QR-preconditioned Jacobi
+// of Drmac & Veselic, "New fast and accurate Jacobi SVD algorithm I", SIAM J.
+// Matrix Anal. Appl. 29 (2008)): for A = U diag(exp(-k/20)) V^T, 10 sweeps
+// instead of about 30.  With B = R^T = U_B S V_B^T: A = (Q V_B) S U_B^T.
+//
+// Householder step j of A (m x n, column-major): every CTA reads column j
+// (never written during the step) and forms the same reflector
+//   beta = -sign(alpha) |x|, tau = (beta - alpha) / beta, v = x / (alpha - beta), v_j = 1;
+// CTA 0 stores v, tau and beta; CTA c > 0 applies I - tau v v^T to column j + c.
+template <int T>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < T / 32; ++w) s += sh[w];
+  __syncthreads();
+  return s;
+}
+
+__global__ void __launch_bounds__(256)
+k_house_step(double* __restrict__ A, int64_t m, int j, double* __restrict__ Vh, double* __restrict__ tau,
+             double* __restrict__ rdiag) {
+  __shared__ double sh[8];
+  const double* x = A + (int64_t)j * m;
+  const double alpha = x[j];
+  double s2 = 0.0;
+  for (int64_t i = j + 1 + threadIdx.x; i < m; i += 256) s2 = fma(x[i], x[i], s2);
+  s2 = block_sum<256>(s2, sh);
+  double tj = 0.0, beta = alpha, scale = 0.0;
+  if (s2 > 0.0) {
+    beta = -copysign(hypot(alpha, sqrt(s2)), alpha);
+    tj = (beta - alpha) / beta;
+    scale = 1.0 / (alpha - beta);
+  }
+  if (blockIdx.x == 0) {
+    double* v = Vh + (int64_t)j * m;
+    for (int64_t i = threadIdx.x; i < m; i += 256) v[i] = i < j ? 0.0 : (i == j ? 1.0 : x[i] * scale);
+    if (threadIdx.x == 0) {
+      tau[j] = tj;
+      rdiag[j] = beta;
+    }
+    return;
+  }
+  if (tj == 0.0) return;
+  double* col = A + (int64_t)(j + blockIdx.x) * m;
+  double w = 0.0;
+  for (int64_t i = j + 1 + threadIdx.x; i < m; i += 256) w = fma(x[i] * scale, col[i], w);
+  w = block_sum<256>(w, sh) + col[j];
+  const double f = tj * w;
+  for (int64_t i = j + threadIdx.x; i < m; i += 256) col[i] -= f * (i == j ? 1.0 : x[i] * scale);
+}
+
+// B = R^T (n x n, lower triangular) from the factored A (R above the diagonal, diagonal in rdiag).
+__global__ void k_build_rt(const double* __restrict__ A, int64_t m, int n, const double* __restrict__ rdiag,
+                           double* __restrict__ B) {
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nn; t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / n), i = (int)(t - (int64_t)k * n);  // B(i, k) = R(k, i)
+    B[t] = k < i ? A[k + (int64_t)i * m] : (k == i ? rdiag[i] : 0.0);
+  }
+}
+
+// Y <- (I - tau_j v_j v_j^T) Y for the first `ncols` columns of Y (m rows, ld m).
+__global__ void __launch_bounds__(256)
+k_house_apply(double* __restrict__ Y, int64_t m, int j, const double* __restrict__ Vh,
+              const double* __restrict__ tau) {
+  __shared__ double sh[8];
+  const double tj = tau[j];
+  if (tj == 0.0) return;
+  const double* v = Vh + (int64_t)j * m;
+  double* y = Y + (int64_t)blockIdx.x * m;
+  double w = 0.0;
+  for (int64_t i = j + threadIdx.x; i < m; i += 256) w = fma(v[i], y[i], w);
+  w = block_sum<256>(w, sh);
+  const double f = tj * w;
+  for (int64_t i = j + threadIdx.x; i < m; i += 256) y[i] -= f * v[i];
+}
+
 constexpr int JACOBI_MAX_SWEEPS = 60;
 constexpr int JACOBI_AUX_INTS = 8 + JACOBI_MAX_SWEEPS;
 constexpr int64_t ONECTA_MAX_N = 192;
@@ -419,8 +500,8 @@ int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* f
     *sweeps_done = hp[0];
     return hp[0] >= JACOBI_MAX_SWEEPS ? ITG_ERR_NOTCONVERGED : ITG_OK;
   }
-  {
-    const int st = itg::jacobi_persistent<double>(h, W, m, (int)n, V, tol, JACOBI_MAX_SWEEPS, flag_dev,
+  if (h->jacobi_mode == 2) {
+    const int st = itg::jacobi_persistent<double>(h, W, m, (int)n, V, tol, 0.0, JACOBI_MAX_SWEEPS, flag_dev,
                                                   sweeps_done);
     if (st != ITG_ERR_UNSUPPORTED) return st;
   }
@@ -454,17 +535,21 @@ __global__ void k_sqrt_clamp(const double* __restrict__ lam, int n, double* __re
     sig[i] = sqrt(fmax(lam[i], 0.0));
 }
 
+// Side of the working matrix that must come out exactly orthonormal (see svd_trunc_impl).
+enum { ISO_NONE = -1, ISO_LEFT = 0, ISO_RIGHT = 1 };
+
 static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
                           int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
                           int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
-                          int64_t* k, double* truncerr, double* docut, int method, int precision);
+                          int64_t* k, double* truncerr, double* docut, int method, int precision,
+                          int iso);
 
 extern "C" int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
                              int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
                              int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
                              int64_t* k, double* truncerr, double* docut) {
   return svd_trunc_impl(h, m, n, A, lda, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff,
-                        legacy_gpu, U, S, V, k, truncerr, docut, ITG_SVD_JACOBI, ITG_PREC_FP64);
+                        legacy_gpu, U, S, V, k, truncerr, docut, ITG_SVD_JACOBI, ITG_PREC_FP64, ISO_NONE);
 }
 
 extern "C" int itg_svd_trunc_ex(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
@@ -477,13 +562,41 @@ extern "C" int itg_svd_trunc_ex(itg_handle* h, int64_t m, int64_t n, const doubl
   if (precision != ITG_PREC_FP64 && precision != ITG_PREC_SPLIT)
     return itg_fail(h, ITG_ERR_INVALID, "unknown precision %d", precision);
   return svd_trunc_impl(h, m, n, A, lda, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff,
-                        legacy_gpu, U, S, V, k, truncerr, docut, method, precision);
+                        legacy_gpu, U, S, V, k, truncerr, docut, method, precision, ISO_NONE);
 }
+
+// Householder QR of the tall matrix X (rows x cols, ld rows) in place:
+// reflectors in Vh, tau; R's diagonal in rd, its strict upper triangle in X.
+static int house_qr(itg_handle* h, double* X, int64_t rows, int64_t cols, double* Vh, double* tau, double* rd) {
+  for (int64_t j = 0; j < cols; ++j)
+    k_house_step<<<(unsigned)(cols - j), 256, 0, h->stream>>>(X, rows, (int)j, Vh, tau, rd);
+  ITG_CHECK_LAUNCH(h);
+  return ITG_OK;
+}
+
+// Y <- H_0 ... H_{cols-1} Y on the first ncols columns of Y (rows x ., ld rows).
+static int house_apply(itg_handle* h, double* Y, int64_t rows, int64_t cols, int64_t ncols, const double* Vh,
+                       const double* tau) {
+  if (ncols <= 0) return ITG_OK;
+  for (int64_t j = cols - 1; j >= 0; --j)
+    k_house_apply<<<(unsigned)ncols, 256, 0, h->stream>>>(Y, rows, (int)j, Vh, tau);
+  ITG_CHECK_LAUNCH(h);
+  return ITG_OK;
+}
+
+// iso: which side of the working matrix W (the tall orientation of A) must
+// come out with exactly orthonormal columns when W is large:
+//   ISO_LEFT : W = Q R, Jacobi on J = R^T;             W = (Q V_J) S U_J^T
+//   ISO_RIGHT: W = Q1 R1, R1^T = Q2 R2, J = R2^T;      W = (Q1 U_J) S (Q2 V_J)^T
+// V_J (the Jacobi rotations, or the refined eigenvectors of the mixed method)
+// is orthonormal to rounding; U_J = J V_J / S is accurate only where S is
+// resolved.  ISO_NONE uses ISO_LEFT when QR preconditioning is on.
 
 static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
                           int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
                           int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
-                          int64_t* k, double* truncerr, double* docut, int method, int precision) {
+                          int64_t* k, double* truncerr, double* docut, int method, int precision,
+                          int iso) {
   if (!h || m < 0 || n < 0 || lda < m || !A || !U || !S || !V) return ITG_ERR_INVALID;
   if (m == 0 || n == 0) {
     if (k) *k = 0;
@@ -494,19 +607,37 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
   const bool tr = m < n;
   const int64_t mm = tr ? n : m, nn = tr ? m : n;  // working shape, mm >= nn
   if (nn > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "svd: min(m,n) too large");
-  // scratch: W (mm*nn) | Vw (nn*nn) | sig (nn) | S,P (2 nn) | order (nn ints) | out3 | flag
   size_t off = 0;
   auto take = [&](size_t bytes) { size_t o = off; off += itg_align256(bytes); return o; };
   const bool mixed = method == ITG_SVD_MIXED || (method == ITG_SVD_AUTO && nn > ONECTA_MAX_N);
+  // QR preconditioning for large problems, and for the mixed method whenever
+  // a side must be exactly orthonormal
+  const bool pre = (h->svd_qr_precond && nn > ONECTA_MAX_N) || (mixed && iso != ISO_NONE);
+  const bool two = pre && iso == ISO_RIGHT;
+  // the Jacobi problem: W itself (mj = mm rows) or J (nn x nn)
+  const int64_t mj = pre ? nn : mm;
   size_t oW = take(sizeof(double) * mm * nn), oV = take(sizeof(double) * nn * nn),
          oSig = take(sizeof(double) * nn), oP = take(sizeof(double) * nn),
          oOrd = take(sizeof(int) * nn), oOut = take(4 * sizeof(double)), oFlag = take(sizeof(int) * JACOBI_AUX_INTS);
-  size_t oLam = 0, oUw = 0, oWs = 0, oWs32 = 0;
+  size_t oLam = 0, oUw = 0, oWs = 0, oWs32 = 0, oVh = 0, oTau = 0, oRd = 0, oB = 0, oVh2 = 0, oTau2 = 0,
+         oRd2 = 0, oB2 = 0;
   if (mixed) {
     oLam = take(sizeof(double) * nn);
-    oUw = take(sizeof(double) * mm * nn);
-    oWs = take(sizeof(double) * itg::svd_mixed_ws_doubles(mm, nn));
-    oWs32 = take(sizeof(float) * (mm * nn + nn * nn));
+    oUw = take(sizeof(double) * mj * nn);
+    oWs = take(sizeof(double) * itg::svd_mixed_ws_doubles(mj, nn));
+    oWs32 = take(sizeof(float) * (mj * nn + nn * nn));
+  }
+  if (pre) {
+    oVh = take(sizeof(double) * mm * nn);
+    oTau = take(sizeof(double) * nn);
+    oRd = take(sizeof(double) * nn);
+    oB = take(sizeof(double) * nn * nn);
+  }
+  if (two) {
+    oVh2 = take(sizeof(double) * nn * nn);
+    oTau2 = take(sizeof(double) * nn);
+    oRd2 = take(sizeof(double) * nn);
+    oB2 = take(sizeof(double) * nn * nn);
   }
   ITG_TRY(itg_scratch_reserve(h, off));
   char* base = (char*)h->scratch;
@@ -528,36 +659,119 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
   int st = ITG_OK;
   double* Uw_dst = tr ? V : U;  // rows mm
   double* Vw_dst = tr ? U : V;  // rows nn
-  dim3 g1(itg_blocks_for(mm, 256, 64), (unsigned)nn), g2(itg_blocks_for(nn, 256, 64), (unsigned)nn);
+  double* J = W;
+  double *Vh = nullptr, *tau = nullptr, *Vh2 = nullptr, *tau2 = nullptr;
+  if (pre) {
+    Vh = (double*)(base + oVh);
+    tau = (double*)(base + oTau);
+    double* rd = (double*)(base + oRd);
+    J = (double*)(base + oB);
+    ITG_TRY(house_qr(h, W, mm, nn, Vh, tau, rd));
+    k_build_rt<<<itg_blocks_for(nn * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(W, mm, (int)nn, rd, J);
+    ITG_CHECK_LAUNCH(h);
+    if (two) {
+      Vh2 = (double*)(base + oVh2);
+      tau2 = (double*)(base + oTau2);
+      double* rd2 = (double*)(base + oRd2);
+      double* J2 = (double*)(base + oB2);
+      ITG_TRY(house_qr(h, J, nn, nn, Vh2, tau2, rd2));
+      k_build_rt<<<itg_blocks_for(nn * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(J, nn, (int)nn, rd2, J2);
+      ITG_CHECK_LAUNCH(h);
+      J = J2;
+    }
+  }
+  // J's factors: left U_J (mj rows) and right V_J (nn rows), written where
+  // they end up: without preconditioning W's left / right; with one QR, V_J
+  // goes (zero-padded) to W's left slot and is rotated by Q; with two, U_J goes
+  // to W's left slot (rotated by Q1) and V_J to the right slot (rotated by Q2).
+  double* Jl_dst = !pre ? Uw_dst : (two ? Uw_dst : Vw_dst);
+  double* Jr_dst = !pre ? Vw_dst : (two ? Vw_dst : Uw_dst);
+  const int64_t ld_l = !pre ? mm : (two ? mm : nn);
+  const int64_t ld_r = !pre ? nn : (two ? nn : mm);
+  if (pre) ITG_CUDA(h, cudaMemsetAsync(Uw_dst, 0, sizeof(double) * mm * nn, h->stream));
+  dim3 g1(itg_blocks_for(mj, 256, 64), (unsigned)nn), g2(itg_blocks_for(nn, 256, 64), (unsigned)nn);
   if (mixed) {
     double* lam = (double*)(base + oLam);
     double* Uw = (double*)(base + oUw);
-    ITG_TRY(itg::svd_mixed_core(h, W, mm, nn, precision, Vw, lam, Uw, (double*)(base + oWs),
+    ITG_TRY(itg::svd_mixed_core(h, J, mj, nn, precision, Vw, lam, Uw, (double*)(base + oWs),
                                 (float*)(base + oWs32), flag, &sweeps));
     k_sqrt_clamp<<<itg_blocks_for(nn, 256, 64), 256, 0, h->stream>>>(lam, (int)nn, sig);
     k_rank_desc<<<itg_blocks_for(nn, 256, 1024), 256, 0, h->stream>>>(sig, (int)nn, 0.0, order, S, P, 1);
     ITG_CHECK_LAUNCH(h);
     ITG_TRY(itg::truncate_dev(h, P, nn, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, out3));
-    k_gather_cols<<<g1, 256, 0, h->stream>>>(Uw, mm, order, sig, 0, (int)nn, Uw_dst, mm);
-    k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, nn, order, sig, 0, (int)nn, Vw_dst, nn);
+    k_gather_cols<<<g1, 256, 0, h->stream>>>(Uw, mj, order, sig, 0, (int)nn, Jl_dst, ld_l);
+    k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, nn, order, sig, 0, (int)nn, Jr_dst, ld_r);
     ITG_CHECK_LAUNCH(h);
   } else {
-    st = jacobi_run(h, W, mm, nn, Vw, flag, &sweeps);
+    st = jacobi_run(h, J, mj, nn, Vw, flag, &sweeps);
     if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED) return st;
     k_unit_cols<<<(unsigned)nn, 256, 0, h->stream>>>(Vw, nn);
-    k_col_norms<<<(unsigned)nn, 256, 0, h->stream>>>(W, mm, sig);
+    k_col_norms<<<(unsigned)nn, 256, 0, h->stream>>>(J, mj, sig);
     k_rank_desc<<<itg_blocks_for(nn, 256, 1024), 256, 0, h->stream>>>(sig, (int)nn, 0.0, order, S, P, 1);
     ITG_CHECK_LAUNCH(h);
     ITG_TRY(itg::truncate_dev(h, P, nn, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, out3));
-    // Left factor of the working problem = W[:, order] / sig; right = Vw[:, order].
-    k_gather_cols<<<g1, 256, 0, h->stream>>>(W, mm, order, sig, 1, (int)nn, Uw_dst, mm);
-    k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, nn, order, sig, 0, (int)nn, Vw_dst, nn);
+    // U_J = J[:, order] / sig; V_J = Vw[:, order].
+    k_gather_cols<<<g1, 256, 0, h->stream>>>(J, mj, order, sig, 1, (int)nn, Jl_dst, ld_l);
+    k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, nn, order, sig, 0, (int)nn, Jr_dst, ld_r);
     ITG_CHECK_LAUNCH(h);
   }
+  h->last_sweeps = sweeps;
   ITG_TRY(read_out3(h, out3, k, truncerr, docut));
+  if (pre) {
+    // rotate the kept columns back
+    const int64_t kk = (k && *k > 0) ? *k : nn;
+    ITG_TRY(house_apply(h, Uw_dst, mm, nn, kk, Vh, tau));
+    if (two) ITG_TRY(house_apply(h, Vw_dst, nn, nn, kk, Vh2, tau2));
+  }
   if (st == ITG_ERR_NOTCONVERGED)
     return itg_fail(h, ITG_ERR_NOTCONVERGED, "Jacobi SVD did not converge in %d sweeps", sweeps);
   return ITG_OK;
+}
+
+extern "C" int itg_factorize_trunc(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
+                                   int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
+                                   int doRelCutoff, int legacy_gpu, int ortho, int method, int precision,
+                                   double* L, double* S, double* C, int64_t* k, double* truncerr,
+                                   double* docut) {
+  if (!h || !A || !L || !S || !C || m < 0 || n < 0 || lda < m) return ITG_ERR_INVALID;
+  if (ortho != ITG_ORTHO_LEFT && ortho != ITG_ORTHO_RIGHT) return itg_fail(h, ITG_ERR_INVALID, "unknown ortho %d", ortho);
+  if (method != ITG_SVD_AUTO && method != ITG_SVD_JACOBI && method != ITG_SVD_MIXED)
+    return itg_fail(h, ITG_ERR_INVALID, "unknown SVD method %d", method);
+  if (precision != ITG_PREC_FP64 && precision != ITG_PREC_SPLIT)
+    return itg_fail(h, ITG_ERR_INVALID, "unknown precision %d", precision);
+  int64_t kk = 0;
+  if (m == 0 || n == 0) {
+    if (k) *k = 0;
+    if (truncerr) *truncerr = 0;
+    if (docut) *docut = 0;
+    return ITG_OK;
+  }
+  if (lda != m) return itg_fail(h, ITG_ERR_UNSUPPORTED, "factorize needs lda == m");
+  // the isometric factor in L's slot (U for ortho left, V for right); the other
+  // SVD factor is scratch output in C's slot and replaced by the projection
+  const bool tr = m < n;
+  const int iso = (ortho == ITG_ORTHO_LEFT) == !tr ? ISO_LEFT : ISO_RIGHT;
+  double* Ubuf = ortho == ITG_ORTHO_LEFT ? L : C;
+  double* Vbuf = ortho == ITG_ORTHO_LEFT ? C : L;
+  int st = svd_trunc_impl(h, m, n, A, lda, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, Ubuf,
+                          S, Vbuf, &kk, truncerr, docut, method, precision, iso);
+  if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED) return st;
+  if (k) *k = kk;
+  if (kk == 0) return st;
+  // C = L^T A (kk x n) or C = A L (m x kk); C must not alias the GEMM operands,
+  // so the scratch factor in C's slot is simply overwritten
+  const int64_t dA[2] = {m, n};
+  const int32_t mA[2] = {1, 2};
+  if (ortho == ITG_ORTHO_LEFT) {
+    const int64_t dL[2] = {m, kk}, dC[2] = {kk, n};
+    const int32_t mL[2] = {1, 3}, mC[2] = {3, 2};
+    ITG_TRY(itg::contract_f64(h, 1.0, L, 2, dL, mL, A, 2, dA, mA, 0.0, C, 2, dC, mC, precision));
+  } else {
+    const int64_t dR[2] = {n, kk}, dC[2] = {m, kk};
+    const int32_t mR[2] = {2, 3}, mC[2] = {1, 3};
+    ITG_TRY(itg::contract_f64(h, 1.0, A, 2, dA, mA, L, 2, dR, mR, 0.0, C, 2, dC, mC, precision));
+  }
+  return st == ITG_ERR_NOTCONVERGED ? itg_fail(h, st, "Jacobi SVD did not converge") : ITG_OK;
 }
 
 extern "C" int itg_eigh_trunc(itg_handle* h, int64_t n, const double* A, int64_t lda,
@@ -609,6 +823,7 @@ extern "C" int itg_eigh_trunc(itg_handle* h, int64_t n, const double* A, int64_t
   dim3 g2(itg_blocks_for(n, 256, 64), (unsigned)n);
   k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, n, order, sig, 0, (int)n, U, n);
   ITG_CHECK_LAUNCH(h);
+  h->last_sweeps = sweeps;
   ITG_TRY(read_out3(h, out3, k, truncerr, docut));
   if (st == ITG_ERR_NOTCONVERGED)
     return itg_fail(h, ITG_ERR_NOTCONVERGED, "Jacobi eigensolver did not converge in %d sweeps", sweeps);
@@ -699,5 +914,18 @@ extern "C" int itg_qr(itg_handle* h, int64_t m, int64_t n, const double* A, int6
     }
     ITG_CHECK_LAUNCH(h);
   }
+  return ITG_OK;
+}
+
+extern "C" int itg_svd_info(itg_handle* h, int* sweeps) {
+  if (!h || !sweeps) return ITG_ERR_INVALID;
+  *sweeps = h->last_sweeps;
+  return ITG_OK;
+}
+
+extern "C" int itg_set_svd_options(itg_handle* h, int qr_precondition, int jacobi_mode) {
+  if (!h || jacobi_mode < 0 || jacobi_mode > 2) return ITG_ERR_INVALID;
+  h->svd_qr_precond = qr_precondition != 0;
+  h->jacobi_mode = jacobi_mode;
   return ITG_OK;
 }

@@ -76,6 +76,9 @@ struct itg_handle {
   void* tune_buf = nullptr;   // throw-away outputs of tuning launches
   size_t tune_buf_bytes = 0;
   int64_t tune_runs = 0;
+  int last_sweeps = 0;        // Jacobi sweeps of the last SVD / eigh call
+  bool svd_qr_precond = true; // itg_set_svd_options
+  int jacobi_mode = 0;        // 0 / 1: one launch per step, 2: one cooperative launch
 };
 
 // Record a timing event pair around a launch when profiling is on.
@@ -92,7 +95,7 @@ namespace itg {
 // launch; aux holds jacobi_aux_ints(max_sweeps) device ints.
 int jacobi_aux_ints(int max_sweeps);
 template <class T>
-int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, int max_sweeps, int* aux,
+int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* aux,
                       int* sweeps);
 }  // namespace itg
 

@@ -3,11 +3,12 @@
 //
 // The per-step formulation (one launch per round-robin step, 2n launches per
 // sweep) is bound by launch latency and by re-fetching the pair's columns
-// cold each step.  Here one launch runs all sweeps: warps own column pairs
-// (warp w takes pairs w, w + #warps, ... of the step), the steps are separated
+// cold each step.  Here one launch runs all sweeps: the steps are separated
 // by a grid-wide barrier, and the kernel leaves when a sweep rotated nothing.
-// Same pairing (Brent-Luk round robin), rotation formula and skip rule as the
-// one-CTA and per-step kernels of itg_factor.cu:
+// CTAs own column pairs (CTA b takes pairs b, b + gridDim.x, ... of the
+// step; a pair's columns are cached in registers between the dot products and
+// the rotation).  Same pairing (Brent-Luk round robin), rotation formula and
+// skip rule as the one-CTA and per-step kernels of itg_factor.cu:
 //   zeta = (b - a) / (2g), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)),
 //   c = 1/sqrt(1 + t^2), s = c t;  skip when |g| <= tol sqrt(a) sqrt(b).
 //
@@ -80,62 +81,114 @@ __device__ bool jp_grid_sync(unsigned* count, unsigned* gen, int* status, unsign
   return ok != 0;
 }
 
+// Block-wide sums of three values (every thread gets the same totals: the
+// per-warp partials are added in a fixed order).
+template <class T>
+__device__ __forceinline__ void jp_block_sum3(T& a, T& b, T& g, T (*sh)[JP_WARPS]) {
+  a = jp_warp_sum(a);
+  b = jp_warp_sum(b);
+  g = jp_warp_sum(g);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    sh[0][warp] = a;
+    sh[1][warp] = b;
+    sh[2][warp] = g;
+  }
+  __syncthreads();
+  a = 0;
+  b = 0;
+  g = 0;
+#pragma unroll
+  for (int w = 0; w < JP_WARPS; ++w) {
+    a += sh[0][w];
+    b += sh[1][w];
+    g += sh[2][w];
+  }
+  __syncthreads();  // sh is reused by the next pair
+}
+
 // aux (ints, zeroed by the host): [0] barrier count, [1] generation,
 // [2] timeout status, [3] sweeps run (max_sweeps + 1: limit hit, -1: timed
 // out), [8 + s] "sweep s rotated".
-template <class T>
+// One CTA per column pair (CTA b takes pairs b, b + gridDim.x, ... of the
+// step).  RC = column elements cached per thread (m <= JP_THREADS * RC), so a
+// pair's columns are read once per step; RC = 0 streams them (any m).
+template <class T, int RC>
 __global__ void __launch_bounds__(JP_THREADS)
-k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, int max_sweeps, int* aux) {
+k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T amin, int max_sweeps,
+                 int* aux) {
+  __shared__ T sh[3][JP_WARPS];
   unsigned* count = (unsigned*)aux;
   unsigned* gen = (unsigned*)aux + 1;
   int* status = aux + 2;
   int* rot = aux + 8;
   const int np = n + (n & 1), npairs = np / 2;
-  const int lane = threadIdx.x & 31;
-  const int gw = blockIdx.x * JP_WARPS + (threadIdx.x >> 5), nw = gridDim.x * JP_WARPS;
+  const int t = threadIdx.x;
   int done = max_sweeps + 1;  // not converged within max_sweeps
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     for (int step = 0; step < np - 1; ++step) {
-      for (int pi = gw; pi < npairs; pi += nw) {
+      for (int pi = blockIdx.x; pi < npairs; pi += gridDim.x) {
         int p = jp_player(pi, step, np), q = jp_player(np - 1 - pi, step, np);
-        if (p >= n || q >= n) continue;
+        if (p >= n || q >= n) continue;  // block-uniform
         if (p > q) {
-          const int t = p;
+          const int tmp = p;
           p = q;
-          q = t;
+          q = tmp;
         }
         T* wp = W + (int64_t)p * m;
         T* wq = W + (int64_t)q * m;
         T a = 0, b = 0, g = 0;
-#pragma unroll 4
-        for (int64_t i = lane; i < m; i += 32) {
-          const T x = __ldcg(wp + i), y = __ldcg(wq + i);
-          a = fma(x, x, a);
-          b = fma(y, y, b);
-          g = fma(x, y, g);
+        T xr[RC > 0 ? RC : 1], yr[RC > 0 ? RC : 1];
+        if (RC > 0) {
+#pragma unroll
+          for (int r = 0; r < RC; ++r) {
+            const int64_t i = t + (int64_t)r * JP_THREADS;
+            xr[r] = i < m ? __ldcg(wp + i) : T(0);
+            yr[r] = i < m ? __ldcg(wq + i) : T(0);
+          }
+#pragma unroll
+          for (int r = 0; r < RC; ++r) {
+            a = fma(xr[r], xr[r], a);
+            b = fma(yr[r], yr[r], b);
+            g = fma(xr[r], yr[r], g);
+          }
+        } else {
+          for (int64_t i = t; i < m; i += JP_THREADS) {
+            const T x = __ldcg(wp + i), y = __ldcg(wq + i);
+            a = fma(x, x, a);
+            b = fma(y, y, b);
+            g = fma(x, y, g);
+          }
         }
-        a = jp_warp_sum(a);
-        b = jp_warp_sum(b);
-        g = jp_warp_sum(g);
-        if (a == T(0) || b == T(0) || fabs(g) <= tol * sqrt(a) * sqrt(b)) continue;
+        jp_block_sum3(a, b, g, sh);
+        if (a <= amin || b <= amin || fabs(g) <= tol * sqrt(a) * sqrt(b)) continue;  // block-uniform
         const T zeta = (b - a) / (T(2) * g);
-        const T t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-        const T c = T(1) / sqrt(T(1) + t * t), s = c * t;
-#pragma unroll 4
-        for (int64_t i = lane; i < m; i += 32) {
-          const T x = __ldcg(wp + i), y = __ldcg(wq + i);
-          __stcg(wp + i, c * x - s * y);
-          __stcg(wq + i, s * x + c * y);
+        const T tt = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+        const T c = T(1) / sqrt(T(1) + tt * tt), s = c * tt;
+        if (RC > 0) {
+#pragma unroll
+          for (int r = 0; r < RC; ++r) {
+            const int64_t i = t + (int64_t)r * JP_THREADS;
+            if (i < m) {
+              __stcg(wp + i, c * xr[r] - s * yr[r]);
+              __stcg(wq + i, s * xr[r] + c * yr[r]);
+            }
+          }
+        } else {
+          for (int64_t i = t; i < m; i += JP_THREADS) {
+            const T x = __ldcg(wp + i), y = __ldcg(wq + i);
+            __stcg(wp + i, c * x - s * y);
+            __stcg(wq + i, s * x + c * y);
+          }
         }
         T* vp = V + (int64_t)p * n;
         T* vq = V + (int64_t)q * n;
-#pragma unroll 4
-        for (int i = lane; i < n; i += 32) {
+        for (int i = t; i < n; i += JP_THREADS) {
           const T x = __ldcg(vp + i), y = __ldcg(vq + i);
           __stcg(vp + i, c * x - s * y);
           __stcg(vq + i, s * x + c * y);
         }
-        if (lane == 0) __stcg(rot + sweep, 1);
+        if (t == 0) __stcg(rot + sweep, 1);
       }
       if (!jp_grid_sync(count, gen, status, gridDim.x)) {
         done = -1;
@@ -161,25 +214,36 @@ int jacobi_aux_ints(int max_sweeps) { return 8 + max_sweeps; }
 // by the caller).  *sweeps = sweeps run; ITG_ERR_NOTCONVERGED when the limit
 // was hit (results usable), ITG_ERR_UNSUPPORTED when the device cannot run a
 // cooperative launch (the caller then uses per-step launches).
+template <class T, int RC>
+int launch_persist(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* aux) {
+  int per_sm = 0;
+  ITG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi_persist<T, RC>, JP_THREADS, 0));
+  if (per_sm < 1) return ITG_ERR_UNSUPPORTED;
+  if (per_sm > 4) per_sm = 4;  // fewer arrivals per barrier
+  const int np = n + (n & 1);
+  int64_t grid = (int64_t)h->num_sms * per_sm;
+  if ((int64_t)np / 2 < grid) grid = np / 2;
+  if (grid < 1) grid = 1;
+  void* args[] = {(void*)&W,   (void*)&m,          (void*)&n,  (void*)&V,
+                  (void*)&tol, (void*)&amin, (void*)&max_sweeps, (void*)&aux};
+  ITG_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_jacobi_persist<T, RC>, dim3((unsigned)grid),
+                                          dim3(JP_THREADS), args, 0, h->stream));
+  return ITG_OK;
+}
+
 template <class T>
-int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, int max_sweeps, int* aux,
+int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* aux,
                       int* sweeps) {
   int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device);
   if (!coop) return ITG_ERR_UNSUPPORTED;
-  int per_sm = 0;
-  ITG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi_persist<T>, JP_THREADS, 0));
-  if (per_sm < 1) return ITG_ERR_UNSUPPORTED;
-  if (per_sm > 2) per_sm = 2;  // fewer arrivals per barrier; 16 warps per SM is enough
-  const int np = n + (n & 1);
-  const int64_t want = ((int64_t)np / 2 + JP_WARPS - 1) / JP_WARPS;
-  int64_t grid = (int64_t)h->num_sms * per_sm;
-  if (want < grid) grid = want;
-  if (grid < 1) grid = 1;
   ITG_CUDA(h, cudaMemsetAsync(aux, 0, sizeof(int) * jacobi_aux_ints(max_sweeps), h->stream));
-  void* args[] = {(void*)&W, (void*)&m, (void*)&n, (void*)&V, (void*)&tol, (void*)&max_sweeps, (void*)&aux};
-  ITG_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_jacobi_persist<T>, dim3((unsigned)grid), dim3(JP_THREADS),
-                                          args, 0, h->stream));
+  int st;
+  if (m <= 4 * JP_THREADS) st = launch_persist<T, 4>(h, W, m, n, V, tol, amin, max_sweeps, aux);
+  else if (m <= 8 * JP_THREADS) st = launch_persist<T, 8>(h, W, m, n, V, tol, amin, max_sweeps, aux);
+  else if (m <= 16 * JP_THREADS) st = launch_persist<T, 16>(h, W, m, n, V, tol, amin, max_sweeps, aux);
+  else st = launch_persist<T, 0>(h, W, m, n, V, tol, amin, max_sweeps, aux);
+  if (st != ITG_OK) return st;
   int* hp = (int*)h->pinned;
   ITG_CUDA(h, cudaMemcpyAsync(hp, aux, sizeof(int) * 4, cudaMemcpyDeviceToHost, h->stream));
   ITG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -189,7 +253,8 @@ int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, int ma
   return hp[3] > max_sweeps ? ITG_ERR_NOTCONVERGED : ITG_OK;
 }
 
-template int jacobi_persistent<float>(itg_handle*, float*, int64_t, int, float*, float, int, int*, int*);
-template int jacobi_persistent<double>(itg_handle*, double*, int64_t, int, double*, double, int, int*, int*);
+template int jacobi_persistent<float>(itg_handle*, float*, int64_t, int, float*, float, float, int, int*, int*);
+template int jacobi_persistent<double>(itg_handle*, double*, int64_t, int, double*, double, double, int, int*,
+                                        int*);
 
 }  // namespace itg

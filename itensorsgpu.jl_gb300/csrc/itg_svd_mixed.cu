@@ -41,6 +41,8 @@ int contract_f64(itg_handle* h, double alpha, const double* A, int rankA, const 
 
 namespace {
 
+constexpr int ONECTA32_MAX_N = 192;  // larger problems: one launch per step
+
 __device__ __forceinline__ int rr_player32(int pos, int step, int np) {
   if (pos == 0) return 0;
   return ((pos - 1 + step) % (np - 1)) + 1;
@@ -53,8 +55,8 @@ __device__ __forceinline__ float warp_sumf(float v) {
 
 // One round-robin step of FP32 one-sided Jacobi: one CTA per column pair.
 __global__ void __launch_bounds__(256)
-k_jacobi32_step(float* __restrict__ W, int64_t m, int n, float* __restrict__ V, float tol, int step,
-                int* __restrict__ rotated) {
+k_jacobi32_step(float* __restrict__ W, int64_t m, int n, float* __restrict__ V, float tol, float amin,
+                int step, int* __restrict__ rotated) {
   __shared__ float sh[3][8];
   const int np = n + (n & 1);
   int p = rr_player32(blockIdx.x, step, np), q = rr_player32(np - 1 - blockIdx.x, step, np);
@@ -75,7 +77,7 @@ k_jacobi32_step(float* __restrict__ W, int64_t m, int n, float* __restrict__ V, 
   __syncthreads();
   a = 0.f; b = 0.f; g = 0.f;
   for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a += sh[0][w]; b += sh[1][w]; g += sh[2][w]; }
-  if (a == 0.f || b == 0.f || fabsf(g) <= tol * sqrtf(a) * sqrtf(b)) return;
+  if (a <= amin || b <= amin || fabsf(g) <= tol * sqrtf(a) * sqrtf(b)) return;
   const float zeta = (b - a) / (2.f * g);
   const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
   const float c = 1.f / sqrtf(1.f + t * t), s = c * t;
@@ -97,8 +99,8 @@ k_jacobi32_step(float* __restrict__ W, int64_t m, int n, float* __restrict__ V, 
 // All sweeps in one CTA (n <= 512): warps take column pairs of each
 // round-robin step; __syncthreads between steps.
 __global__ void __launch_bounds__(1024)
-k_jacobi32_onecta(float* __restrict__ W, int64_t m, int n, float* __restrict__ V, float tol, int max_sweeps,
-                  int* __restrict__ sweeps_out) {
+k_jacobi32_onecta(float* __restrict__ W, int64_t m, int n, float* __restrict__ V, float tol, float amin,
+                  int max_sweeps, int* __restrict__ sweeps_out) {
   __shared__ int rotated;
   const int np = n + (n & 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -121,7 +123,7 @@ k_jacobi32_onecta(float* __restrict__ W, int64_t m, int n, float* __restrict__ V
           g = fmaf(x, y, g);
         }
         a = warp_sumf(a); b = warp_sumf(b); g = warp_sumf(g);
-        if (a == 0.f || b == 0.f || fabsf(g) <= tol * sqrtf(a) * sqrtf(b)) continue;
+        if (a <= amin || b <= amin || fabsf(g) <= tol * sqrtf(a) * sqrtf(b)) continue;
         const float zeta = (b - a) / (2.f * g);
         const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
         const float c = 1.f / sqrtf(1.f + t * t), s = c * t;
@@ -279,29 +281,46 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
   int* hp = (int*)h->pinned;
   int sweeps = 0;
   const float tol32 = 1e-5f;
-  if (n <= 512) {
-    k_jacobi32_onecta<<<1, 1024, 0, h->stream>>>(W32, mm, n, V32, tol32, 30, flag);
+  // Columns whose norm is below 1e-7 |A|_F are FP32 rounding noise (and their
+  // squared norms underflow for graded inputs such as R^T); rotations that
+  // involve them are skipped, otherwise the sweeps never settle.  Their
+  // directions are resolved (as far as FP64 resolves them) by the refinement.
+  double fro = 0.0;
+  {
+    // partial sums in the workspace tail (the handle's scratch holds the caller's buffers)
+    const int64_t sq = nn * nn;
+    double* red = ws + 5 * sq + ((mm * nn > sq) ? mm * nn : sq) + 64;
+    ITG_TRY(itg::nrm2_dev(h, mm * nn, Awork, red + 520, red));
+    ITG_CUDA(h, cudaMemcpyAsync(h->pinned, red + 520, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    fro = h->pinned[0];
+  }
+  const float amin = (float)(1e-14 * fro * fro);
+  if (n <= ONECTA32_MAX_N) {
+    k_jacobi32_onecta<<<1, 1024, 0, h->stream>>>(W32, mm, n, V32, tol32, amin, 30, flag);
     ITG_CHECK_LAUNCH(h);
     ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     ITG_CUDA(h, cudaStreamSynchronize(h->stream));
     sweeps = hp[0];
   } else {
-    const int st = itg::jacobi_persistent<float>(h, W32, mm, n, V32, tol32, 30, flag, &sweeps);
+    int st = ITG_ERR_UNSUPPORTED;
+    if (h->jacobi_mode == 2)
+      st = itg::jacobi_persistent<float>(h, W32, mm, n, V32, tol32, amin, 30, flag, &sweeps);
     if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED && st != ITG_ERR_UNSUPPORTED) return st;
-    if (st == ITG_ERR_UNSUPPORTED) sweeps = 0;
-  }
-  if (n > 512 && sweeps == 0) {
-    // per-step launches (devices without cooperative launch)
-    for (; sweeps < 30; ++sweeps) {
-      ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
-      for (int step = 0; step < np - 1; ++step)
-        k_jacobi32_step<<<np / 2, 256, 0, h->stream>>>(W32, mm, n, V32, tol32, step, flag);
-      ITG_CHECK_LAUNCH(h);
-      ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-      ITG_CUDA(h, cudaStreamSynchronize(h->stream));
-      if (hp[0] == 0) break;
+    if (st == ITG_ERR_UNSUPPORTED) {
+      // one launch per round-robin step (queued back to back)
+      sweeps = 0;
+      for (; sweeps < 30; ++sweeps) {
+        ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+        for (int step = 0; step < np - 1; ++step)
+          k_jacobi32_step<<<np / 2, 256, 0, h->stream>>>(W32, mm, n, V32, tol32, amin, step, flag);
+        ITG_CHECK_LAUNCH(h);
+        ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+        if (hp[0] == 0) break;
+      }
+      sweeps++;
     }
-    sweeps++;
   }
   *sweeps_out = sweeps;
   // 2. refinement of X on G = A^T A
@@ -362,7 +381,9 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
   // 3. U = A X diag(1/sigma), one Newton-Schulz step
   ITG_TRY(gemm(h, false, mm, nn, nn, 1.0, Awork, X, 0.0, Uw, precision));
   double* inv = E;  // E is free after the refinement
-  k_inv_sigma<<<itg_blocks_for(nn, 256, 64), 256, 0, h->stream>>>(lam, n, 1e-14 * smax, inv);
+  // columns with sigma < 1e-7 sigma_max are not resolved (A X / sigma is noise
+  // there); they are left zero so that they cannot pollute the Newton-Schulz step
+  k_inv_sigma<<<itg_blocks_for(nn, 256, 64), 256, 0, h->stream>>>(lam, n, 1e-7 * smax, inv);
   k_scale_cols<<<itg_blocks_for(mm * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(Uw, mm, n, inv);
   ITG_CHECK_LAUNCH(h);
   ITG_TRY(gemm(h, true, nn, nn, mm, 1.0, Uw, Uw, 0.0, P, precision));  // P = U^T U
@@ -378,7 +399,7 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
 size_t svd_mixed_ws_doubles(int64_t mm, int64_t nn) {
   const int64_t sq = nn * nn;
   const int64_t s_slot = (mm * nn > sq) ? mm * nn : sq;
-  return (size_t)(5 * sq + s_slot + 64);
+  return (size_t)(5 * sq + s_slot + 64 + 528);
 }
 
 }  // namespace itg

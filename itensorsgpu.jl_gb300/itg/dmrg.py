@@ -83,6 +83,10 @@ class SweepRecord:
     maxtruncerr: float
     seconds: float
     matvecs: int
+    # seconds per phase (eigensolver, factorisation, environment update, the
+    # rest); phases are separated by stream synchronisations only when
+    # dmrg(..., phase_timing=True)
+    phases: dict = field(default_factory=dict)
 
 
 @dataclass
@@ -190,7 +194,7 @@ def _orthogonalize_left_end(h, ch: _Chain):
 
 def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int = 2,
          eigsolve_tol: float = 1e-14, precision: str | int = "fp64", legacy_gpu_truncate: bool = False,
-         svd_method: int = 0, preconditioner=None, bond_hook=None,
+         svd_method: int = 0, preconditioner=None, bond_hook=None, phase_timing: bool = False,
          outputlevel: int = 0, return_result: bool = False):
     """Ground state by two-site DMRG.  Returns (energy, psi) like ITensors' dmrg.
 
@@ -237,7 +241,18 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
         maxdim, mindim, cutoff = sweeps.maxdim(sw), sweeps.mindim(sw), sweeps.cutoff(sw)
         maxerr = 0.0
         nmv_tot = 0
+        ph = dict(eig=0.0, svd=0.0, env=0.0)
+
+        def tick(key, t):
+            if phase_timing:
+                h.call("itg_synchronize")
+                now = time.perf_counter()
+                ph[key] += now - t
+                return now
+            return t
+
         for b, ha in sweepnext(N):
+            tp = tick("env", time.perf_counter()) if phase_timing else 0.0
             a, d1, _ = ch.Ad[b]
             _, d2, c = ch.Ad[b + 1]
             k_old = ch.Ad[b][2]
@@ -271,46 +286,50 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
                 fallbacks_total += fb.value
             energy = e.value
             nmv_tot += nmv.value
-            # SVD of phi as (a d1) x (d2 c)
+            tp = tick("eig", tp)
+            # bond split of phi as (a d1) x (d2 c): one orthonormal factor
+            # (left-moving half: A_b; right-moving: A_{b+1}), the other one
+            # carries S (itg_factorize_trunc)
             m, n = a * d1, d2 * c
             r = min(m, n)
-            U = T.empty_dev(m * r)
+            Lb = T.empty_dev(max(m, n) * r)
             S = T.empty_dev(r)
-            V = T.empty_dev(n * r)
+            Cb = T.empty_dev(max(m, n) * r)
             k = C.c_int64()
             te = C.c_double()
             dc = C.c_double()
             try:
-                h.call("itg_svd_trunc_ex", C.c_int64(m), C.c_int64(n), _ptr(phi), C.c_int64(m),
+                h.call("itg_factorize_trunc", C.c_int64(m), C.c_int64(n), _ptr(phi), C.c_int64(m),
                        C.c_int64(maxdim), C.c_int64(mindim), C.c_double(cutoff), 0, 1,
-                       int(legacy_gpu_truncate), _ptr(U), _ptr(S), _ptr(V), C.byref(k), C.byref(te),
-                       C.byref(dc), int(svd_method), int(precision))
+                       int(legacy_gpu_truncate), 0 if ha == 1 else 1, int(svd_method), int(precision),
+                       _ptr(Lb), _ptr(S), _ptr(Cb), C.byref(k), C.byref(te), C.byref(dc))
             except NotConverged:
                 pass  # factors are still returned; the rotation limit is generous
+            tp = tick("svd", tp)
             kk = int(k.value)
             maxerr = max(maxerr, te.value)
-            Uk = U[: m * kk]
-            Vk = V[: n * kk]
-            Sk = S[:kk]
-            schmidt[b + 1] = Sk.clone()
+            schmidt[b + 1] = S[:kk].clone()
             if ha == 1:
-                ch.A[b] = Uk.clone()
+                # A_b = L[(a d1), k]; A_{b+1}[k, d2, c] = (S V^T)[k, (d2 c)]
+                ch.A[b] = Lb[: m * kk].clone()
                 ch.Ad[b] = (a, d1, kk)
-                # A_{b+1}[k, d2, c] = S[k] V[(d2 c), k]
-                ch.A[b + 1] = _diag_raw(h, Sk, (kk, kk), [1, 2], Vk, (d2, c, kk), [3, 4, 1],
-                                        (kk, d2, c), [2, 3, 4])
+                ch.A[b + 1] = Cb[: kk * n].clone()
                 ch.Ad[b + 1] = (kk, d2, c)
                 Lenv[b + 1] = _env_left(h, Lt, Ld, ch.A[b], ch.Ad[b], W1, W1d, precision)
             else:
-                # A_b[a, d1, k] = U[(a d1), k] S[k];  A_{b+1} = V^T
-                ch.A[b] = _diag_raw(h, Sk, (kk, kk), [1, 2], Uk, (a, d1, kk), [3, 4, 1],
-                                    (a, d1, kk), [3, 4, 2])
+                # A_b[a, d1, k] = (U S)[(a d1), k];  A_{b+1} = V^T, V = L[(d2 c), k]
+                ch.A[b] = Cb[: m * kk].clone()
                 ch.Ad[b] = (a, d1, kk)
-                ch.A[b + 1] = _permute_raw(h, Vk, (d2, c, kk), [1, 2, 3], [3, 1, 2])
+                ch.A[b + 1] = _permute_raw(h, Lb[: n * kk], (d2, c, kk), [1, 2, 3], [3, 1, 2])
                 ch.Ad[b + 1] = (kk, d2, c)
                 Renv[b + 1] = _env_right(h, Rt, Rd, ch.A[b + 1], ch.Ad[b + 1], W2, W2d, precision)
+            tick("env", tp)
         h.call("itg_synchronize")
-        rec = SweepRecord(energy, max(x[2] for x in ch.Ad[:-1]), maxerr, time.perf_counter() - t0, nmv_tot)
+        secs = time.perf_counter() - t0
+        if phase_timing:
+            ph["other"] = max(0.0, secs - ph["eig"] - ph["svd"] - ph["env"])
+        rec = SweepRecord(energy, max(x[2] for x in ch.Ad[:-1]), maxerr, secs, nmv_tot,
+                          ph if phase_timing else {})
         records.append(rec)
         if outputlevel > 0:
             print(f"After sweep {sw + 1} energy={energy:.14f} maxlinkdim={rec.maxlinkdim} "

@@ -48,6 +48,12 @@ def get_precision() -> int:
     return _state["precision"]
 
 
+def _precision_code(p: str | int) -> int:
+    if isinstance(p, str):
+        return {"fp64": PREC_FP64, "split": PREC_SPLIT}[p.lower()]
+    return int(p)
+
+
 def _h():
     return _lib.handle(_state["device"])
 
@@ -490,6 +496,54 @@ def svd(A: ITensor, *left_inds, **kw):
     Vt = ITensor(Dense(V[: n * kk].clone()), (*right, v))
     P = (S[:kk] ** 2).detach().cpu().numpy()
     return Ut, St, Vt, Spectrum(P, te.value)
+
+
+def factorize(A: ITensor, *left_inds, ortho: str = "left", **kw):
+    """L, R with A ~ L * R and one orthonormal factor (ITensors' factorize with
+    which_decomp = "svd"; the two-site bond split of dmrg).
+
+    ortho="left": L (left_inds..., l) has orthonormal columns, R = S V^T.
+    ortho="right": R (l, right inds...) has orthonormal rows, L = U S.
+    Keywords as svd, plus method (0 auto, 1 FP64 Jacobi, 2 mixed) and
+    precision ("fp64" / "split") of the products.  Returns (L, R, spec).
+    """
+    _require_cuda(A)
+    if len(left_inds) == 1 and isinstance(left_inds[0], (list, tuple)):
+        left_inds = tuple(left_inds[0])
+    left = [i for i in A.inds if i in left_inds]
+    if len(left) != len(left_inds):
+        raise DimensionMismatch(2, "factorize: left index not in tensor")
+    right = [i for i in A.inds if i not in left_inds]
+    Am = permute(A, *left, *right) if A.isdiag() or tuple(left + right) != A.inds else A
+    if Am.isdiag():
+        Am = dense(Am)
+    if ortho not in ("left", "right"):
+        raise ValueError("factorize: ortho must be 'left' or 'right'")
+    m, n = dim(left), dim(right)
+    r = min(m, n)
+    big = max(m, n) * r
+    Lb = empty_dev(big)
+    S = empty_dev(r)
+    Cb = empty_dev(big)
+    k = C.c_int64()
+    te = C.c_double()
+    dc = C.c_double()
+    maxdim, mindim, cutoff, ab, rel, legacy = _trunc_args(m, n, kw)
+    prec = _precision_code(kw.get("precision", get_precision()))
+    _h().call("itg_factorize_trunc", C.c_int64(m), C.c_int64(n), _ptr(Am.store.data), C.c_int64(m),
+              C.c_int64(maxdim), C.c_int64(mindim), C.c_double(cutoff), ab, rel, legacy,
+              0 if ortho == "left" else 1, int(kw.get("method", 0)), prec,
+              _ptr(Lb), _ptr(S), _ptr(Cb), C.byref(k), C.byref(te), C.byref(dc))
+    kk = int(k.value)
+    l = Index(kk, kw.get("tags", "Link,fac"))
+    if ortho == "left":
+        Lt = ITensor(Dense(Lb[: m * kk].clone()), (*left, l))
+        Rt = ITensor(Dense(Cb[: kk * n].clone()), (l, *right))
+    else:
+        Lt = ITensor(Dense(Cb[: m * kk].clone()), (*left, l))
+        Rt = ITensor(Dense(Lb[: n * kk].clone()), (*right, l))
+    P = (S[:kk] ** 2).detach().cpu().numpy()
+    return Lt, Rt, Spectrum(P, te.value)
 
 
 def eigen(A: ITensor, left_inds, right_inds, **kw):

@@ -162,7 +162,8 @@ def test_svd_mixed_haar_exp_spectrum(gpu, n, prec):
     # the kept factorisation reproduces the matrix to ~sqrt(cutoff) of sigma_max
     assert np.abs((Uh * Sh) @ Vh.T - M).max() < 2e-6 * So[0]
     assert np.abs((Ub * Sh[big]) @ Vb.T - (Uo[:, big] * So[big]) @ Vo[:, big].T).max() < 1e-10 * So[0]
-    assert te.value == pytest.approx(teo, rel=1e-6, abs=1e-20)
+    # truncerr sums the discarded P values, each accurate to ~eps * P_max
+    assert abs(te.value - teo) < 1e-13 * So[0] ** 2
 
 
 def test_qr(gpu):
@@ -205,3 +206,100 @@ def test_eigen_hermitian(gpu):
     D, U, spec = gpu.eigen(gpu.cuITensor(S, i, ip), [i], [ip], maxdim=20)
     wref = np.linalg.eigvalsh(S)[::-1]
     assert np.abs(D.store.data.cpu().numpy() - wref[:20]).max() < 1e-11 * np.abs(wref).max()
+
+
+@pytest.mark.parametrize("method", [1, 2])
+def test_svd_qr_preconditioning_and_jacobi_modes(gpu, method):
+    """The QR-preconditioned Jacobi (default) and the plain one, with one
+    launch per step (default) or all sweeps in one cooperative launch, give the same
+    factorisation (singular values to 1e-13 sigma_max for the FP64 method;
+    the mixed method to its P accuracy), and preconditioning cuts the sweeps
+    on a graded spectrum."""
+    from itg import _lib
+    import torch
+    n, m = 300, 340
+    rng = np.random.default_rng(77)
+    Q1, _ = np.linalg.qr(rng.standard_normal((m, n)))
+    Q2, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.exp(-np.arange(n) / 20.0)
+    M = (Q1 * s) @ Q2.T
+    h = _lib.handle(0)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    A = torch.from_numpy(O.flat(M).copy()).cuda()
+    res = {}
+    try:
+        for pre, mode in ((1, 0), (0, 0), (1, 2), (0, 2)):
+            h.call("itg_set_svd_options", pre, mode)
+            U = torch.empty(m * n, dtype=torch.float64, device="cuda")
+            S = torch.empty(n, dtype=torch.float64, device="cuda")
+            V = torch.empty(n * n, dtype=torch.float64, device="cuda")
+            k, te, dc = C.c_int64(), C.c_double(), C.c_double()
+            h.call("itg_svd_trunc_ex", C.c_int64(m), C.c_int64(n), p(A), C.c_int64(m), C.c_int64(0), C.c_int64(1),
+                   C.c_double(1e-12), 0, 1, 0, p(U), p(S), p(V), C.byref(k), C.byref(te), C.byref(dc), method, 0)
+            sw = C.c_int()
+            h.call("itg_svd_info", C.byref(sw))
+            kk = k.value
+            res[(pre, mode)] = (kk, S.cpu().numpy()[:kk], O.unflat(U.cpu().numpy()[: m * kk], (m, kk)),
+                                O.unflat(V.cpu().numpy()[: n * kk], (n, kk)), sw.value)
+    finally:
+        h.call("itg_set_svd_options", 1, 0)
+    kk0 = res[(1, 0)][0]
+    for key, (kk, Sh, Uh, Vh, sw) in res.items():
+        assert kk == kk0, key
+        big = s[:kk] > 1e-4
+        tol = 1e-13 if method == 1 else 1e-12
+        assert np.abs(Sh[big] - s[:kk][big]).max() < tol, key
+        assert np.abs(Uh.T @ Uh - np.eye(kk)).max() < 1e-12, key
+        assert np.abs(Vh.T @ Vh - np.eye(kk)).max() < 1e-12, key
+        assert np.abs((Uh * Sh) @ Vh.T - M).max() < 2e-6, key
+    # fewer sweeps with the preconditioner
+    assert res[(1, 0)][4] < res[(0, 0)][4], (res[(1, 0)][4], res[(0, 0)][4])
+
+
+@pytest.mark.parametrize("m,n", [(300, 300), (400, 260), (260, 400), (90, 70)])
+@pytest.mark.parametrize("method,prec", [(1, 0), (2, 0), (2, 1)])
+@pytest.mark.parametrize("ortho", [0, 1])
+def test_factorize_trunc(gpu, m, n, method, prec, ortho):
+    """itg_factorize_trunc: the orthonormal factor is orthonormal to 1e-13 for
+    every kept column (also for singular values far below sqrt(eps) sigma_max),
+    the product reproduces the oracle's truncated SVD, and k / S / truncerr
+    follow the ITensors truncation of the oracle's spectrum."""
+    from itg import _lib
+    import torch
+    rng = np.random.default_rng(m * 7 + n + method + 10 * prec + 100 * ortho)
+    r = min(m, n)
+    Q1, _ = np.linalg.qr(rng.standard_normal((m, r)))
+    Q2, _ = np.linalg.qr(rng.standard_normal((n, r)))
+    s = np.exp(-np.arange(r) / 12.0)  # down to ~1e-11 at r = 300
+    M = (Q1 * s) @ Q2.T
+    h = _lib.handle(0)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    A = torch.from_numpy(O.flat(M).copy()).cuda()
+    big = max(m, n) * r
+    L = torch.empty(big, dtype=torch.float64, device="cuda")
+    S = torch.empty(r, dtype=torch.float64, device="cuda")
+    Cm = torch.empty(big, dtype=torch.float64, device="cuda")
+    k, te, dc = C.c_int64(), C.c_double(), C.c_double()
+    # FP64 Jacobi: keep sigma down to ~1e-9 sigma_max; mixed: down to ~1e-6
+    # (its singular vectors are resolved above ~1e-7 sigma_max)
+    cutoff = 1e-18 if method == 1 else 1e-12
+    h.call("itg_factorize_trunc", C.c_int64(m), C.c_int64(n), p(A), C.c_int64(m), C.c_int64(0), C.c_int64(1),
+           C.c_double(cutoff), 0, 1, 0, ortho, method, prec, p(L), p(S), p(Cm), C.byref(k), C.byref(te),
+           C.byref(dc))
+    kk = k.value
+    Uo, So, Vo, teo, _ = O.svd_trunc(M, cutoff=cutoff)
+    assert kk == len(So)
+    Sh = S.cpu().numpy()[:kk]
+    assert np.abs(Sh ** 2 - So ** 2).max() < 3e-14 * So[0] ** 2
+    if ortho == 0:
+        Lh = O.unflat(L.cpu().numpy()[: m * kk], (m, kk))
+        Ch = O.unflat(Cm.cpu().numpy()[: kk * n], (kk, n))
+        prod = Lh @ Ch
+    else:
+        Lh = O.unflat(L.cpu().numpy()[: n * kk], (n, kk))
+        Ch = O.unflat(Cm.cpu().numpy()[: m * kk], (m, kk))
+        prod = Ch @ Lh.T
+    assert np.abs(Lh.T @ Lh - np.eye(kk)).max() < 1e-13
+    ref = (Uo * So) @ Vo.T
+    assert np.abs(prod - ref).max() < (1e-12 if method == 1 else 1e-11) * So[0]
+    assert abs(te.value - teo) < 1e-13 * So[0] ** 2
