@@ -245,12 +245,14 @@ ITG_API int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* A, 
 /* itg_svd_trunc with an explicit method and GEMM precision.
  *  ITG_SVD_JACOBI: one-sided FP64 Jacobi (every rotation in FP64).
  *  ITG_SVD_MIXED : FP32 one-sided Jacobi, then FP64-accurate refinement of the
- *                  right singular vectors as eigenvectors of A^T A (matrix
- *                  products through the contraction engine at `precision`),
- *                  U = A V / sigma and one Newton-Schulz orthonormalisation.
- *                  P = sigma^2 to ~eps * P_max absolute (sigma_j to
- *                  ~eps * sigma_max^2 / sigma_j): exact for truncation, and
- *                  full accuracy for sigma_j above ~1e-4 sigma_max.
+ *                  singular vectors as eigenvectors of the Gram matrix
+ *                  (matrix products through the contraction engine at
+ *                  `precision`) and Newton-Schulz orthonormalisation.
+ *                  P = sigma^2 to ~1e-13 P_max absolute; singular values and
+ *                  vectors at FP64 accuracy above ~1e-4 sigma_max.  With QR
+ *                  preconditioning (min(m,n) > 192) U is orthonormal for every
+ *                  kept column and V only where sigma is resolved; use
+ *                  itg_factorize_trunc when one factor must be orthonormal.
  *  ITG_SVD_AUTO  : Jacobi for min(m, n) <= 192, mixed above.
  * itg_svd_trunc always uses ITG_SVD_JACOBI (LAPACK-level accuracy). */
 enum { ITG_SVD_AUTO = 0, ITG_SVD_JACOBI = 1, ITG_SVD_MIXED = 2 };
@@ -278,16 +280,20 @@ ITG_API int itg_factorize_trunc(itg_handle* h, int64_t m, int64_t n, const doubl
                                 int doRelCutoff, int legacy_gpu, int ortho, int method, int precision,
                                 double* L, double* S, double* C, int64_t* k, double* truncerr,
                                 double* docut);
-/* Jacobi sweeps run by the last itg_svd_trunc / itg_svd_trunc_ex / itg_eigh_trunc
- * call on this handle (FP32 sweeps for the mixed method). */
-ITG_API int itg_svd_info(itg_handle* h, int* sweeps);
+/* Diagnostics of the last itg_svd_trunc / itg_svd_trunc_ex / itg_factorize_trunc /
+ * itg_eigh_trunc call on this handle: Jacobi sweeps (FP32 sweeps for the mixed
+ * method), whether the mixed method finished it (0: FP64 Jacobi), and the
+ * handle's count of mixed SVDs whose refinement check failed and that were
+ * redone with FP64 Jacobi.  Any pointer may be NULL. */
+ITG_API int itg_svd_info(itg_handle* h, int* sweeps, int* mixed_used, int64_t* mixed_fallbacks);
 /* SVD options of this handle.  qr_precondition = 1 (default): for
  * min(m, n) > 192 the working matrix is first factored A = Q R by Householder
  * reflections and the Jacobi iteration runs on R^T (far fewer sweeps on
  * graded spectra; A = (Q V_B) S U_B^T from R^T = U_B S V_B^T).  jacobi_mode:
- * 0 (default) or 1: one launch per round-robin step (queued back to back);
- * 2: all sweeps in one cooperative launch with a grid barrier between steps
- * (measured slower on GB300; kept for comparison). */
+ * 0 (default): block-cyclic Jacobi, block pairs staged in shared memory,
+ * one launch per block step; 1: one CTA per column pair, one launch per
+ * round-robin step; 2: element pairs with all sweeps in one cooperative
+ * launch and a grid barrier between steps (measured slower than 1 on GB300). */
 ITG_API int itg_set_svd_options(itg_handle* h, int qr_precondition, int jacobi_mode);
 
 /* Eigendecomposition of the symmetric n x n matrix A: A = U diag(D) U^T with D

@@ -500,7 +500,11 @@ int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* f
     *sweeps_done = hp[0];
     return hp[0] >= JACOBI_MAX_SWEEPS ? ITG_ERR_NOTCONVERGED : ITG_OK;
   }
-  if (h->jacobi_mode == 2) {
+  if (h->jacobi_mode == 0) {
+    const int st = itg::jacobi_blocked<double>(h, W, m, (int)n, V, tol, 0.0, JACOBI_MAX_SWEEPS, flag_dev,
+                                               sweeps_done);
+    if (st != ITG_ERR_UNSUPPORTED) return st;
+  } else if (h->jacobi_mode == 2) {
     const int st = itg::jacobi_persistent<double>(h, W, m, (int)n, V, tol, 0.0, JACOBI_MAX_SWEEPS, flag_dev,
                                                   sweeps_done);
     if (st != ITG_ERR_UNSUPPORTED) return st;
@@ -690,11 +694,22 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
   const int64_t ld_r = !pre ? nn : (two ? nn : mm);
   if (pre) ITG_CUDA(h, cudaMemsetAsync(Uw_dst, 0, sizeof(double) * mm * nn, h->stream));
   dim3 g1(itg_blocks_for(mj, 256, 64), (unsigned)nn), g2(itg_blocks_for(nn, 256, 64), (unsigned)nn);
+  bool use_mixed = mixed;
   if (mixed) {
     double* lam = (double*)(base + oLam);
     double* Uw = (double*)(base + oUw);
-    ITG_TRY(itg::svd_mixed_core(h, J, mj, nn, precision, Vw, lam, Uw, (double*)(base + oWs),
-                                (float*)(base + oWs32), flag, &sweeps));
+    const int ms = itg::svd_mixed_core(h, J, mj, nn, precision, Vw, lam, Uw, (double*)(base + oWs),
+                                       (float*)(base + oWs32), flag, &sweeps);
+    if (ms == ITG_ERR_NOTCONVERGED) {
+      use_mixed = false;  // refinement failed its check: FP64 Jacobi on the same J
+      h->svd_fallbacks++;
+    } else if (ms != ITG_OK) {
+      return ms;
+    }
+  }
+  if (use_mixed) {
+    double* lam = (double*)(base + oLam);
+    double* Uw = (double*)(base + oUw);
     k_sqrt_clamp<<<itg_blocks_for(nn, 256, 64), 256, 0, h->stream>>>(lam, (int)nn, sig);
     k_rank_desc<<<itg_blocks_for(nn, 256, 1024), 256, 0, h->stream>>>(sig, (int)nn, 0.0, order, S, P, 1);
     ITG_CHECK_LAUNCH(h);
@@ -716,6 +731,7 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
     ITG_CHECK_LAUNCH(h);
   }
   h->last_sweeps = sweeps;
+  h->last_mixed = use_mixed;
   ITG_TRY(read_out3(h, out3, k, truncerr, docut));
   if (pre) {
     // rotate the kept columns back
@@ -917,9 +933,11 @@ extern "C" int itg_qr(itg_handle* h, int64_t m, int64_t n, const double* A, int6
   return ITG_OK;
 }
 
-extern "C" int itg_svd_info(itg_handle* h, int* sweeps) {
-  if (!h || !sweeps) return ITG_ERR_INVALID;
-  *sweeps = h->last_sweeps;
+extern "C" int itg_svd_info(itg_handle* h, int* sweeps, int* mixed_used, int64_t* mixed_fallbacks) {
+  if (!h) return ITG_ERR_INVALID;
+  if (sweeps) *sweeps = h->last_sweeps;
+  if (mixed_used) *mixed_used = h->last_mixed ? 1 : 0;
+  if (mixed_fallbacks) *mixed_fallbacks = h->svd_fallbacks;
   return ITG_OK;
 }
 

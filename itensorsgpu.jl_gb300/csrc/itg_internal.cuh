@@ -77,8 +77,10 @@ struct itg_handle {
   size_t tune_buf_bytes = 0;
   int64_t tune_runs = 0;
   int last_sweeps = 0;        // Jacobi sweeps of the last SVD / eigh call
+  bool last_mixed = false;    // the last SVD finished on the mixed method
+  int64_t svd_fallbacks = 0;  // mixed SVDs redone with FP64 Jacobi
   bool svd_qr_precond = true; // itg_set_svd_options
-  int jacobi_mode = 0;        // 0 / 1: one launch per step, 2: one cooperative launch
+  int jacobi_mode = 0;        // 0 blocked, 1 element pairs per step, 2 one cooperative launch
 };
 
 // Record a timing event pair around a launch when profiling is on.
@@ -97,6 +99,11 @@ int jacobi_aux_ints(int max_sweeps);
 template <class T>
 int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* aux,
                       int* sweeps);
+// Blocked one-sided Jacobi (itg_jacobi.cu): block pairs staged in shared
+// memory, one launch per block step; ITG_ERR_UNSUPPORTED when m is too large.
+template <class T>
+int jacobi_blocked(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* flag,
+                   int* sweeps);
 }  // namespace itg
 
 // Error helpers ---------------------------------------------------------------

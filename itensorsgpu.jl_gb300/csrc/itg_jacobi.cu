@@ -204,6 +204,142 @@ k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, 
   if (blockIdx.x == 0 && threadIdx.x == 0) aux[3] = done;
 }
 
+// ------------------------------------------------------ blocked step
+// Block-cyclic one-sided Jacobi: the columns form blocks of WB; step `step`
+// of a sweep pairs the blocks round robin (nbp slots), one CTA per block
+// pair.  The CTA stages the pair's 2 WB columns in shared memory, rotates
+// every cross pair (i in block I, j in block J; WB rounds of WB disjoint
+// pairs), accumulates the rotations into a 2WB x 2WB matrix Q, writes the
+// columns back and applies Q to the pair's columns of V.  The first step of
+// a sweep also rotates the pairs inside each block (a full round robin over
+// the 2 WB columns), so every column pair is visited once per sweep.  Same
+// rotation formula and skip rule as the element-wise kernels; a step moves
+// 2 WB columns per CTA through shared memory instead of two per CTA.
+constexpr int JB_THREADS = 512;
+
+template <class T, int WB>
+__global__ void __launch_bounds__(JB_THREADS)
+k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T amin, int step,
+                    int first, int* __restrict__ rotated) {
+  constexpr int C2 = 2 * WB;              // local columns
+  constexpr int TP = JB_THREADS / WB;     // threads per pair
+  constexpr int WPG = TP / 32;            // warps per pair group
+  extern __shared__ __align__(16) unsigned char jb_smem[];
+  T* cols = (T*)jb_smem;                  // [C2][m]
+  T* Q = cols + (int64_t)C2 * m;          // [C2][C2], column-major
+  T* red = Q + C2 * C2;                   // [WB][WPG][3]
+  __shared__ int any;
+  const int nb = (n + WB - 1) / WB, nbp = nb + (nb & 1);
+  const int bi = jp_player(blockIdx.x, step, nbp), bj = jp_player(nbp - 1 - blockIdx.x, step, nbp);
+  const int t = threadIdx.x;
+  auto gcol = [&](int c) -> int {  // global column of local c, or -1
+    const int blk = c < WB ? bi : bj;
+    const int gc = blk * WB + (c < WB ? c : c - WB);
+    return (blk < nb && gc < n) ? gc : -1;
+  };
+  if (t == 0) any = 0;
+  for (int c = 0; c < C2; ++c) {
+    const int gc = gcol(c);
+    T* dst = cols + (int64_t)c * m;
+    if (gc >= 0) {
+      const T* src = W + (int64_t)gc * m;
+      for (int64_t i = t; i < m; i += JB_THREADS) dst[i] = src[i];
+    } else {
+      for (int64_t i = t; i < m; i += JB_THREADS) dst[i] = T(0);
+    }
+  }
+  for (int i = t; i < C2 * C2; i += JB_THREADS) Q[i] = (i % (C2 + 1) == 0) ? T(1) : T(0);
+  __syncthreads();
+  const int g = t / TP, lt = t % TP, wg = lt / 32, lane = t & 31;
+  const int rounds = first ? C2 - 1 : WB;
+  for (int r = 0; r < rounds; ++r) {
+    int p, q;
+    if (first) {
+      p = jp_player(g, r, C2);
+      q = jp_player(C2 - 1 - g, r, C2);
+    } else {
+      p = g;
+      q = WB + (g + r) % WB;
+    }
+    if (p > q) {
+      const int tmp = p;
+      p = q;
+      q = tmp;
+    }
+    T* xp = cols + (int64_t)p * m;
+    T* xq = cols + (int64_t)q * m;
+    T a = 0, b = 0, gg = 0;
+    for (int64_t i = lt; i < m; i += TP) {
+      const T x = xp[i], y = xq[i];
+      a = fma(x, x, a);
+      b = fma(y, y, b);
+      gg = fma(x, y, gg);
+    }
+    a = jp_warp_sum(a);
+    b = jp_warp_sum(b);
+    gg = jp_warp_sum(gg);
+    if (lane == 0) {
+      red[(g * WPG + wg) * 3 + 0] = a;
+      red[(g * WPG + wg) * 3 + 1] = b;
+      red[(g * WPG + wg) * 3 + 2] = gg;
+    }
+    __syncthreads();
+    a = 0;
+    b = 0;
+    gg = 0;
+#pragma unroll
+    for (int w = 0; w < WPG; ++w) {
+      a += red[(g * WPG + w) * 3 + 0];
+      b += red[(g * WPG + w) * 3 + 1];
+      gg += red[(g * WPG + w) * 3 + 2];
+    }
+    const bool rot = !(a <= amin || b <= amin || fabs(gg) <= tol * sqrt(a) * sqrt(b));
+    if (rot) {
+      const T zeta = (b - a) / (T(2) * gg);
+      const T tt = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+      const T c = T(1) / sqrt(T(1) + tt * tt), sn = c * tt;
+      for (int64_t i = lt; i < m; i += TP) {
+        const T x = xp[i], y = xq[i];
+        xp[i] = c * x - sn * y;
+        xq[i] = sn * x + c * y;
+      }
+      if (lt < C2) {
+        const T x = Q[lt + p * C2], y = Q[lt + q * C2];
+        Q[lt + p * C2] = c * x - sn * y;
+        Q[lt + q * C2] = sn * x + c * y;
+      }
+      if (lt == 0) any = 1;
+    }
+    __syncthreads();  // columns, Q and red are reused by the next round
+  }
+  if (!any) return;  // block-uniform (read after the last barrier)
+  for (int c = 0; c < C2; ++c) {
+    const int gc = gcol(c);
+    if (gc < 0) continue;
+    const T* src = cols + (int64_t)c * m;
+    T* dst = W + (int64_t)gc * m;
+    for (int64_t i = t; i < m; i += JB_THREADS) dst[i] = src[i];
+  }
+  // V[:, cols] <- V[:, cols] Q, one row per thread
+  int gcs[C2];
+#pragma unroll
+  for (int c = 0; c < C2; ++c) gcs[c] = gcol(c);
+  for (int row = t; row < n; row += JB_THREADS) {
+    T v[C2];
+#pragma unroll
+    for (int c = 0; c < C2; ++c) v[c] = gcs[c] >= 0 ? V[row + (int64_t)gcs[c] * n] : T(0);
+#pragma unroll
+    for (int c = 0; c < C2; ++c) {
+      if (gcs[c] < 0) continue;
+      T s = 0;
+#pragma unroll
+      for (int d = 0; d < C2; ++d) s = fma(v[d], Q[d + c * C2], s);
+      V[row + (int64_t)gcs[c] * n] = s;
+    }
+  }
+  if (t == 0) *rotated = 1;
+}
+
 }  // namespace
 
 namespace itg {
@@ -252,6 +388,58 @@ int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin
   *sweeps = hp[3] > max_sweeps ? max_sweeps : hp[3];
   return hp[3] > max_sweeps ? ITG_ERR_NOTCONVERGED : ITG_OK;
 }
+
+template <class T, int WB>
+size_t jb_smem_bytes(int64_t m) {
+  return sizeof(T) * ((size_t)2 * WB * m + (size_t)4 * WB * WB + (size_t)WB * (JB_THREADS / WB / 32) * 3);
+}
+
+template <class T, int WB>
+int jb_run(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* flag, int* sweeps) {
+  const size_t smem = jb_smem_bytes<T, WB>(m);
+  static bool attr = false;
+  if (!attr) {
+    ITG_CUDA(h, cudaFuncSetAttribute(k_jacobi_block_step<T, WB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
+    attr = true;
+  }
+  const int nb = (n + WB - 1) / WB, nbp = nb + (nb & 1);
+  int* hp = (int*)h->pinned;
+  for (int sw = 0; sw < max_sweeps; ++sw) {
+    ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+    for (int step = 0; step < nbp - 1; ++step)
+      k_jacobi_block_step<T, WB><<<nbp / 2, JB_THREADS, smem, h->stream>>>(W, m, n, V, tol, amin, step,
+                                                                          step == 0, flag);
+    ITG_CHECK_LAUNCH(h);
+    ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hp[0] == 0) {
+      *sweeps = sw + 1;
+      return ITG_OK;
+    }
+  }
+  *sweeps = max_sweeps;
+  return ITG_ERR_NOTCONVERGED;
+}
+
+// Blocked Jacobi with the widest block whose column pair fits in 200 KB of
+// shared memory; ITG_ERR_UNSUPPORTED when not even 2 + 2 columns fit.
+template <class T>
+int jacobi_blocked(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* flag,
+                   int* sweeps) {
+  constexpr size_t LIM = 200 * 1024;
+  if (n < 2) {
+    *sweeps = 0;
+    return ITG_OK;
+  }
+  if (jb_smem_bytes<T, 8>(m) <= LIM && n >= 64) return jb_run<T, 8>(h, W, m, n, V, tol, amin, max_sweeps, flag, sweeps);
+  if (jb_smem_bytes<T, 4>(m) <= LIM) return jb_run<T, 4>(h, W, m, n, V, tol, amin, max_sweeps, flag, sweeps);
+  if (jb_smem_bytes<T, 2>(m) <= LIM) return jb_run<T, 2>(h, W, m, n, V, tol, amin, max_sweeps, flag, sweeps);
+  return ITG_ERR_UNSUPPORTED;
+}
+
+template int jacobi_blocked<float>(itg_handle*, float*, int64_t, int, float*, float, float, int, int*, int*);
+template int jacobi_blocked<double>(itg_handle*, double*, int64_t, int, double*, double, double, int, int*, int*);
 
 template int jacobi_persistent<float>(itg_handle*, float*, int64_t, int, float*, float, float, int, int*, int*);
 template int jacobi_persistent<double>(itg_handle*, double*, int64_t, int, double*, double, double, int, int*,

@@ -5,8 +5,9 @@
 // the contraction engine (FP64 gather-GEMM, or the split-precision tensor-core
 // path, which is FP64-accurate):
 //
-//  1. W32 = float(A); one-sided Jacobi sweeps in FP32 (same round-robin pairs
-//     and rotation formula as the FP64 kernels) until |w_p.w_q| <= 1e-5 |w_p||w_q|.
+//  1. W32 = float(A); one-sided Jacobi sweeps in FP32 (same rotation formula as
+//     the FP64 kernels; block-cyclic in shared memory for large n) until
+//     |w_p.w_q| <= 1e-5 |w_p||w_q|, skipping columns below FP32 resolution.
 //  2. Refine X = double(V32) as eigenvectors of G = A^T A.  Per iteration
 //       R = I - X^T X,  S = X^T (G X),  l_i = s_ii / (1 - r_ii),
 //       e_ij = (s_ij + l_j r_ij) / (l_j - l_i)  (i != j, |l_j - l_i| > delta),
@@ -21,13 +22,16 @@
 //     Two Newton-Schulz steps then restore X's orthonormality to rounding.
 //  3. sigma_i = sqrt(max(l_i, 0)), U = A X diag(1/sigma), then one Newton-
 //     Schulz step U <- U + U (I - U^T U)/2 to restore orthonormality.
-// Accuracy: P = sigma^2 (what truncation uses) to ~eps * P_max absolute, so
-// sigma_j to ~eps * sigma_max^2 / sigma_j: full FP64 accuracy for the
-// singular values above ~1e-4 sigma_max, degrading below sqrt(eps) sigma_max.
-// DMRG keeps sigma_j^2 >= cutoff * sum(P) (sigma_j >= 1e-6 sigma_max at
-// cutoff 1e-12), where the error is <= 1e-10 sigma_max.  itg_svd_trunc keeps
-// the FP64 Jacobi path for callers that need LAPACK-level accuracy on tiny
-// singular values.
+// Accuracy (measured on U diag(exp(-k/20)) V^T, n = 300 ... 2048): P = sigma^2
+// (what truncation uses) to ~1e-13 P_max absolute, singular values and both
+// factors to FP64 accuracy above ~1e-4 sigma_max.  Below that the FP32 start
+// does not resolve the singular vectors well enough for the first-order
+// refinement, so they are accurate only to ~1e-13 P_max / (their P gap): a
+// value within ~1e-13 P_max of the truncation threshold may land on either
+// side.  X (V) stays orthonormal to rounding for every column; U = A X / S
+// only where S is resolved (itg_factorize_trunc never divides by S).
+// itg_svd_trunc keeps the FP64 Jacobi path for callers that need LAPACK-level
+// accuracy on tiny singular values.
 #include "itg_internal.cuh"
 
 #include <cmath>
@@ -199,8 +203,18 @@ __global__ void k_refine_E(const double* __restrict__ P, const double* __restric
     if (i == j) {
       e = 0.5 * rij;
     } else {
+      // A pair is resolved only when it is separated (gap > delta) and the
+      // first-order correction is small against the gap from both sides (the
+      // decision reads (i, j) and (j, i), so e_ij + e_ji = r_ij holds for
+      // every pair); otherwise it is treated as part of a cluster and only
+      // its orthogonality is restored.  This keeps a poor FP32 start (large
+      // mixing between close eigenvalues) from driving the iteration away.
+      const int64_t tt = (int64_t)j + (int64_t)i * n;
+      const double rji = -P[tt];
       const double d = lam[j] - lam[i];
-      e = (fabs(d) > delta) ? (S[t] + lam[j] * rij) / d : 0.5 * rij;
+      const double nij = S[t] + lam[j] * rij, nji = S[tt] + lam[i] * rji;
+      const bool ok = fabs(d) > delta && fabs(nij) <= 0.25 * fabs(d) && fabs(nji) <= 0.25 * fabs(d);
+      e = ok ? nij / d : 0.5 * rij;
     }
     E[t] = e;
   }
@@ -231,6 +245,30 @@ __global__ void k_scale_cols(double* __restrict__ U, int64_t m, int n, const dou
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x)
     U[t] *= inv[t / m];
+}
+
+// out = max |I - P| over the n x n matrix P (NaN propagates as failure)
+__global__ void k_max_offident(const double* __restrict__ P, int n, double* __restrict__ out) {
+  __shared__ double sh[32];
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  double mx = 0.0;
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x) {
+    const int j = (int)(t / n), i = (int)(t - (int64_t)j * n);
+    const double v = fabs((i == j ? 1.0 : 0.0) - P[t]);
+    if (!(v == v)) bad = 1;
+    mx = fmax(mx, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) b = fmax(b, sh[i]);
+    *out = bad ? __longlong_as_double(0x7ff8000000000000ll) : b;
+  }
 }
 
 __global__ void k_max_abs(const double* __restrict__ x, int n, double* __restrict__ out) {
@@ -304,7 +342,9 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
     sweeps = hp[0];
   } else {
     int st = ITG_ERR_UNSUPPORTED;
-    if (h->jacobi_mode == 2)
+    if (h->jacobi_mode == 0)
+      st = itg::jacobi_blocked<float>(h, W32, mm, n, V32, tol32, amin, 30, flag, &sweeps);
+    else if (h->jacobi_mode == 2)
       st = itg::jacobi_persistent<float>(h, W32, mm, n, V32, tol32, amin, 30, flag, &sweeps);
     if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED && st != ITG_ERR_UNSUPPORTED) return st;
     if (st == ITG_ERR_UNSUPPORTED) {
@@ -374,9 +414,15 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
   ITG_TRY(gemm(h, true, nn, nn, nn, 1.0, X, Q, 0.0, S, precision));
   k_refine_lambda<<<itg_blocks_for(nn, 256, 64), 256, 0, h->stream>>>(P, S, n, lam);
   k_max_abs<<<1, 1024, 0, h->stream>>>(lam, n, mx);
+  k_max_offident<<<1, 1024, 0, h->stream>>>(P, n, mx + 1);
   ITG_CHECK_LAUNCH(h);
-  ITG_CUDA(h, cudaMemcpyAsync(h->pinned, mx, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  ITG_CUDA(h, cudaMemcpyAsync(h->pinned, mx, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  // Safeguard: the first-order refinement needs a start close enough to the
+  // eigenvectors; when it was not (X not orthonormal to 1e-10 after the
+  // Newton-Schulz steps, or not finite) the caller redoes the problem with
+  // FP64 Jacobi.
+  if (!(h->pinned[1] <= 1e-10) || !std::isfinite(h->pinned[0])) return ITG_ERR_NOTCONVERGED;
   const double smax = sqrt(h->pinned[0] > 0.0 ? h->pinned[0] : 0.0);
   // 3. U = A X diag(1/sigma), one Newton-Schulz step
   ITG_TRY(gemm(h, false, mm, nn, nn, 1.0, Awork, X, 0.0, Uw, precision));

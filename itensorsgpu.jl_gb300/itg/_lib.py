@@ -109,7 +109,7 @@ SIGNATURES = {
                                      C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "itg_autotune_force": (C.c_int, [_P, C.c_int, _I64P, _I32P, C.c_int, _I64P, _I32P, C.c_int, _I64P, _I32P,
                                      C.c_int, C.c_int]),
-    "itg_svd_info": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "itg_svd_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), _I64P]),
     "itg_factorize_trunc": (C.c_int, [_P, C.c_int64, C.c_int64, _P, C.c_int64, C.c_int64, C.c_int64, C.c_double,
                                       C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P, _I64P,
                                       C.POINTER(C.c_double), C.POINTER(C.c_double)]),
