@@ -254,6 +254,10 @@ def run_gpu(args):
         fp64_peak = json.loads(pf.read_text()).get("fp64_tflops")
     flop_step = flops(chi)
     gemm_flop_step = 80 * chi ** 3  # the two chi^3 contractions, FP64-equivalent
+    traffic = {}
+    tf = REPO / "profiles" / "heff2_chi1024_traffic.json"
+    if tf.exists() and chi == 1024:
+        traffic = json.loads(tf.read_text())
 
     results = {}
     for name, prec in (("split", PREC_SPLIT), ("fp64", PREC_FP64)):
@@ -268,7 +272,9 @@ def run_gpu(args):
             slices = 7 * 8 // 2
             achieved = slices * gemm_flop_step * steps / (kms / 1e3) / 1e12 if kms > 0 else None
             roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                    "frac": (achieved / peaks["bf16_tflops"]) if achieved else None, "traffic": None,
+                    "frac": (achieved / peaks["bf16_tflops"]) if achieved else None,
+                    "traffic": traffic.get("k_split_gemm"),
+                    "traffic_source": "ncu capture, profiles/k_split_gemm_heff2_chi1024.md" if traffic else None,
                     "peak_source": f"MEASURED_PEAKS.json bf16_tflops (burst, {src})",
                     "kernel": "k_split_gemm", "launches": kn, "kernel_ms_per_launch": kms / max(kn, 1),
                     "kernel_flop_per_launch": slices * 40 * chi ** 3,
@@ -280,7 +286,9 @@ def run_gpu(args):
             kms, kn = prof[KERNEL_GEMM_F64]
             achieved = gemm_flop_step * steps / (kms / 1e3) / 1e12 if kms > 0 else None
             roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                    "frac": (achieved / fp64_peak) if (achieved and fp64_peak) else None, "traffic": None,
+                    "frac": (achieved / fp64_peak) if (achieved and fp64_peak) else None,
+                    "traffic": traffic.get("k_gemm_gather_f64"),
+                    "traffic_source": "ncu capture, profiles/k_gemm_gather_f64_heff2_chi1024.md" if traffic else None,
                     "peak_source": "profiles/fp64_peak.json (project DFMA probe, measured)",
                     "kernel": "k_gemm_gather_f64", "launches": kn, "kernel_ms_per_launch": kms / max(kn, 1),
                     "kernel_flop_per_launch": 40 * chi ** 3, "gemm_share_of_step": kms / ms}
