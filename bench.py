@@ -373,7 +373,7 @@ def run_gpu(args):
 
 
 # ------------------------------------------------------ DMRG sweep workload
-def measure_sweeps(N, chi, nsweep, cutoff, seed=1236):
+def measure_sweeps(N, chi, nsweep, cutoff, seed=1236, init_linkdim=None, maxdims=None):
     """One DMRG run per form from the same initial state; per-sweep times and phases.
 
     S=1/2 Heisenberg chain of N sites (MPO bond dimension 5), random initial MPS
@@ -388,10 +388,10 @@ def measure_sweeps(N, chi, nsweep, cutoff, seed=1236):
     import itg
     sites = itg.siteinds("S=1/2", N)
     H = itg.cuMPO(itg.heisenberg_mpo(sites))
-    psi0 = itg.randomCuMPS(sites, chi, seed=seed)
+    psi0 = itg.randomCuMPS(sites, init_linkdim or chi, seed=seed)
     out = {}
     for form, prec, svd in (("chosen", "split", 2), ("plain", "fp64", 1)):
-        sw = itg.Sweeps(nsweep, maxdim=[chi], cutoff=[cutoff])
+        sw = itg.Sweeps(nsweep, maxdim=list(maxdims or [chi]), cutoff=[cutoff])
         torch.cuda.synchronize()
         with ClockSampler(0) as clk:
             res = itg.dmrg(H, psi0, sw, precision=prec, svd_method=svd, phase_timing=True, return_result=True)
@@ -405,6 +405,7 @@ def measure_sweeps(N, chi, nsweep, cutoff, seed=1236):
     return {"N": N, "chi": chi, "sweeps": nsweep, "cutoff": cutoff,
             "chosen_seconds": min(ch["sweep_seconds"]), "plain_seconds": min(pl["sweep_seconds"]),
             "chosen_vs_plain_speedup": min(pl["sweep_seconds"]) / min(ch["sweep_seconds"]),
+            "chosen_total_seconds": sum(ch["sweep_seconds"]), "plain_total_seconds": sum(pl["sweep_seconds"]),
             "energy_diff_last_sweep": abs(ch["energies"][-1] - pl["energies"][-1]),
             "detail": out}
 
@@ -412,13 +413,22 @@ def measure_sweeps(N, chi, nsweep, cutoff, seed=1236):
 def run_dmrg(args):
     """DMRG sweep time at bond dimension chi, chosen vs plain form (see measure_sweeps)."""
     N, chi = args.dmrg_n, args.chi
-    r = measure_sweeps(N, chi, args.dmrg_sweeps, args.dmrg_cutoff)
-    line = {"metric": f"DMRG sweep time at chi={chi} (Heisenberg N={N}), chosen vs plain",
-            "value": r["chosen_seconds"], "unit": "s", "higher_is_better": False,
-            "plain_value": r["plain_seconds"], "chosen_vs_plain_speedup": r["chosen_vs_plain_speedup"],
+    maxdims = [int(x) for x in args.dmrg_maxdims.split(",")] if args.dmrg_maxdims else None
+    r = measure_sweeps(N, chi, args.dmrg_sweeps, args.dmrg_cutoff, init_linkdim=args.dmrg_init or None,
+                       maxdims=maxdims)
+    ramp = maxdims is not None
+    line = {"metric": (f"DMRG run time (Heisenberg N={N}, {args.dmrg_sweeps} sweeps, maxdim ramp to {max(maxdims)}), "
+                       f"chosen vs plain" if ramp else
+                       f"DMRG sweep time at chi={chi} (Heisenberg N={N}), chosen vs plain"),
+            "value": r["chosen_total_seconds"] if ramp else r["chosen_seconds"], "unit": "s",
+            "higher_is_better": False,
+            "plain_value": r["plain_total_seconds"] if ramp else r["plain_seconds"],
+            "chosen_vs_plain_speedup": (r["plain_total_seconds"] / r["chosen_total_seconds"]) if ramp
+            else r["chosen_vs_plain_speedup"],
             "energy_diff_last_sweep": r["energy_diff_last_sweep"],
             "config": {"workload": f"dmrg heisenberg N={N} chi={chi}", "sweeps": args.dmrg_sweeps,
-                       "cutoff": args.dmrg_cutoff, "krylovdim": 3, "maxiter": 2},
+                       "cutoff": args.dmrg_cutoff, "krylovdim": 3, "maxiter": 2,
+                       "maxdims": maxdims or [chi], "init_linkdim": args.dmrg_init or chi},
             "dtype": "f64", "data": "synthetic (seeded Philox initial MPS)", "detail": r["detail"]}
     print(json.dumps(line), flush=True)
     return 0
@@ -508,7 +518,14 @@ def run_learned(args):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     l1 = net.step(X, M, Y, 0.0)
-    H = itg.cuMPO(itg.j1j2_mpo(sites, J1=1.0, J2=0.5))
+    # regression loss of the best-scaled diagonal preconditioner on the same samples
+    # (features: f2 = clip(scale / (diag - theta), -10, 10) / 10, so g = c * f2)
+    f2 = X.view(-1, 5)[:, 2].double()
+    Md, Yd = M.double(), Y.double()
+    c = float((f2 * Md * Yd).sum() / (f2 * f2 * Md * Md).sum().clamp_min(1e-300))
+    diag_fit_loss = float(((c * f2 * Md - Yd) ** 2).mean())
+    j2t = args.learn_test_j2
+    H = itg.cuMPO(itg.j1j2_mpo(sites, J1=1.0, J2=j2t))
     psi0 = itg.randomCuMPS(sites, 8, seed=505)
     res = {}
     for name, pc in (("diag", None), ("learned", net)):
@@ -521,17 +538,18 @@ def run_learned(args):
                      "matvecs_per_bond": [x.matvecs / nb for x in r.sweeps],
                      "maxlinkdim": r.sweeps[-1].maxlinkdim, "fallbacks": getattr(r, "fallbacks", 0)}
     d, l = res["diag"], res["learned"]
-    line = {"metric": f"learned vs diagonal Davidson preconditioner, J1-J2 N={N} J2=0.5 (held out)",
+    line = {"metric": f"learned vs diagonal Davidson preconditioner, J1-J2 N={N} J2={j2t}"
+                      + (" (held out)" if j2t not in (0.2, 0.3, 0.4) else " (training coupling)"),
             "value": sum(l["matvecs_per_bond"]) / len(l["matvecs_per_bond"]), "unit": "matvecs/bond",
             "higher_is_better": False,
             "diag_value": sum(d["matvecs_per_bond"]) / len(d["matvecs_per_bond"]),
             "energy_diff_final": abs(l["energies"][-1] - d["energies"][-1]),
             "sweep_seconds_learned": l["sweep_seconds"], "sweep_seconds_diag": d["sweep_seconds"],
             "train": {"samples": int(M.numel()), "loss_before": l0, "loss_after": l1, "steps": args.learn_steps,
-                      "collect_s": t_collect, "train_s": t_train},
+                      "diag_fit_loss": diag_fit_loss, "collect_s": t_collect, "train_s": t_train},
             "detail": res,
             "config": {"workload": f"j1j2 N={N} maxdim={args.learn_maxdim}", "train_J2": [0.2, 0.3, 0.4],
-                       "test_J2": 0.5, "cutoff": 1e-10, "krylovdim": 3, "maxiter": 4, "tol": 1e-9},
+                       "test_J2": j2t, "cutoff": 1e-10, "krylovdim": 3, "maxiter": 4, "tol": 1e-9},
             "dtype": "f64 (network bf16/fp32)", "data": "synthetic (seeded Philox initial MPS)"}
     net.close()
     print(json.dumps(line), flush=True)
@@ -554,6 +572,9 @@ def main():
     ap.add_argument("--dmrg-n", type=int, default=24)
     ap.add_argument("--dmrg-sweeps", type=int, default=2)
     ap.add_argument("--dmrg-cutoff", type=float, default=0.0)
+    ap.add_argument("--dmrg-init", type=int, default=0, help="initial MPS link dimension (0: chi)")
+    ap.add_argument("--dmrg-maxdims", default="", help="comma-separated maxdim per sweep (last repeats)")
+    ap.add_argument("--learn-test-j2", type=float, default=0.5)
     ap.add_argument("--sweep-n", type=int, default=24,
                     help="chain length of the sweep measurement in the default run (0: skip)")
     ap.add_argument("--batch-count", type=int, default=256)
