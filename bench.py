@@ -399,6 +399,8 @@ def measure_sweeps(N, chi, nsweep, cutoff, seed=1236, init_linkdim=None, maxdims
                      "energies": [r.energy for r in res.sweeps],
                      "phases": [r.phases for r in res.sweeps],
                      "maxlinkdim": res.sweeps[-1].maxlinkdim, "matvecs": [r.matvecs for r in res.sweeps],
+                     "svd_jacobi_sweeps": [r.svd_sweeps for r in res.sweeps],
+                     "svd_fp64_fallbacks": [r.svd_fallbacks for r in res.sweeps],
                      "precision": prec, "svd": "mixed" if svd == 2 else "fp64 jacobi",
                      "clocks": clk.summary()}
     ch, pl = out["chosen"], out["plain"]
@@ -430,6 +432,108 @@ def run_dmrg(args):
                        "cutoff": args.dmrg_cutoff, "krylovdim": 3, "maxiter": 2,
                        "maxdims": maxdims or [chi], "init_linkdim": args.dmrg_init or chi},
             "dtype": "f64", "data": "synthetic (seeded Philox initial MPS)", "detail": r["detail"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------ HBM-bound operators + SVD
+def run_ops(args):
+    """Rooflines of the HBM-bound operators and of the SVD kernels (config 2).
+
+    permute: rank-4 tensor of 2^27 doubles (1 GiB) to the reversed mode order,
+    bytes = 2 * 8 |T|; permuted axpby C = a P(A) + b B: 3 * 8 |T|; Diag x Dense
+    (chi x chi times a diagonal on its second index, chi = 16384): 8 (2|T| + |d|).
+    Each is timed with CUDA events over `steps` launches after warm-up, inputs
+    far larger than L2.  SVD: one factorisation of a 2048 x 2048 matrix with
+    sigma_k = exp(-k/20), FP64 Jacobi and mixed, with the Jacobi sweep count.
+    """
+    import torch
+    from itg import _lib
+    h = _lib.handle(0)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    arr = lambda t, xs: (t * len(xs))(*xs)
+    peaks, src = measured_peaks()
+    hbm = peaks["hbm_gbs"]
+    res = {}
+
+    def timed(fn, steps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps / 1e3
+
+    dims = [128, 256, 64, 64]  # 2^27 elements
+    n = 1
+    for x in dims:
+        n *= x
+    A = torch.randn(n, dtype=torch.float64, device="cuda")
+    B = torch.empty_like(A)
+    Cc = torch.randn(n, dtype=torch.float64, device="cuda")
+    mA, mB = [1, 2, 3, 4], [4, 3, 2, 1]
+    t = timed(lambda: h.call("itg_permute", 0, C.c_double(1.0), p(A), 4, arr(C.c_int64, dims), arr(C.c_int32, mA),
+                             p(B), arr(C.c_int32, mB)), args.steps)
+    res["permute_rank4_reverse"] = {"GB/s": 16 * n / t / 1e9, "frac_hbm": 16 * n / t / 1e9 / hbm, "ms": t * 1e3}
+    t = timed(lambda: h.call("itg_axpby_permuted", 0, C.c_double(1.5), p(A), 4, arr(C.c_int64, dims),
+                             arr(C.c_int32, mA), C.c_double(-0.5), p(Cc), arr(C.c_int32, mB), p(Cc)), args.steps)
+    res["axpby_permuted"] = {"GB/s": 24 * n / t / 1e9, "frac_hbm": 24 * n / t / 1e9 / hbm, "ms": t * 1e3}
+    del A, B, Cc
+    chi = 16384
+    T = torch.randn(chi * chi, dtype=torch.float64, device="cuda")
+    dv = torch.randn(chi, dtype=torch.float64, device="cuda")
+    Out = torch.empty_like(T)
+    t = timed(lambda: h.call("itg_diag_contract", 0, C.c_double(1.0), p(dv), 0, 2, arr(C.c_int64, [chi, chi]),
+                             arr(C.c_int32, [2, 3]), p(T), 2, arr(C.c_int64, [chi, chi]), arr(C.c_int32, [1, 2]),
+                             C.c_double(0.0), p(Out), 2, arr(C.c_int64, [chi, chi]), arr(C.c_int32, [1, 3])),
+              args.steps)
+    res["diag_times_dense"] = {"GB/s": 8 * (2 * chi * chi + chi) / t / 1e9,
+                               "frac_hbm": 8 * (2 * chi * chi + chi) / t / 1e9 / hbm, "ms": t * 1e3}
+    del T, Out
+    # SVD microbench
+    nn = 2048
+    g = torch.Generator(device="cuda").manual_seed(1234 + 2)
+    Q1, _ = torch.linalg.qr(torch.randn(nn, nn, dtype=torch.float64, device="cuda", generator=g))
+    Q2, _ = torch.linalg.qr(torch.randn(nn, nn, dtype=torch.float64, device="cuda", generator=g))
+    sv = torch.exp(-torch.arange(nn, dtype=torch.float64, device="cuda") / 20.0)
+    M = ((Q1 * sv) @ Q2.T).T.contiguous().reshape(-1)
+    U = torch.empty(nn * nn, dtype=torch.float64, device="cuda")
+    S = torch.empty(nn, dtype=torch.float64, device="cuda")
+    V = torch.empty_like(U)
+    fp64_peak = None
+    pf = REPO / "profiles" / "fp64_peak.json"
+    if pf.exists():
+        fp64_peak = json.loads(pf.read_text()).get("fp64_tflops")
+    for name, method, prec in (("fp64_jacobi", 1, 0), ("mixed_split", 2, 1)):
+        k, te, dc = C.c_int64(), C.c_double(), C.c_double()
+        for rep in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            h.call("itg_svd_trunc_ex", C.c_int64(nn), C.c_int64(nn), p(M), C.c_int64(nn), C.c_int64(nn // 2),
+                   C.c_int64(1), C.c_double(1e-12), 0, 1, 0, p(U), p(S), p(V), C.byref(k), C.byref(te),
+                   C.byref(dc), method, prec)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+        sw = C.c_int()
+        mu = C.c_int()
+        h.call("itg_svd_info", C.byref(sw), C.byref(mu), None)
+        err = float((S[: k.value] - sv[: k.value]).abs().max())
+        r = {"seconds": dt, "jacobi_sweeps": sw.value, "k": k.value, "max_sigma_err": err, "mixed_used": mu.value}
+        if method == 1:
+            # one-sided Jacobi: n(n-1)/2 pairs x (3 dot FMAs + 4 rotation flops per row) x 2 (W and V)
+            flop_sweep = nn * (nn - 1) / 2 * 14.0 * nn * 2
+            r["jacobi_flop_per_sweep"] = flop_sweep
+            r["tflops_lower_bound"] = flop_sweep * sw.value / dt / 1e12
+            r["frac_fp64_peak_lower_bound"] = r["tflops_lower_bound"] / fp64_peak if fp64_peak else None
+        res["svd2048_" + name] = r
+    line = {"metric": "HBM-bound operator and SVD rooflines (config 2)", "value": res["permute_rank4_reverse"]["GB/s"],
+            "unit": "GB/s", "higher_is_better": True, "hbm_peak": hbm, "peak_source": src, "detail": res,
+            "config": {"workload": "ops", "permute_elements": n, "diag_chi": chi, "svd_n": nn, "steps": args.steps},
+            "dtype": "f64", "data": "synthetic (torch randn / Haar exp spectrum)"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -568,7 +672,7 @@ def main():
     ap.add_argument("--chi", type=int, default=CHI)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="heff", choices=["heff", "dmrg", "batched", "learned"])
+    ap.add_argument("--workload", default="heff", choices=["heff", "dmrg", "batched", "learned", "ops"])
     ap.add_argument("--dmrg-n", type=int, default=24)
     ap.add_argument("--dmrg-sweeps", type=int, default=2)
     ap.add_argument("--dmrg-cutoff", type=float, default=0.0)
@@ -594,6 +698,8 @@ def main():
         return run_batched(args)
     if args.workload == "learned":
         return run_learned(args)
+    if args.workload == "ops":
+        return run_ops(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -141,6 +141,30 @@ __device__ __forceinline__ void tc_ld_32x32b_x32(uint32_t taddr, uint32_t (&r)[3
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+__device__ __forceinline__ void tc_ld_32x32b_x32_nowait(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_st_32x32b_x32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]),
+      "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]),
+      "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
 // core groups 1024 bytes apart (SBO), descriptor version 1.
 __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
@@ -265,12 +289,18 @@ __device__ __forceinline__ double i64_to_double_scaled(long long v, int exp2) {
       (long long)(sgn | ((unsigned long long)be << 52) | (mant & ((1ull << 52) - 1))));
 }
 
+// Tile variants: BN = 256 keeps the int64 accumulators in global memory
+// (two 256-column FP32 TMEM buffers fill the TMEM); BN = 128 keeps them in
+// TMEM columns 256..511 (low / high words), so a drain never leaves the SM,
+// and runs a 6-stage operand ring.
 template <int BN>
 struct Smem {
+  static constexpr bool TACC = BN == 128;
+  static constexpr int NSTAGE = TACC ? 6 : STAGES;
   static constexpr int A_BYTES = BM * BK * 2;
   static constexpr int B_BYTES = BN * BK * 2;
   static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-  static constexpr int TOTAL = 1024 /*align slack*/ + STAGES * STAGE_BYTES + 256;
+  static constexpr int TOTAL = 1024 /*align slack*/ + NSTAGE * STAGE_BYTES + 256;
 };
 
 template <int BN>
@@ -279,24 +309,26 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
              GemmArgs args) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  constexpr int NST = Smem<BN>::NSTAGE;
+  constexpr bool TACC = Smem<BN>::TACC;
   uint8_t* stage_mem = base;
-  uint64_t* bars = (uint64_t*)(base + STAGES * Smem<BN>::STAGE_BYTES);
-  uint64_t* full = bars;                 // [STAGES]
-  uint64_t* empty = bars + STAGES;       // [STAGES]
-  uint64_t* acc_full = bars + 2 * STAGES;      // [2]
-  uint64_t* acc_empty = bars + 2 * STAGES + 2; // [2]
-  uint64_t* done_bar = bars + 2 * STAGES + 4;  // [1]
-  volatile int* abort_flag = (volatile int*)(bars + 2 * STAGES + 5);
-  uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 6);
+  uint64_t* bars = (uint64_t*)(base + NST * Smem<BN>::STAGE_BYTES);
+  uint64_t* full = bars;                 // [NST]
+  uint64_t* empty = bars + NST;          // [NST]
+  uint64_t* acc_full = bars + 2 * NST;      // [2]
+  uint64_t* acc_empty = bars + 2 * NST + 2; // [2]
+  uint64_t* done_bar = bars + 2 * NST + 4;  // [1]
+  volatile int* abort_flag = (volatile int*)(bars + 2 * NST + 5);
+  uint32_t* tmem_slot = (uint32_t*)(bars + 2 * NST + 6);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tile = blockIdx.x;
   const int m_tile = tile / args.tiles_n, n_tile = tile - m_tile * args.tiles_n;
   const int m0 = m_tile * BM, n0 = n_tile * BN;
-  constexpr uint32_t TMEM_COLS = 2 * BN;
+  constexpr uint32_t TMEM_COLS = TACC ? 512 : 2 * BN;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
+    for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -326,9 +358,9 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
       sc.begin(args.S, args.nkb);
       int it = 0;
       while (sc.valid() && !*abort_flag) {
-        const int s = it % STAGES;
-        if (it >= STAGES) {
-          if (!mbar_wait(&empty[s], ((it / STAGES) - 1) & 1, args.err, abort_flag)) break;
+        const int s = it % NST;
+        if (it >= NST) {
+          if (!mbar_wait(&empty[s], ((it / NST) - 1) & 1, args.err, abort_flag)) break;
         }
         uint8_t* sa = stage_mem + s * Smem<BN>::STAGE_BYTES;
         uint8_t* sb = sa + Smem<BN>::A_BYTES;
@@ -339,8 +371,8 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
         ++it;
       }
       // make sure no copy is still landing in shared memory when we leave
-      for (int j = std::max(0, it - STAGES); j < it; ++j)
-        mbar_wait(&full[j % STAGES], (j / STAGES) & 1, args.err, abort_flag);
+      for (int j = std::max(0, it - NST); j < it; ++j)
+        mbar_wait(&full[j % NST], (j / NST) & 1, args.err, abort_flag);
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
@@ -358,8 +390,8 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
           tc_fence_after();
           if (!ok) break;
         }
-        const int s = it % STAGES;
-        ok = mbar_wait(&full[s], (it / STAGES) & 1, args.err, abort_flag);
+        const int s = it % NST;
+        ok = mbar_wait(&full[s], (it / NST) & 1, args.err, abort_flag);
         if (!ok) break;
         tc_fence_after();
         const uint32_t sa = smem_u32(stage_mem + s * Smem<BN>::STAGE_BYTES);
@@ -413,15 +445,28 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
 #pragma unroll 1
       for (int c0 = col_lo; c0 < col_hi; c0 += 32) {
         uint32_t r[32];
-        tc_ld_32x32b_x32(tbase + (uint32_t)c0, r);
-        long long* ap = acc + (size_t)c0 * BM + row;
         long long old[32];
-        if (!first_drain) {
+        long long* ap = TACC ? nullptr : acc + (size_t)c0 * BM + row;
+        // TMEM-resident accumulator: low words in columns 256 + c, high words in 384 + c
+        const uint32_t tlo = tmem_base + ((uint32_t)(quarter * 32) << 16) + 256u + (uint32_t)c0;
+        const uint32_t thi = tlo + 128u;
+        if (TACC && !first_drain) {
+          uint32_t lo[32], hi[32];
+          tc_ld_32x32b_x32_nowait(tbase + (uint32_t)c0, r);
+          tc_ld_32x32b_x32_nowait(tlo, lo);
+          tc_ld_32x32b_x32_nowait(thi, hi);
+          tc_wait_ld();
 #pragma unroll
-          for (int j = 0; j < 32; ++j) old[j] = ap[(size_t)j * BM];
+          for (int j = 0; j < 32; ++j) old[j] = (long long)(((unsigned long long)hi[j] << 32) | lo[j]);
         } else {
+          tc_ld_32x32b_x32(tbase + (uint32_t)c0, r);
+          if (!TACC && !first_drain) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) old[j] = 0;
+            for (int j = 0; j < 32; ++j) old[j] = ap[(size_t)j * BM];
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) old[j] = 0;
+          }
         }
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
@@ -430,8 +475,20 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
           old[j] += t;
         }
         if (!last) {
+          if (TACC) {
+            uint32_t lo[32], hi[32];
 #pragma unroll
-          for (int j = 0; j < 32; ++j) ap[(size_t)j * BM] = old[j];
+            for (int j = 0; j < 32; ++j) {
+              lo[j] = (uint32_t)((unsigned long long)old[j] & 0xFFFFFFFFull);
+              hi[j] = (uint32_t)((unsigned long long)old[j] >> 32);
+            }
+            tc_st_32x32b_x32(tlo, lo);
+            tc_st_32x32b_x32(thi, hi);
+            tc_wait_st();
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) ap[(size_t)j * BM] = old[j];
+          }
         } else if (m < args.M) {
           // final drain: convert to FP64 with integer instructions, scatter through the plan
           const int64_t cm = args.offCm[m];
@@ -640,7 +697,7 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   auto take = [&](size_t b) { size_t o = off; off += itg_align256(b); return o; };
   const size_t oEA = take(sizeof(int) * Mpad), oEB = take(sizeof(int) * Npad);
   const size_t oSA = take((size_t)2 * S * Mpad * Kpad), oSB = take((size_t)2 * S * Npad * Kpad);
-  const size_t oAcc = take(sizeof(long long) * (size_t)tiles * BN * BM);
+  const size_t oAcc = take(Smem<BN>::TACC ? 0 : sizeof(long long) * (size_t)tiles * BN * BM);
   const size_t oErr = take(sizeof(int));
   ITG_TRY(ws_reserve(h, off));
   char* ws = (char*)h->split_ws;

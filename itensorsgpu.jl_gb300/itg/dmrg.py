@@ -87,6 +87,10 @@ class SweepRecord:
     # rest); phases are separated by stream synchronisations only when
     # dmrg(..., phase_timing=True)
     phases: dict = field(default_factory=dict)
+    # factorisations of the sweep: Jacobi sweeps in total, and how many mixed
+    # SVDs failed their refinement check and were redone in FP64
+    svd_sweeps: int = 0
+    svd_fallbacks: int = 0
 
 
 @dataclass
@@ -241,6 +245,9 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
         maxdim, mindim, cutoff = sweeps.maxdim(sw), sweeps.mindim(sw), sweeps.cutoff(sw)
         maxerr = 0.0
         nmv_tot = 0
+        svd_sw = 0
+        fb0 = C.c_int64()
+        h.call("itg_svd_info", None, None, C.byref(fb0))
         ph = dict(eig=0.0, svd=0.0, env=0.0)
 
         def tick(key, t):
@@ -306,6 +313,9 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
             except NotConverged:
                 pass  # factors are still returned; the rotation limit is generous
             tp = tick("svd", tp)
+            swc = C.c_int()
+            h.call("itg_svd_info", C.byref(swc), None, None)
+            svd_sw += swc.value
             kk = int(k.value)
             maxerr = max(maxerr, te.value)
             schmidt[b + 1] = S[:kk].clone()
@@ -328,8 +338,10 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
         secs = time.perf_counter() - t0
         if phase_timing:
             ph["other"] = max(0.0, secs - ph["eig"] - ph["svd"] - ph["env"])
+        fb1 = C.c_int64()
+        h.call("itg_svd_info", None, None, C.byref(fb1))
         rec = SweepRecord(energy, max(x[2] for x in ch.Ad[:-1]), maxerr, secs, nmv_tot,
-                          ph if phase_timing else {})
+                          ph if phase_timing else {}, svd_sw, int(fb1.value - fb0.value))
         records.append(rec)
         if outputlevel > 0:
             print(f"After sweep {sw + 1} energy={energy:.14f} maxlinkdim={rec.maxlinkdim} "
