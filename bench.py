@@ -689,7 +689,7 @@ def main():
     ap.add_argument("--learn-maxdim", type=int, default=512)
     ap.add_argument("--learn-train-maxdim", type=int, default=64)
     ap.add_argument("--learn-samples", type=int, default=4_000_000)
-    ap.add_argument("--learn-steps", type=int, default=600)
+    ap.add_argument("--learn-steps", type=int, default=3000)
     ap.add_argument("--learn-sweeps", type=int, default=4)
     args = ap.parse_args()
     if args.workload == "dmrg":

@@ -388,12 +388,15 @@ ITG_API int itg_mlp_train_step(itg_handle* h, void* mlp, int64_t n, const float*
 /* Features of the learned preconditioner for the residual r of the two-site
  * problem (F = 5): normalised residual, (diag - theta)/scale, clipped inverse,
  * left / right Schmidt values of each element's link indices (lamL: chiL
- * values, lamR: chiR values, either may be NULL).  mult = normalised residual. */
+ * values, lamR: chiR values, either may be NULL).  mult = the diagonally
+ * preconditioned normalised residual (normalised residual x clipped inverse). */
 ITG_API int itg_heff2_features(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d,
                                const double* r, const double* diag, double theta,
                                const double* lamL, const double* lamR, float* X, float* mult);
 /* itg_davidson_heff2 with the learned preconditioner: corrections are
- * t = network(features) * r_hat; convergence is still judged by the exact
+ * t = (1 + network(features)) * mult (mult as in itg_heff2_features: an
+ * untrained network with a zero output layer is the diagonal preconditioner);
+ * convergence is still judged by the exact
  * residual norm, and when a learned correction fails to reduce the residual by
  * 10% the diagonal preconditioner takes over for the rest of the solve
  * (*fallbacks counts those hand-overs, may be NULL). */

@@ -50,6 +50,11 @@ extern "C" int itg_create(int device, itg_handle** out) {
     delete h;
     return ITG_ERR_ALLOC;
   }
+  if (cudaMalloc((void**)&h->gemv_part, sizeof(double) * ITG_GEMV_MAX_PART) != cudaSuccess) {
+    cudaFreeHost(h->pinned);
+    delete h;
+    return ITG_ERR_ALLOC;
+  }
   if (cudaMalloc((void**)&h->dev_status, 64) != cudaSuccess) {
     cudaFreeHost(h->pinned);
     delete h;
@@ -137,6 +142,7 @@ extern "C" int itg_destroy(itg_handle* h) {
   if (h->tune_buf) cudaFree(h->tune_buf);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->dev_status) cudaFree(h->dev_status);
+  if (h->gemv_part) cudaFree(h->gemv_part);
   delete h;
   return ITG_OK;
 }
@@ -376,13 +382,25 @@ extern "C" int itg_nrm2(itg_handle* h, int64_t n, const double* x, double* resul
   return ITG_OK;
 }
 
-// out[j] = X[:, j] . y for j < k.  One block per column, fixed reduction order.
-__global__ void k_gemv_t(int64_t n, const double* __restrict__ X, int64_t ldx,
-                         const double* __restrict__ y, double* __restrict__ out) {
+// out[j] = X[:, j] . y for j < k.  Two-stage, fixed-order reduction: block (b, j) sums its chunk of column j
+// into part[j * nb + b]; k_gemv_t_final adds the nb partials of each column.
+__global__ void k_gemv_t_part(int64_t n, const double* __restrict__ X, int64_t ldx,
+                              const double* __restrict__ y, double* __restrict__ part) {
   __shared__ double sh[32];
-  const double* col = X + (int64_t)blockIdx.x * ldx;
+  const int nb = gridDim.x, b = blockIdx.x, j = blockIdx.y;
+  const double* col = X + (int64_t)j * ldx;
+  const int64_t chunk = (n + nb - 1) / nb;
+  const int64_t lo = (int64_t)b * chunk, hi = lo + chunk < n ? lo + chunk : n;
   double s = 0.0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s = fma(col[i], y[i], s);
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) s = fma(col[i], y[i], s);
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) part[(int64_t)j * nb + b] = s;
+}
+
+__global__ void k_gemv_t_final(int nb, const double* __restrict__ part, double* __restrict__ out) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s += part[(int64_t)blockIdx.x * nb + i];
   s = block_sum(s, sh);
   if (threadIdx.x == 0) out[blockIdx.x] = s;
 }
@@ -403,7 +421,15 @@ extern "C" int itg_gemv_t(itg_handle* h, int64_t n, int64_t k, const double* X, 
   if (!h || n < 0 || k < 0 || ldx < n) return ITG_ERR_INVALID;
   if (k == 0) return ITG_OK;
   if (k > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "gemv_t: k=%lld too large", (long long)k);
-  k_gemv_t<<<(int)k, 512, 0, h->stream>>>(n, X, ldx, y, out);
+  // enough blocks per column to fill the GPU (4 per SM over all columns),
+  // each covering at least 2048 elements; partials in the handle's buffer
+  int64_t nb = (4 * (int64_t)h->num_sms + k - 1) / k;
+  const int64_t by_size = (n + 2047) / 2048;
+  if (nb > by_size) nb = by_size;
+  if (nb > ITG_GEMV_MAX_PART / k) nb = ITG_GEMV_MAX_PART / k;
+  if (nb < 1) nb = 1;
+  k_gemv_t_part<<<dim3((unsigned)nb, (unsigned)k), 256, 0, h->stream>>>(n, X, ldx, y, h->gemv_part);
+  k_gemv_t_final<<<(unsigned)k, 256, 0, h->stream>>>((int)nb, h->gemv_part, out);
   ITG_CHECK_LAUNCH(h);
   return ITG_OK;
 }

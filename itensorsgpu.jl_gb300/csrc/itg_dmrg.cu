@@ -240,11 +240,15 @@ __global__ void k_precond(int64_t n, const double* __restrict__ r, const double*
 }
 
 // Per-element features of the learned preconditioner (F = 5, float, element-major):
-//   f0 = r_e sqrt(n) / |r|                      (normalised residual; also the multiplier)
+//   f0 = r_e sqrt(n) / |r|                      (normalised residual)
 //   f1 = (diag_e - theta) / scale               (scale = mean |diag - theta|)
 //   f2 = clamp(scale / (diag_e - theta), -10, 10) / 10
 //   f3 = log10(max(lamL[a], 1e-12)) / 12 + 0.5  (left Schmidt value of the element's a)
 //   f4 = log10(max(lamR[b], 1e-12)) / 12 + 0.5  (right Schmidt value of its b)
+// and the multiplier m = f0 * 10 f2: the diagonally preconditioned residual
+// (normalised, with the clipped inverse).  The learned correction is
+// t = (1 + g) m, so a network with g = 0 is the diagonal preconditioner and
+// training learns a per-element correction to it.
 __global__ void k_features(int64_t n, int64_t chiL, int64_t dd, const double* __restrict__ r,
                            const double* __restrict__ dg, double theta, double rscale, double dscale,
                            const double* __restrict__ lamL, const double* __restrict__ lamR,
@@ -254,21 +258,21 @@ __global__ void k_features(int64_t n, int64_t chiL, int64_t dd, const double* __
     const double dv = dg[e] - theta;
     double inv = dscale / (fabs(dv) > 1e-300 ? dv : 1e-300);
     inv = inv > 10.0 ? 10.0 : (inv < -10.0 ? -10.0 : inv);
-    const float f0 = (float)(r[e] * rscale);
-    X[e * 5 + 0] = f0;
+    const double f0 = r[e] * rscale;
+    X[e * 5 + 0] = (float)f0;
     X[e * 5 + 1] = (float)(dv / dscale);
     X[e * 5 + 2] = (float)(inv / 10.0);
     X[e * 5 + 3] = lamL ? (float)(log10(fmax(lamL[a], 1e-12)) / 12.0 + 0.5) : 0.f;
     X[e * 5 + 4] = lamR ? (float)(log10(fmax(lamR[b], 1e-12)) / 12.0 + 0.5) : 0.f;
-    mult[e] = f0;
+    mult[e] = (float)(f0 * inv);
   }
 }
 
-// t = g * mult (the learned correction, in FP64)
+// t = (1 + g) * mult (the learned correction, in FP64)
 __global__ void k_learned_corr(int64_t n, const float* __restrict__ g, const float* __restrict__ mult,
                                double* __restrict__ t) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-    t[e] = (double)g[e] * (double)mult[e];
+    t[e] = (1.0 + (double)g[e]) * (double)mult[e];
 }
 
 // out[0] = sum |diag - theta| (block partial sums, reduced on the host side)
@@ -547,7 +551,7 @@ static int davidson_impl(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d, i
       double tn = 0.0;
       for (int attempt = 0; attempt < 2; ++attempt) {
         if (attempt == 0 && use_learned) {
-          // learned correction t = g(features) * r_hat
+          // learned correction t = (1 + g(features)) * (diagonally preconditioned r_hat)
           const int nb = itg_blocks_for(n, 256, 512);
           k_abs_diff_sum<<<nb, 256, 0, h->stream>>>(n, dg, theta, Fp);
           ITG_CHECK_LAUNCH(h);

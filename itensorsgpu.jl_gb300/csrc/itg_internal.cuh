@@ -16,6 +16,7 @@
 
 #define ITG_MAX_RANK 16
 #define ITG_PINNED_DOUBLES 4096  // host staging for small results (Davidson subspace <= 32x32)
+#define ITG_GEMV_MAX_PART 65536  // partial sums of itg_gemv_t
 
 // A lowered contraction C[m,n] = sum_k A[m,k] B[k,n] with every operand
 // addressed through offset tables (see itg_contract.cu).
@@ -56,6 +57,8 @@ struct itg_handle {
   size_t split_ws_bytes = 0;
   // Small pinned host buffer for scalar results (dot, truncation outputs).
   double* pinned = nullptr;
+  // Partial sums of itg_gemv_t (its own buffer: callers hold scratch regions).
+  double* gemv_part = nullptr;
   // Persistent device buffers of the contraction plans, keyed by shape.
   std::unordered_map<std::string, std::shared_ptr<ContractPlan>> plans;
   // Device status word for bounded waits (ITG_ERR_TIMEOUT reporting).

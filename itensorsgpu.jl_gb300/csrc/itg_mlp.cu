@@ -5,12 +5,13 @@
 //   z1 = W1 x + b1, a1 = relu(z1)        W1: 128 x F
 //   z2 = W2 a1 + b2, a2 = relu(z2)       W2: 128 x 128
 //   g  = w3 . a2 + b3                    w3: 128
-// Davidson uses it as a multiplicative preconditioner: the correction is
-// t_e = g(features_e) * r_e, which contains the diagonal preconditioner
-// 1/(diag_e - theta) as one representable function.  Training minimises
+// Davidson uses it as a correction of the diagonal preconditioner: with
+// m_e = r_e / (diag_e - theta) (normalised, clipped), the correction is
+// t_e = (1 + g(features_e)) m_e, so g = 0 (the initial output layer) is the
+// diagonal preconditioner.  Training minimises
 //   loss = mean_e (g_e * m_e - y_e)^2
-// on (features, m = normalised residual, y = normalised ideal correction)
-// samples that the plain solver generates.
+// with m the (scaled) diagonal correction and y the part of the ideal
+// correction it misses, on samples that the plain solver generates.
 //
 // Master weights are FP32; the forward and backward passes read a BF16 copy
 // (rounded to nearest even) and accumulate in FP32.  Per-CTA partial weight
@@ -291,7 +292,9 @@ extern "C" int itg_mlp_create(itg_handle* h, int in_dim, uint64_t seed, void** o
   const int F = in_dim;
   for (int64_t i = 0; i < (int64_t)MW * F; ++i) w[oW1(F) + i] = (float)(uni() * std::sqrt(6.0 / F));
   for (int64_t i = 0; i < (int64_t)MW * MW; ++i) w[oW2(F) + i] = (float)(uni() * std::sqrt(6.0 / MW));
-  for (int64_t i = 0; i < MW; ++i) w[ow3(F) + i] = (float)(uni() * std::sqrt(3.0 / MW));
+  // output layer starts at zero: g = 0, i.e. the learned preconditioner
+  // starts as the diagonal one (the first Adam step moves w3 off zero)
+  for (int64_t i = 0; i < MW; ++i) w[ow3(F) + i] = 0.f;
   ITG_CUDA(h, cudaMemcpy(M->master, w.data(), bytes, cudaMemcpyHostToDevice));
   ITG_CUDA(h, cudaMemset(M->m, 0, bytes));
   ITG_CUDA(h, cudaMemset(M->v, 0, bytes));

@@ -3,11 +3,14 @@
 The network (itg_mlp_*, hand-written BF16/FP32 kernels in csrc/itg_mlp.cu)
 maps per-element features of the two-site problem (normalised residual,
 shifted diagonal, clipped inverse diagonal, left/right Schmidt values) to a
-multiplier g, and the correction is t = g * r_hat.  Training samples come from
-the plain solver itself: at every bond of a plain DMRG run the starting vector
-x0 is refined to the converged eigenvector x* with the plain Davidson, and the
+correction g of the diagonal preconditioner: t = (1 + g) m with m the
+diagonally preconditioned residual, so the untrained network (zero output
+layer) is the diagonal preconditioner.  Training samples come from the plain
+solver itself: at every bond of a plain DMRG run the starting vector x0 is
+refined to the converged eigenvector x* with the plain Davidson; the
 normalised ideal correction d = x* - (x0.x*) x0 (oriented so that d.r >= 0) is
-the regression target.  In use, convergence is judged by the exact residual of
+split into its best fit c m by the diagonal correction and the rest d - c m,
+and the network learns g with g (c m) ~ d - c m.  In use, convergence is judged by the exact residual of
 the plain matvec and the diagonal preconditioner takes over when a learned
 step stalls (itg_davidson_heff2_learned).
 """
@@ -147,9 +150,14 @@ class SampleCollector:
         h.call("itg_heff2_features", C.c_int64(chiL), C.c_int64(chiR), C.c_int64(d), _p(r), _p(dg),
                C.c_double(th.value), _p(lamL) if lamL is not None else None,
                _p(lamR) if lamR is not None else None, _p(X), _p(M))
+        # best scale of the diagonal correction, then the part it misses
+        y = dvec.float()
+        mm = float((M.double() * M.double()).sum())
+        c = float((M.double() * dvec).sum()) / mm if mm > 0 else 0.0
+        Mc = M * c
         self.X.append(X)
-        self.M.append(M)
-        self.Y.append(dvec.float())
+        self.M.append(Mc)
+        self.Y.append(y - Mc)
         self.count += n
 
     def data(self):

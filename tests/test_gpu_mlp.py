@@ -5,8 +5,9 @@
 * the first Adam step against its closed form;
 * training reduces the loss on a synthetic regression;
 * the learned eigensolver reaches the same eigenvalue as the plain one, with
-  an untrained network (the stall rule hands over to the diagonal
-  preconditioner) and inside a full DMRG run with a trained network.
+  a random network (the stall rule hands over to the diagonal
+  preconditioner) and inside a full DMRG run with a trained network;
+* a fresh network (zero output layer) is the diagonal preconditioner.
 """
 import ctypes as C
 import json
@@ -128,9 +129,10 @@ def _sym_heff(chi, d, w, seed):
     return L, W1, W2, R, psi
 
 
-def test_learned_davidson_untrained_falls_back_and_converges(gpu):
-    """A random network: its corrections stall, the diagonal preconditioner
-    takes over (fallbacks counted) and the converged eigenvalue is exact."""
+def test_learned_davidson_random_network_falls_back_and_converges(gpu):
+    """A network with large random weights: its corrections stall, the
+    diagonal preconditioner takes over (fallbacks counted) and the converged
+    eigenvalue is exact."""
     import torch
     from itg import _lib
     chi, d, w = 12, 2, 5
@@ -140,6 +142,7 @@ def test_learned_davidson_untrained_falls_back_and_converges(gpu):
                   for i in range(n)], axis=1)
     e0 = np.linalg.eigvalsh(0.5 * (H + H.T))[0]
     net = _net(seed=1)
+    _rand_params(net, 99, scale=1.0)
     dev = lambda a: torch.from_numpy(O.flat(a).copy()).cuda()
     Ld, W1d, W2d, Rd, pd = map(dev, (L, W1, W2, R, psi))
     h = _lib.handle(0)
@@ -192,4 +195,34 @@ def test_dmrg_with_trained_preconditioner(gpu):
     plain = gpu.dmrg(H2, gpu.randomCuMPS(sites, 4, seed=8), sw2, return_result=True)
     learned = gpu.dmrg(H2, gpu.randomCuMPS(sites, 4, seed=8), sw2, preconditioner=net, return_result=True)
     assert abs(plain.energy - learned.energy) < 1e-9 * abs(plain.energy)
+    net.close()
+
+
+def test_fresh_network_is_the_diagonal_preconditioner(gpu):
+    """With the zero output layer of a new network, g = 0 and the learned
+    correction is the diagonally preconditioned residual: the eigensolver takes
+    the same number of matvecs as the plain one and reaches the same value."""
+    import torch
+    from itg import _lib
+    chi, d, w = 12, 2, 5
+    L, W1, W2, R, psi = _sym_heff(chi, d, w, seed=6)
+    net = _net(seed=4)
+    X = torch.randn(100 * F, dtype=torch.float32, device="cuda")
+    assert torch.count_nonzero(net.forward(X)) == 0
+    dev = lambda a: torch.from_numpy(O.flat(a).copy()).cuda()
+    h = _lib.handle(0)
+    res = []
+    for learned in (False, True):
+        Ld, W1d, W2d, Rd, pd = map(dev, (L, W1, W2, R, psi))
+        e, nmv, fb = C.c_double(), C.c_int(), C.c_int()
+        args = (C.c_int64(chi), C.c_int64(chi), C.c_int64(d), C.c_int64(w), C.c_int64(w), C.c_int64(w),
+                _p(Ld), _p(W1d), _p(W2d), _p(Rd), _p(pd), 8, 50, C.c_double(1e-10), 0)
+        if learned:
+            h.call("itg_davidson_heff2_learned", *args, net.ptr, None, None, C.byref(e), C.byref(nmv), C.byref(fb))
+        else:
+            h.call("itg_davidson_heff2", *args, C.byref(e), C.byref(nmv))
+        res.append((e.value, nmv.value))
+    (e0, n0), (e1, n1) = res
+    assert abs(e0 - e1) < 1e-9 * abs(e0)
+    assert abs(n0 - n1) <= max(2, n0 // 5), (n0, n1)
     net.close()
