@@ -538,6 +538,41 @@ def run_ops(args):
     return 0
 
 
+# ------------------------------------------------------ one bond factorisation
+def run_svd(args):
+    """One itg_factorize_trunc of an n x n matrix A = Q1 diag(exp(-k/60)) Q2^T (Haar Q1, Q2
+    from numpy, seed 7), keeping n/2 columns: the DMRG bond split at chi = n/2.  Used as the
+    small driver of the SVD profiles; prints time, Jacobi sweeps and the method used."""
+    import numpy as np
+    import torch
+    from itg import _lib
+    h = _lib.handle(0)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    n = args.svd_n
+    rng = np.random.default_rng(7)
+    Q1, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    Q2, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    M = (Q1 * np.exp(-np.arange(n) / 60.0)) @ Q2.T
+    A = torch.from_numpy(np.asfortranarray(M).ravel(order="F").copy()).cuda()
+    L = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    S = torch.empty(n, dtype=torch.float64, device="cuda")
+    Cm = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    k = C.c_int64()
+    prec = 1 if args.svd_method == 2 else 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h.call("itg_factorize_trunc", C.c_int64(n), C.c_int64(n), p(A), C.c_int64(n), C.c_int64(n // 2), C.c_int64(1),
+           C.c_double(0.0), 0, 1, 0, 0, args.svd_method, prec, p(L), p(S), p(Cm), C.byref(k), None, None)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    sw, mu, fb = C.c_int(), C.c_int(), C.c_int64()
+    h.call("itg_svd_info", C.byref(sw), C.byref(mu), C.byref(fb))
+    print(json.dumps({"metric": f"bond factorisation n={n}", "value": dt, "unit": "s", "higher_is_better": False,
+                      "method": "mixed" if args.svd_method == 2 else "fp64 jacobi", "k": k.value,
+                      "jacobi_sweeps": sw.value, "mixed_used": mu.value, "fallbacks": fb.value}), flush=True)
+    return 0
+
+
 # ------------------------------------------------------ many instances (batched)
 def run_batched(args):
     """Many independent disordered XXZ chains advanced in lockstep vs looping the plain path.
@@ -672,13 +707,15 @@ def main():
     ap.add_argument("--chi", type=int, default=CHI)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="heff", choices=["heff", "dmrg", "batched", "learned", "ops"])
+    ap.add_argument("--workload", default="heff", choices=["heff", "dmrg", "batched", "learned", "ops", "svd"])
     ap.add_argument("--dmrg-n", type=int, default=24)
     ap.add_argument("--dmrg-sweeps", type=int, default=2)
     ap.add_argument("--dmrg-cutoff", type=float, default=0.0)
     ap.add_argument("--dmrg-init", type=int, default=0, help="initial MPS link dimension (0: chi)")
     ap.add_argument("--dmrg-maxdims", default="", help="comma-separated maxdim per sweep (last repeats)")
     ap.add_argument("--learn-test-j2", type=float, default=0.5)
+    ap.add_argument("--svd-n", type=int, default=2048)
+    ap.add_argument("--svd-method", type=int, default=2, choices=[1, 2])
     ap.add_argument("--sweep-n", type=int, default=24,
                     help="chain length of the sweep measurement in the default run (0: skip)")
     ap.add_argument("--batch-count", type=int, default=256)
@@ -700,6 +737,8 @@ def main():
         return run_learned(args)
     if args.workload == "ops":
         return run_ops(args)
+    if args.workload == "svd":
+        return run_svd(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -143,6 +143,7 @@ extern "C" int itg_destroy(itg_handle* h) {
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->dev_status) cudaFree(h->dev_status);
   if (h->gemv_part) cudaFree(h->gemv_part);
+  if (h->tab_buf) cudaFree(h->tab_buf);
   delete h;
   return ITG_OK;
 }

@@ -452,6 +452,17 @@ k_house_step(double* __restrict__ A, int64_t m, int j, double* __restrict__ Vh, 
   for (int64_t i = j + threadIdx.x; i < m; i += 256) col[i] -= f * (i == j ? 1.0 : x[i] * scale);
 }
 
+}  // namespace
+
+namespace itg {
+void house_step_launch(itg_handle* h, double* A, int64_t m, int j, int ncta, double* Vh, double* tau,
+                       double* rdiag) {
+  k_house_step<<<(unsigned)ncta, 256, 0, h->stream>>>(A, m, j, Vh, tau, rdiag);
+}
+}  // namespace itg
+
+namespace {
+
 // B = R^T (n x n, lower triangular) from the factored A (R above the diagonal, diagonal in rdiag).
 __global__ void k_build_rt(const double* __restrict__ A, int64_t m, int n, const double* __restrict__ rdiag,
                            double* __restrict__ B) {
@@ -462,21 +473,6 @@ __global__ void k_build_rt(const double* __restrict__ A, int64_t m, int n, const
   }
 }
 
-// Y <- (I - tau_j v_j v_j^T) Y for the first `ncols` columns of Y (m rows, ld m).
-__global__ void __launch_bounds__(256)
-k_house_apply(double* __restrict__ Y, int64_t m, int j, const double* __restrict__ Vh,
-              const double* __restrict__ tau) {
-  __shared__ double sh[8];
-  const double tj = tau[j];
-  if (tj == 0.0) return;
-  const double* v = Vh + (int64_t)j * m;
-  double* y = Y + (int64_t)blockIdx.x * m;
-  double w = 0.0;
-  for (int64_t i = j + threadIdx.x; i < m; i += 256) w = fma(v[i], y[i], w);
-  w = block_sum<256>(w, sh);
-  const double f = tj * w;
-  for (int64_t i = j + threadIdx.x; i < m; i += 256) y[i] -= f * v[i];
-}
 
 constexpr int JACOBI_MAX_SWEEPS = 60;
 constexpr int JACOBI_AUX_INTS = 8 + JACOBI_MAX_SWEEPS;
@@ -569,24 +565,6 @@ extern "C" int itg_svd_trunc_ex(itg_handle* h, int64_t m, int64_t n, const doubl
                         legacy_gpu, U, S, V, k, truncerr, docut, method, precision, ISO_NONE);
 }
 
-// Householder QR of the tall matrix X (rows x cols, ld rows) in place:
-// reflectors in Vh, tau; R's diagonal in rd, its strict upper triangle in X.
-static int house_qr(itg_handle* h, double* X, int64_t rows, int64_t cols, double* Vh, double* tau, double* rd) {
-  for (int64_t j = 0; j < cols; ++j)
-    k_house_step<<<(unsigned)(cols - j), 256, 0, h->stream>>>(X, rows, (int)j, Vh, tau, rd);
-  ITG_CHECK_LAUNCH(h);
-  return ITG_OK;
-}
-
-// Y <- H_0 ... H_{cols-1} Y on the first ncols columns of Y (rows x ., ld rows).
-static int house_apply(itg_handle* h, double* Y, int64_t rows, int64_t cols, int64_t ncols, const double* Vh,
-                       const double* tau) {
-  if (ncols <= 0) return ITG_OK;
-  for (int64_t j = cols - 1; j >= 0; --j)
-    k_house_apply<<<(unsigned)ncols, 256, 0, h->stream>>>(Y, rows, (int)j, Vh, tau);
-  ITG_CHECK_LAUNCH(h);
-  return ITG_OK;
-}
 
 // iso: which side of the working matrix W (the tall orientation of A) must
 // come out with exactly orthonormal columns when W is large:
@@ -631,17 +609,21 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
     oWs = take(sizeof(double) * itg::svd_mixed_ws_doubles(mj, nn));
     oWs32 = take(sizeof(float) * (mj * nn + nn * nn));
   }
+  size_t oTq = 0, oTq2 = 0, oQws = 0;
   if (pre) {
     oVh = take(sizeof(double) * mm * nn);
     oTau = take(sizeof(double) * nn);
     oRd = take(sizeof(double) * nn);
     oB = take(sizeof(double) * nn * nn);
+    oTq = take(sizeof(double) * itg::qr_blocked_t_doubles(nn));
+    oQws = take(sizeof(double) * itg::qr_blocked_ws_doubles(nn));
   }
   if (two) {
     oVh2 = take(sizeof(double) * nn * nn);
     oTau2 = take(sizeof(double) * nn);
     oRd2 = take(sizeof(double) * nn);
     oB2 = take(sizeof(double) * nn * nn);
+    oTq2 = take(sizeof(double) * itg::qr_blocked_t_doubles(nn));
   }
   ITG_TRY(itg_scratch_reserve(h, off));
   char* base = (char*)h->scratch;
@@ -665,12 +647,18 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
   double* Vw_dst = tr ? U : V;  // rows nn
   double* J = W;
   double *Vh = nullptr, *tau = nullptr, *Vh2 = nullptr, *tau2 = nullptr;
+  double *Tq = nullptr, *Tq2 = nullptr, *Qws = nullptr;
+  // products of the QR's trailing updates: FP64 (their depth is one 32-column
+  // panel, too shallow for the split path's operand preparation to pay off)
+  const int qr_prec = ITG_PREC_FP64;
   if (pre) {
     Vh = (double*)(base + oVh);
     tau = (double*)(base + oTau);
     double* rd = (double*)(base + oRd);
     J = (double*)(base + oB);
-    ITG_TRY(house_qr(h, W, mm, nn, Vh, tau, rd));
+    Tq = (double*)(base + oTq);
+    Qws = (double*)(base + oQws);
+    ITG_TRY(itg::qr_blocked(h, W, mm, nn, Vh, tau, rd, Tq, Qws, qr_prec));
     k_build_rt<<<itg_blocks_for(nn * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(W, mm, (int)nn, rd, J);
     ITG_CHECK_LAUNCH(h);
     if (two) {
@@ -678,7 +666,8 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
       tau2 = (double*)(base + oTau2);
       double* rd2 = (double*)(base + oRd2);
       double* J2 = (double*)(base + oB2);
-      ITG_TRY(house_qr(h, J, nn, nn, Vh2, tau2, rd2));
+      Tq2 = (double*)(base + oTq2);
+      ITG_TRY(itg::qr_blocked(h, J, nn, nn, Vh2, tau2, rd2, Tq2, Qws, qr_prec));
       k_build_rt<<<itg_blocks_for(nn * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(J, nn, (int)nn, rd2, J2);
       ITG_CHECK_LAUNCH(h);
       J = J2;
@@ -736,8 +725,8 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
   if (pre) {
     // rotate the kept columns back
     const int64_t kk = (k && *k > 0) ? *k : nn;
-    ITG_TRY(house_apply(h, Uw_dst, mm, nn, kk, Vh, tau));
-    if (two) ITG_TRY(house_apply(h, Vw_dst, nn, nn, kk, Vh2, tau2));
+    ITG_TRY(itg::q_apply_blocked(h, Uw_dst, mm, nn, kk, Vh, Tq, Qws));
+    if (two) ITG_TRY(itg::q_apply_blocked(h, Vw_dst, nn, nn, kk, Vh2, Tq2, Qws));
   }
   if (st == ITG_ERR_NOTCONVERGED)
     return itg_fail(h, ITG_ERR_NOTCONVERGED, "Jacobi SVD did not converge in %d sweeps", sweeps);

@@ -17,6 +17,8 @@
 #define ITG_MAX_RANK 16
 #define ITG_PINNED_DOUBLES 4096  // host staging for small results (Davidson subspace <= 32x32)
 #define ITG_GEMV_MAX_PART 65536  // partial sums of itg_gemv_t
+#define QR_NB 32                 // panel width of the blocked Householder QR
+#define QR_NB_MAX 64
 
 // A lowered contraction C[m,n] = sum_k A[m,k] B[k,n] with every operand
 // addressed through offset tables (see itg_contract.cu).
@@ -79,6 +81,8 @@ struct itg_handle {
   void* tune_buf = nullptr;   // throw-away outputs of tuning launches
   size_t tune_buf_bytes = 0;
   int64_t tune_runs = 0;
+  int64_t* tab_buf = nullptr; // offset tables of the blocked QR's submatrix products
+  int64_t tab_buf_elems = 0;
   int last_sweeps = 0;        // Jacobi sweeps of the last SVD / eigh call
   bool last_mixed = false;    // the last SVD finished on the mixed method
   int64_t svd_fallbacks = 0;  // mixed SVDs redone with FP64 Jacobi
@@ -102,6 +106,14 @@ int jacobi_aux_ints(int max_sweeps);
 template <class T>
 int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* aux,
                       int* sweeps);
+// Blocked Householder QR (itg_qr_blocked.cu): panels of QR_NB columns, WY
+// trailing updates through the contraction engine at `precision`.
+int qr_blocked(itg_handle* h, double* W, int64_t m, int64_t n, double* Vh, double* tau, double* rd, double* Tbuf,
+               double* ws, int precision);
+int q_apply_blocked(itg_handle* h, double* Y, int64_t m, int64_t n, int64_t ncols, const double* Vh,
+                    const double* Tbuf, double* ws);
+size_t qr_blocked_ws_doubles(int64_t n);
+size_t qr_blocked_t_doubles(int64_t n);
 // Blocked one-sided Jacobi (itg_jacobi.cu): block pairs staged in shared
 // memory, one launch per block step; ITG_ERR_UNSUPPORTED when m is too large.
 template <class T>

@@ -247,15 +247,17 @@ __global__ void k_scale_cols(double* __restrict__ U, int64_t m, int n, const dou
     U[t] *= inv[t / m];
 }
 
-// out = max |I - P| over the n x n matrix P (NaN propagates as failure)
-__global__ void k_max_offident(const double* __restrict__ P, int n, double* __restrict__ out) {
+// part[block] = max |I - P| over the block's share of the n x n matrix P
+// (+inf when a NaN was seen, so that the max over the partials keeps it);
+// k_max_abs then reduces the partials.
+__global__ void k_max_offident(const double* __restrict__ P, int n, double* __restrict__ part) {
   __shared__ double sh[32];
   __shared__ int bad;
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
   double mx = 0.0;
   const int64_t nn = (int64_t)n * n;
-  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nn; t += (int64_t)gridDim.x * blockDim.x) {
     const int j = (int)(t / n), i = (int)(t - (int64_t)j * n);
     const double v = fabs((i == j ? 1.0 : 0.0) - P[t]);
     if (!(v == v)) bad = 1;
@@ -267,7 +269,7 @@ __global__ void k_max_offident(const double* __restrict__ P, int n, double* __re
   if (threadIdx.x == 0) {
     double b = 0.0;
     for (int i = 0; i < (int)(blockDim.x >> 5); ++i) b = fmax(b, sh[i]);
-    *out = bad ? __longlong_as_double(0x7ff8000000000000ll) : b;
+    part[blockIdx.x] = bad ? __longlong_as_double(0x7ff0000000000000ll) : b;
   }
 }
 
@@ -414,7 +416,13 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
   ITG_TRY(gemm(h, true, nn, nn, nn, 1.0, X, Q, 0.0, S, precision));
   k_refine_lambda<<<itg_blocks_for(nn, 256, 64), 256, 0, h->stream>>>(P, S, n, lam);
   k_max_abs<<<1, 1024, 0, h->stream>>>(lam, n, mx);
-  k_max_offident<<<1, 1024, 0, h->stream>>>(P, n, mx + 1);
+  {
+    // partials in the workspace tail (512 blocks), then the max over them
+    const int64_t sq = nn * nn;
+    double* red = ws + 5 * sq + ((mm * nn > sq) ? mm * nn : sq) + 64;
+    k_max_offident<<<512, 256, 0, h->stream>>>(P, n, red);
+    k_max_abs<<<1, 1024, 0, h->stream>>>(red, 512, mx + 1);
+  }
   ITG_CHECK_LAUNCH(h);
   ITG_CUDA(h, cudaMemcpyAsync(h->pinned, mx, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   ITG_CUDA(h, cudaStreamSynchronize(h->stream));
