@@ -97,7 +97,7 @@ ITG_API int itg_profile_read(itg_handle* h, int kernel, double* total_ms, int64_
  * first use of a shape.  Here the first FP64 contraction of a shape whose
  * 128x128 tiling leaves the GPU under-filled times the tile variants
  * (128x128, 128x64, 64x64) on the call's own operands into a throw-away
- * output, and split contractions time the 256- and 128-wide tcgen05 tiles;
+ * output, and split contractions time the tcgen05 tile variants;
  * grouped launches choose their tile per shape class.  All variants compute
  * bit-identical results (the same k order per output element), so tuning only
  * changes speed.  The choices live in one per-process cache guarded by a
@@ -107,6 +107,10 @@ ITG_API int itg_profile_read(itg_handle* h, int kernel, double* total_ms, int64_
  * enable: 1 (default unless ITG_AUTOTUNE=0 in the environment) or 0
  * (heuristic choice only). */
 enum { ITG_TILE_128x128 = 0, ITG_TILE_128x64 = 1, ITG_TILE_64x64 = 2 };
+/* Split-precision tile variants (split_bn below): 128 and 256 columns, and
+ * 256 columns computed by a 2-CTA cluster that shares its B tile through TMA
+ * multicast. */
+enum { ITG_SPLIT_BN_128 = 128, ITG_SPLIT_BN_256 = 256, ITG_SPLIT_BN_256_PAIR = 257 };
 ITG_API int itg_set_autotune(itg_handle* h, int enable);
 /* entries: size of the process-wide cache; tunings: tuning runs by this handle. */
 ITG_API int itg_autotune_info(itg_handle* h, int64_t* entries, int64_t* tunings);
@@ -117,7 +121,7 @@ ITG_API int itg_autotune_clear(itg_handle* h);
 ITG_API int itg_autotune_query(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA,
                                int rankB, const int64_t* dimsB, const int32_t* modesB, int rankC,
                                const int64_t* dimsC, const int32_t* modesC, int* tile, int* split_bn);
-/* Pin the variants of one shape (tile: ITG_TILE_*, split_bn: 128 or 256; a
+/* Pin the variants of one shape (tile: ITG_TILE_*, split_bn: ITG_SPLIT_BN_*; a
  * negative / zero value leaves that choice alone); stored in the process-wide
  * cache like a tuned choice. */
 ITG_API int itg_autotune_force(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA,

@@ -451,10 +451,11 @@ int itg_split_gemm(itg_handle* h, const ContractPlan& p, const double* A, const 
 // ---------------------------------------------------------- autotuning
 // Per-shape choice of the kernel variant, the counterpart of the reference's
 // algorithm cache (src/cudense.jl:284-326), which times every cuTENSOR
-// algorithm on the first contraction of a (mode, dim) key.  Here only shapes
-// whose default tiling under-fills the GPU are timed (larger ones take the
-// 128x128 / 256-wide tile outright); the launches write into a throw-away
-// buffer so C is untouched.  Variants give bit-identical results.
+// algorithm on the first contraction of a (mode, dim) key.  FP64 shapes whose
+// 128x128 tiling under-fills the GPU are timed (larger ones take 128x128
+// outright); split shapes wider than 128 columns time their three tcgen05
+// variants.  The launches write into a throw-away buffer so C is untouched.
+// Variants give bit-identical results.
 namespace tune {
 
 std::mutex mu;
@@ -606,10 +607,11 @@ int choose_split(itg_handle* h, const ContractPlan& p, const double* A, const do
     bn = p.split_bn;
     return ITG_OK;
   }
-  bn = (p.N <= 128) ? 128 : 256;
-  const int64_t tiles256 = ((p.M + 127) / 128) * ((p.N + 255) / 256);
-  const bool fixed = p.N <= 128 || tiles256 >= 2 * (int64_t)h->num_sms;
-  if (p.key.empty() || fixed) {
+  // heuristic: 128-wide tiles for narrow outputs; otherwise the 2-CTA cluster
+  // sharing its B tile when there are M tiles to pair
+  const bool narrow = p.N <= 128;
+  bn = narrow ? ITG_SPLIT_BN_128 : (p.M > 128 ? ITG_SPLIT_BN_256_PAIR : ITG_SPLIT_BN_256);
+  if (p.key.empty() || narrow) {
     if (!p.key.empty()) p.split_bn = bn;
     return ITG_OK;
   }
@@ -627,7 +629,7 @@ int choose_split(itg_handle* h, const ContractPlan& p, const double* A, const do
   float best = 1e30f;
   int best_bn = bn;
   int st = ITG_OK;
-  for (int cand : {256, 128}) {
+  for (int cand : {ITG_SPLIT_BN_256_PAIR, ITG_SPLIT_BN_256, ITG_SPLIT_BN_128}) {
     float ms = 0.f;
     st = time_variant(h, [&]() { return itg_split_gemm(h, p, A, B, out, alpha, 0.0, cand); }, ms);
     if (st != ITG_OK) break;
@@ -945,7 +947,7 @@ extern "C" int itg_autotune_query(itg_handle* h, int rankA, const int64_t* dimsA
   else *tile = tune::heuristic_tile(h, p.M, p.N);
   if (p.split_bn) *split_bn = p.split_bn;
   else if (tune::lookup("split|" + p.key, v)) *split_bn = v;
-  else *split_bn = p.N <= 128 ? 128 : 256;
+  else *split_bn = p.N <= 128 ? ITG_SPLIT_BN_128 : (p.M > 128 ? ITG_SPLIT_BN_256_PAIR : ITG_SPLIT_BN_256);
   return ITG_OK;
 }
 
@@ -953,7 +955,9 @@ extern "C" int itg_autotune_force(itg_handle* h, int rankA, const int64_t* dimsA
                                   int rankB, const int64_t* dimsB, const int32_t* modesB, int rankC,
                                   const int64_t* dimsC, const int32_t* modesC, int tile, int split_bn) {
   if (!h) return ITG_ERR_INVALID;
-  if (tile > ITG_TILE_64x64 || (split_bn > 0 && split_bn != 128 && split_bn != 256))
+  if (tile > ITG_TILE_64x64 ||
+      (split_bn > 0 && split_bn != ITG_SPLIT_BN_128 && split_bn != ITG_SPLIT_BN_256 &&
+       split_bn != ITG_SPLIT_BN_256_PAIR))
     return itg_fail(h, ITG_ERR_INVALID, "unknown variant (tile %d, split_bn %d)", tile, split_bn);
   if (rankA < 0 || rankB < 0 || rankC < 0 || rankA > ITG_MAX_RANK || rankB > ITG_MAX_RANK || rankC > ITG_MAX_RANK)
     return itg_fail(h, ITG_ERR_UNSUPPORTED, "rank outside 0..%d", ITG_MAX_RANK);

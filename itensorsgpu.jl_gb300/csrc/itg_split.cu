@@ -109,6 +109,25 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
 }
+// Multicast variant: the tile lands at the same shared-memory offset in every
+// CTA of ctaMask, and complete_tx is signalled on the mbarrier at the same
+// offset in each of them.
+__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
@@ -119,6 +138,14 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
+}
+// Commit arriving on the mbarrier at the same offset in every CTA of ctaMask.
+__device__ __forceinline__ void tc_commit_mc(uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(mask)
+      : "memory");
 }
 __device__ __forceinline__ void tc_mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
                                             uint32_t idesc, uint32_t accumulate) {
@@ -303,7 +330,12 @@ struct Smem {
   static constexpr int TOTAL = 1024 /*align slack*/ + NSTAGE * STAGE_BYTES + 256;
 };
 
-template <int BN>
+// MC: 2-CTA cluster along M.  The pair shares its B tile: each CTA loads one
+// half of it with a TMA multicast into both CTAs' stage, so every stage's B
+// bytes come half from each CTA and a stage is refilled only when the MMAs of
+// both CTAs have released it (empty barriers count two commits, sent to both
+// CTAs).  Halves the L2 -> SM traffic of B.
+template <int BN, bool MC>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
              GemmArgs args) {
@@ -322,15 +354,26 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
   uint32_t* tmem_slot = (uint32_t*)(bars + 2 * NST + 6);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile = blockIdx.x;
-  const int m_tile = tile / args.tiles_n, n_tile = tile - m_tile * args.tiles_n;
+  int m_tile, n_tile;
+  uint32_t rank = 0;
+  if (MC) {
+    rank = cluster_ctarank();
+    const int pair = blockIdx.x >> 1;
+    const int m_pair = pair / args.tiles_n;
+    n_tile = pair - m_pair * args.tiles_n;
+    m_tile = 2 * m_pair + (int)rank;  // may be one past the last tile (a zero-filled partner)
+  } else {
+    m_tile = blockIdx.x / args.tiles_n;
+    n_tile = blockIdx.x - m_tile * args.tiles_n;
+  }
+  const int tile = m_tile * args.tiles_n + n_tile;  // accumulator slot
   const int m0 = m_tile * BM, n0 = n_tile * BN;
   constexpr uint32_t TMEM_COLS = TACC ? 512 : 2 * BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], MC ? 2 : 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
@@ -349,6 +392,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  if (MC) cluster_sync_all();  // the partner's barriers exist before any multicast reaches them
   const uint32_t tmem_base = *tmem_slot;
 
   if (warp == 0) {
@@ -366,7 +410,13 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
         uint8_t* sb = sa + Smem<BN>::A_BYTES;
         mbar_arrive_expect_tx(&full[s], Smem<BN>::STAGE_BYTES);
         tma_load_2d(sa, &mapA, sc.kb * BK, sc.p * args.Mpad + m0, &full[s]);
-        tma_load_2d(sb, &mapB, sc.kb * BK, sc.q() * args.Npad + n0, &full[s]);
+        if (MC) {
+          // this CTA's half of the B tile, into both CTAs (rows rank*BN/2 .. +BN/2)
+          tma_load_2d_mc(sb + rank * (Smem<BN>::B_BYTES / 2), &mapB, sc.kb * BK,
+                         sc.q() * args.Npad + n0 + (int)rank * (BN / 2), &full[s], (uint16_t)0x3);
+        } else {
+          tma_load_2d(sb, &mapB, sc.kb * BK, sc.q() * args.Npad + n0, &full[s]);
+        }
         sc.advance();
         ++it;
       }
@@ -403,7 +453,8 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
           const uint32_t accum = (sc.first_in_group && kk == 0) ? 0u : 1u;
           tc_mma_bf16(tmem_d, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), idesc, accum);
         }
-        tc_commit(&empty[s]);
+        if (MC) tc_commit_mc(&empty[s], (uint16_t)0x3);
+        else tc_commit(&empty[s]);
         const bool closes = sc.advance();
         if (closes) tc_commit(&acc_full[b]);
         ++it;
@@ -521,6 +572,9 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                  "r"(TMEM_COLS));
   }
+  // the partner may still multicast into this CTA's stages or arrive on its
+  // barriers until it has left its loops (every wait there is bounded)
+  if (MC) cluster_sync_all();
 }
 
 // ----------------------------------------------------------- slicing
@@ -678,7 +732,7 @@ int make_map(itg_handle* h, CUtensorMap* map, void* base, int64_t inner, int64_t
 
 int ws_reserve(itg_handle* h, size_t bytes);
 
-template <int BN>
+template <int BN, bool MC>
 int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
         double alpha, double beta) {
   constexpr int S = S_SLICES;
@@ -687,7 +741,9 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   const int64_t Kpad = (p.K + BK - 1) / BK * BK;
   if (Mpad * S > (int64_t)INT32_MAX || Npad * S > (int64_t)INT32_MAX || Kpad > (int64_t)INT32_MAX)
     return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: problem too large");
-  const int64_t tiles = (Mpad / BM) * (Npad / BN);
+  // MC pairs M tiles: an odd count gets one zero-filled partner tile
+  const int64_t tiles_m = (Mpad / BM + (MC ? 1 : 0)) / (MC ? 2 : 1) * (MC ? 2 : 1);
+  const int64_t tiles = tiles_m * (Npad / BN);
   // F: fixed-point fraction bits of the int64 accumulator (keeps |acc| < 2^62).
   int lk = 0;
   while (((int64_t)1 << lk) < p.K) ++lk;
@@ -747,7 +803,7 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   }
   CUtensorMap mA, mB;
   ITG_TRY(make_map(h, &mA, sA, Kpad, Mpad * S, BM));
-  ITG_TRY(make_map(h, &mB, sB, Kpad, Npad * S, BN));
+  ITG_TRY(make_map(h, &mB, sB, Kpad, Npad * S, MC ? BN / 2 : BN));
   GemmArgs a;
   a.M = p.M;
   a.N = p.N;
@@ -770,14 +826,30 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   a.err = err;
   static bool attr = false;
   if (!attr) {
-    ITG_CUDA(h, cudaFuncSetAttribute(k_split_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    ITG_CUDA(h, cudaFuncSetAttribute(k_split_gemm<BN, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      Smem<BN>::TOTAL));
     attr = true;
   }
   if (tiles > (int64_t)INT32_MAX) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: too many tiles");
   {
     ProfScope prof(h, ITG_KERNEL_GEMM_SPLIT);
-    k_split_gemm<BN><<<(unsigned)tiles, NUM_THREADS, Smem<BN>::TOTAL, h->stream>>>(mA, mB, a);
+    if (MC) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)tiles);
+      cfg.blockDim = dim3(NUM_THREADS);
+      cfg.dynamicSmemBytes = Smem<BN>::TOTAL;
+      cfg.stream = h->stream;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 2;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      ITG_CUDA(h, cudaLaunchKernelEx(&cfg, k_split_gemm<BN, MC>, mA, mB, a));
+    } else {
+      k_split_gemm<BN, MC><<<(unsigned)tiles, NUM_THREADS, Smem<BN>::TOTAL, h->stream>>>(mA, mB, a);
+    }
   }
   ITG_CHECK_LAUNCH(h);
   // surface a device-side timeout on the next synchronising call
@@ -805,12 +877,14 @@ int ws_reserve(itg_handle* h, size_t bytes) {
 
 }  // namespace split
 
-// bn: tcgen05 tile width, 128 or 256 (0: 128 when N <= 128, else 256).
+// bn: tcgen05 tile variant: 128, 256, or ITG_SPLIT_BN_256_PAIR (256 wide, 2-CTA
+// cluster sharing the B tile); 0: 128 when N <= 128, else 256.
 int itg_split_gemm(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
                    double alpha, double beta, int bn) {
   if (bn == 0) bn = p.N <= 128 ? 128 : 256;
-  if (bn == 128) return split::run<128>(h, p, A, B, C, alpha, beta);
-  return split::run<256>(h, p, A, B, C, alpha, beta);
+  if (bn == 128) return split::run<128, false>(h, p, A, B, C, alpha, beta);
+  if (bn == ITG_SPLIT_BN_256_PAIR) return split::run<256, true>(h, p, A, B, C, alpha, beta);
+  return split::run<256, false>(h, p, A, B, C, alpha, beta);
 }
 
 extern "C" double itg_split_error_bound(int64_t K) {

@@ -67,10 +67,10 @@ def test_every_tile_variant_is_bit_identical(gpu, case):
     assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref)
     # split: both tcgen05 tile widths give identical bits too
     so = []
-    for bn in (256, 128):
+    for bn in (256, 128, 257):  # 257: 256-wide tiles on a 2-CTA cluster sharing B
         h.call("itg_autotune_force", *_shape_args(dA, mA, dB, mB, dC, mC), -1, bn)
         so.append(_contract(h, a, dA, mA, b, dB, mB, dC, mC, prec=1).cpu().numpy())
-    assert np.array_equal(so[0], so[1])
+    assert np.array_equal(so[0], so[1]) and np.array_equal(so[0], so[2])
     h.call("itg_autotune_clear")
 
 
