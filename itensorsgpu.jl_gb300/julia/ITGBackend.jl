@@ -139,6 +139,36 @@ function LinearAlgebra.svd(T::CuDenseTensor{Float64,2,IndsT}; maxdim::Int=minimu
     return Ut, St, Vt, Spectrum(Array(S[1:dS]) .^ 2, te[])
 end
 
+# factorize of an order-2 CuDense tensor (the two-site bond split of dmrg,
+# ITensors' factorize with which_decomp = "svd"): ortho = "left" returns L with
+# orthonormal columns and R = S V^T, ortho = "right" returns L = U S and R
+# with orthonormal rows.  method: 0 auto, 1 FP64 Jacobi, 2 mixed.
+const ITG_ORTHO_LEFT = Cint(0)
+const ITG_ORTHO_RIGHT = Cint(1)
+function factorize_svd(T::CuDenseTensor{Float64,2,IndsT}; ortho::String="left", maxdim::Int=minimum(dims(T)),
+                       mindim::Int=1, cutoff::Float64=0.0, method::Int=0, kwargs...) where {IndsT}
+    m, n = dims(T); r = min(m, n); big = max(m, n) * r
+    Lb = CuVector{Float64}(undef, big); S = CuVector{Float64}(undef, r); Cb = CuVector{Float64}(undef, big)
+    k = Ref{Int64}(); te = Ref{Cdouble}(); dc = Ref{Cdouble}()
+    o = ortho == "left" ? ITG_ORTHO_LEFT : ITG_ORTHO_RIGHT
+    st = ccall((:itg_factorize_trunc, libitg), Cint,
+               (Ptr{Cvoid}, Int64, Int64, CuPtr{Float64}, Int64, Int64, Int64, Cdouble, Cint, Cint, Cint,
+                Cint, Cint, Cint, CuPtr{Float64}, CuPtr{Float64}, CuPtr{Float64}, Ref{Int64}, Ref{Cdouble},
+                Ref{Cdouble}),
+               handle(), m, n, pointer(data(store(T))), m, maxdim, mindim, cutoff, 0, 1, 0, o, method,
+               precision[], pointer(Lb), pointer(S), pointer(Cb), k, te, dc)
+    check(st, "itg_factorize_trunc")
+    dk = k[]; l = eltype(IndsT)(dk)
+    if ortho == "left"
+        Lt = Tensor(Dense(Lb[1:m*dk]), IndsT((ind(T, 1), l)))
+        Rt = Tensor(Dense(Cb[1:dk*n]), IndsT((l, ind(T, 2))))
+    else
+        Lt = Tensor(Dense(Cb[1:m*dk]), IndsT((ind(T, 1), l)))
+        Rt = Tensor(Dense(Lb[1:n*dk]), IndsT((ind(T, 2), l)))
+    end
+    return Lt, Rt, Spectrum(Array(S[1:dk]) .^ 2, te[])
+end
+
 # ProjMPO product + eigensolver for the two-site update: the dmrg driver calls
 # this with the device buffers of L, W1, W2, R and phi.
 function davidson_heff2!(phi::CuVector{Float64}, L, W1, W2, R, chiL, chiR, d, wL, wM, wR;
