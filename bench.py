@@ -559,17 +559,31 @@ def run_svd(args):
     Cm = torch.empty(n * n, dtype=torch.float64, device="cuda")
     k = C.c_int64()
     prec = 1 if args.svd_method == 2 else 0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    h.call("itg_factorize_trunc", C.c_int64(n), C.c_int64(n), p(A), C.c_int64(n), C.c_int64(n // 2), C.c_int64(1),
-           C.c_double(0.0), 0, 1, 0, 0, args.svd_method, prec, p(L), p(S), p(Cm), C.byref(k), None, None)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
+    h.call("itg_set_svd_options", int(args.svd_qr), 0)
+
+    def once():
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h.call("itg_factorize_trunc", C.c_int64(n), C.c_int64(n), p(A), C.c_int64(n), C.c_int64(n // 2),
+               C.c_int64(1), C.c_double(0.0), 0, 1, 0, 0, args.svd_method, prec, p(L), p(S), p(Cm), C.byref(k),
+               None, None)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    # --svd-reps 1 (the profiled command): one cold call; more: one warm-up, best of the rest
+    dt = once() if args.svd_reps <= 1 else min([once() for _ in range(args.svd_reps + 1)][1:])
     sw, mu, fb = C.c_int(), C.c_int(), C.c_int64()
     h.call("itg_svd_info", C.byref(sw), C.byref(mu), C.byref(fb))
+    kk = k.value
+    Lh = L[: n * kk].reshape(kk, n).T.cpu().numpy()
+    Ch = Cm[: kk * n].reshape(n, kk).T.cpu().numpy()
+    iso = float(np.abs(Lh.T @ Lh - np.eye(kk)).max())
+    sv = np.exp(-np.arange(n) / 60.0)
+    rec = float(np.abs(Lh @ Ch - M).max() / sv[kk])
     print(json.dumps({"metric": f"bond factorisation n={n}", "value": dt, "unit": "s", "higher_is_better": False,
-                      "method": "mixed" if args.svd_method == 2 else "fp64 jacobi", "k": k.value,
-                      "jacobi_sweeps": sw.value, "mixed_used": mu.value, "fallbacks": fb.value}), flush=True)
+                      "method": "mixed" if args.svd_method == 2 else "fp64 jacobi", "qr_precondition": args.svd_qr,
+                      "k": kk, "jacobi_sweeps": sw.value, "mixed_used": mu.value, "fallbacks": fb.value,
+                      "isometry_err": iso, "reconstruction_err_over_sigma_k": rec}), flush=True)
     return 0
 
 
@@ -716,6 +730,8 @@ def main():
     ap.add_argument("--learn-test-j2", type=float, default=0.5)
     ap.add_argument("--svd-n", type=int, default=2048)
     ap.add_argument("--svd-method", type=int, default=2, choices=[1, 2])
+    ap.add_argument("--svd-qr", type=int, default=1, choices=[0, 1], help="Householder QR preconditioning")
+    ap.add_argument("--svd-reps", type=int, default=1, help="timed factorisations (after one warm-up if > 1)")
     ap.add_argument("--sweep-n", type=int, default=24,
                     help="chain length of the sweep measurement in the default run (0: skip)")
     ap.add_argument("--batch-count", type=int, default=256)

@@ -95,7 +95,9 @@ k_svd_batched(SvdJob* __restrict__ jobs, double tol_eps, int max_sweeps, int* __
           vp[i] = c * x - s * y;
           vq[i] = s * x + c * y;
         }
-        if (lane == 0) rotated = 1;
+        // converged once no pair above the rounding floor of the dot product
+        // (4 tol, as in the single-matrix kernels) needed a rotation
+        if (lane == 0 && fabs(g) > 4.0 * tol * sqrt(a) * sqrt(b)) rotated = 1;
       }
       __syncthreads();
     }

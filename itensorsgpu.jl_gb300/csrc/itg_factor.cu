@@ -1,5 +1,5 @@
 // Factorisations: on-device truncation (K6), one-sided Jacobi SVD (K5),
-// symmetric eigendecomposition through the shifted SVD, and CGS2 thin QR (K7).
+// symmetric eigendecomposition through the shifted SVD, and the thin Householder QR (K7).
 #include "itg_internal.cuh"
 
 #include <cmath>
@@ -180,6 +180,17 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// A pair is rotated when |g| > tol sqrt(a b); the sweep counts as converged
+// when no rotated pair had |g| > JACOBI_CONV * tol sqrt(a b).  Rotations in
+// between polish pairs near the rounding floor of the dot product (about
+// eps sqrt(m) relative, i.e. tol itself), where they can repeat without
+// making progress; they must not keep the sweep loop running.
+constexpr double JACOBI_CONV = 4.0;
+
+__device__ __forceinline__ bool jacobi_significant(double a, double b, double g, double tol) {
+  return fabs(g) > JACOBI_CONV * tol * sqrt(a) * sqrt(b);
+}
+
 __device__ __forceinline__ bool jacobi_rotation(double a, double b, double g, double tol,
                                                 double& c, double& s) {
   if (a == 0.0 || b == 0.0) return false;
@@ -231,7 +242,7 @@ k_jacobi_onecta(double* __restrict__ W, int64_t m, int n, double* __restrict__ V
             vp[i] = c * x - s * y;
             vq[i] = s * x + c * y;
           }
-          if (lane == 0) rotated = 1;
+          if (lane == 0 && jacobi_significant(a, b, g, tol)) rotated = 1;
         }
       }
       __syncthreads();
@@ -282,7 +293,7 @@ k_jacobi_step(double* __restrict__ W, int64_t m, int n, double* __restrict__ V, 
     vp[i] = c * x - s * y;
     vq[i] = s * x + c * y;
   }
-  if (threadIdx.x == 0) *rotated = 1;
+  if (threadIdx.x == 0 && jacobi_significant(a, b, g, tol)) *rotated = 1;
 }
 
 __global__ void k_identity(int n, double* __restrict__ V) {
@@ -658,7 +669,7 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
     J = (double*)(base + oB);
     Tq = (double*)(base + oTq);
     Qws = (double*)(base + oQws);
-    ITG_TRY(itg::qr_blocked(h, W, mm, nn, Vh, tau, rd, Tq, Qws, qr_prec));
+    ITG_TRY(itg::qr_blocked(h, W, mm, nn, nn, Vh, tau, rd, Tq, Qws, qr_prec));
     k_build_rt<<<itg_blocks_for(nn * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(W, mm, (int)nn, rd, J);
     ITG_CHECK_LAUNCH(h);
     if (two) {
@@ -667,7 +678,7 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
       double* rd2 = (double*)(base + oRd2);
       double* J2 = (double*)(base + oB2);
       Tq2 = (double*)(base + oTq2);
-      ITG_TRY(itg::qr_blocked(h, J, nn, nn, Vh2, tau2, rd2, Tq2, Qws, qr_prec));
+      ITG_TRY(itg::qr_blocked(h, J, nn, nn, nn, Vh2, tau2, rd2, Tq2, Qws, qr_prec));
       k_build_rt<<<itg_blocks_for(nn * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(J, nn, (int)nn, rd2, J2);
       ITG_CHECK_LAUNCH(h);
       J = J2;
@@ -836,59 +847,39 @@ extern "C" int itg_eigh_trunc(itg_handle* h, int64_t n, const double* A, int64_t
 }
 
 // ================================================================== QR
-// Classical Gram-Schmidt with one full re-orthogonalisation (CGS2; Giraud,
-// Langou, Rozloznik 2005): column j is projected against Q[:, :j] twice, so the
-// computed Q is orthonormal to working precision for numerically full-rank A.
-// R's diagonal is non-negative.
+// Householder QR through the blocked factorisation (itg_qr_blocked.cu), so Q
+// has orthonormal columns for any A, rank-deficient included (a zero column
+// gives a zero row of R and a unit column of Q).  A wide matrix (m < n) takes
+// m reflectors applied to all n columns.  Rows of R and columns of Q are then
+// sign-flipped together so that R's diagonal is non-negative.
 
-// h[i] = Q[:, i] . q for i < j   (one block per i)
-__global__ void k_proj(const double* __restrict__ Q, int64_t m, const double* __restrict__ q,
-                       double* __restrict__ hcoef) {
-  __shared__ double sh[32];
-  const double* col = Q + (int64_t)blockIdx.x * m;
-  double s = 0.0;
-  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) s = fma(col[i], q[i], s);
-  s = warp_sum(s);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
-    hcoef[blockIdx.x] = t;
+// R (r x n) from the factored W: R(k, i) = s_k W(k, i) above the diagonal,
+// |rd[k]| on it, 0 below, with s_k the sign of rd[k].
+__global__ void k_extract_r(const double* __restrict__ W, int64_t m, int64_t r, int64_t n,
+                            const double* __restrict__ rd, double* __restrict__ R) {
+  const int64_t total = r * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / r, k = t - i * r;
+    const double sk = rd[k] < 0.0 ? -1.0 : 1.0;
+    R[t] = k < i ? sk * W[k + i * m] : (k == i ? fabs(rd[k]) : 0.0);
   }
 }
 
-// q -= Q[:, :j] h ; racc[:j] += h (done by block 0)
-__global__ void k_cgs_update(const double* __restrict__ Q, int64_t m, int j,
-                             const double* __restrict__ hcoef, double* __restrict__ q,
-                             double* __restrict__ racc) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    double s = q[i];
-    for (int c = 0; c < j; ++c) s = fma(-Q[i + c * m], hcoef[c], s);
-    q[i] = s;
+// Q (m x r) = the first r columns of the identity.
+__global__ void k_eye_cols(double* __restrict__ Q, int64_t m, int64_t r) {
+  const int64_t total = m * r;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = t / m, i = t - j * m;
+    Q[t] = i == j ? 1.0 : 0.0;
   }
-  if (blockIdx.x == 0)
-    for (int c = threadIdx.x; c < j; c += blockDim.x) racc[c] += hcoef[c];
 }
 
-__global__ void k_normalize_col(double* __restrict__ q, int64_t m, double* __restrict__ rjj) {
-  __shared__ double sh[32];
-  __shared__ double nrm;
-  double s = 0.0;
-  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) s = fma(q[i], q[i], s);
-  s = warp_sum(s);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
-    nrm = sqrt(t);
-    *rjj = nrm;
+__global__ void k_sign_cols(double* __restrict__ Q, int64_t m, int64_t r, const double* __restrict__ rd) {
+  const int64_t total = m * r;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = t / m;
+    if (rd[j] < 0.0) Q[t] = -Q[t];
   }
-  __syncthreads();
-  double f = nrm > 0.0 ? 1.0 / nrm : 0.0;
-  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) q[i] *= f;
 }
 
 extern "C" int itg_qr(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda, double* Q,
@@ -897,28 +888,35 @@ extern "C" int itg_qr(itg_handle* h, int64_t m, int64_t n, const double* A, int6
   const int64_t r = m < n ? m : n;
   if (r == 0) return ITG_OK;
   if (r > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "qr: min(m,n) too large");
-  ITG_CUDA(h, cudaMemsetAsync(R, 0, sizeof(double) * r * n, h->stream));
-  ITG_TRY(itg_scratch_reserve(h, sizeof(double) * (size_t)(r + 256)));
-  double* hc = (double*)h->scratch;
-  const int gb = itg_blocks_for(m, 256, h->num_sms * 4);
-  for (int64_t j = 0; j < n; ++j) {
-    const double* a = A + j * lda;
-    double* rcol = R + j * r;
-    if (j < r) {
-      double* q = Q + j * m;
-      ITG_CUDA(h, cudaMemcpyAsync(q, a, sizeof(double) * m, cudaMemcpyDeviceToDevice, h->stream));
-      if (j > 0) {
-        for (int pass = 0; pass < 2; ++pass) {
-          k_proj<<<(unsigned)j, 256, 0, h->stream>>>(Q, m, q, hc);
-          k_cgs_update<<<gb, 256, 0, h->stream>>>(Q, m, (int)j, hc, q, rcol);
-        }
-      }
-      k_normalize_col<<<1, 1024, 0, h->stream>>>(q, m, rcol + j);
-    } else {
-      k_proj<<<(unsigned)r, 256, 0, h->stream>>>(Q, m, a, rcol);
-    }
-    ITG_CHECK_LAUNCH(h);
-  }
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  const size_t oW = take(sizeof(double) * m * n);
+  const size_t oVh = take(sizeof(double) * m * r);
+  const size_t oTau = take(sizeof(double) * r);
+  const size_t oRd = take(sizeof(double) * r);
+  const size_t oT = take(sizeof(double) * itg::qr_blocked_t_doubles(r));
+  const size_t oWs = take(sizeof(double) * itg::qr_blocked_ws_doubles(n));
+  ITG_TRY(itg_scratch_reserve(h, off));
+  char* base = (char*)h->scratch;
+  double* W = (double*)(base + oW);
+  double* Vh = (double*)(base + oVh);
+  double* tau = (double*)(base + oTau);
+  double* rd = (double*)(base + oRd);
+  double* Tq = (double*)(base + oT);
+  double* ws = (double*)(base + oWs);
+  k_copy_matrix<<<itg_blocks_for(m * n, 256, h->num_sms * 16), 256, 0, h->stream>>>(A, lda, m, n, W, 0.0);
+  ITG_CHECK_LAUNCH(h);
+  ITG_TRY(itg::qr_blocked(h, W, m, n, r, Vh, tau, rd, Tq, ws, ITG_PREC_FP64));
+  k_extract_r<<<itg_blocks_for(r * n, 256, h->num_sms * 16), 256, 0, h->stream>>>(W, m, r, n, rd, R);
+  k_eye_cols<<<itg_blocks_for(m * r, 256, h->num_sms * 16), 256, 0, h->stream>>>(Q, m, r);
+  ITG_CHECK_LAUNCH(h);
+  ITG_TRY(itg::q_apply_blocked(h, Q, m, r, r, Vh, Tq, ws));
+  k_sign_cols<<<itg_blocks_for(m * r, 256, h->num_sms * 16), 256, 0, h->stream>>>(Q, m, r, rd);
+  ITG_CHECK_LAUNCH(h);
   return ITG_OK;
 }
 

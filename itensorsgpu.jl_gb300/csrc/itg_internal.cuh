@@ -107,9 +107,10 @@ template <class T>
 int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* aux,
                       int* sweeps);
 // Blocked Householder QR (itg_qr_blocked.cu): panels of QR_NB columns, WY
-// trailing updates through the contraction engine at `precision`.
-int qr_blocked(itg_handle* h, double* W, int64_t m, int64_t n, double* Vh, double* tau, double* rd, double* Tbuf,
-               double* ws, int precision);
+// trailing updates through the contraction engine at `precision`; nref
+// reflectors (nref <= min(m, n)) applied to all n columns.
+int qr_blocked(itg_handle* h, double* W, int64_t m, int64_t n, int64_t nref, double* Vh, double* tau, double* rd,
+               double* Tbuf, double* ws, int precision);
 int q_apply_blocked(itg_handle* h, double* Y, int64_t m, int64_t n, int64_t ncols, const double* Vh,
                     const double* Tbuf, double* ws);
 size_t qr_blocked_ws_doubles(int64_t n);

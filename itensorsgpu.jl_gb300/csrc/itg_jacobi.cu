@@ -10,7 +10,8 @@
 // the rotation).  Same pairing (Brent-Luk round robin), rotation formula and
 // skip rule as the one-CTA and per-step kernels of itg_factor.cu:
 //   zeta = (b - a) / (2g), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)),
-//   c = 1/sqrt(1 + t^2), s = c t;  skip when |g| <= tol sqrt(a) sqrt(b).
+//   c = 1/sqrt(1 + t^2), s = c t;  skip when |g| <= tol sqrt(a) sqrt(b); a
+//   sweep has converged when no rotated pair had |g| > conv_tol(tol) sqrt(a b).
 //
 // Columns move between SMs from step to step, so every load of W and V goes
 // through L2 (ld.global.cg) and stores bypass L1 (st.global.cg); the barrier
@@ -115,7 +116,7 @@ __device__ __forceinline__ void jp_block_sum3(T& a, T& b, T& g, T (*sh)[JP_WARPS
 // pair's columns are read once per step; RC = 0 streams them (any m).
 template <class T, int RC>
 __global__ void __launch_bounds__(JP_THREADS)
-k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T amin, int max_sweeps,
+k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T tol_conv, T amin, int max_sweeps,
                  int* aux) {
   __shared__ T sh[3][JP_WARPS];
   unsigned* count = (unsigned*)aux;
@@ -188,7 +189,7 @@ k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, 
           __stcg(vp + i, c * x - s * y);
           __stcg(vq + i, s * x + c * y);
         }
-        if (t == 0) __stcg(rot + sweep, 1);
+        if (t == 0 && fabs(g) > tol_conv * sqrt(a) * sqrt(b)) __stcg(rot + sweep, 1);
       }
       if (!jp_grid_sync(count, gen, status, gridDim.x)) {
         done = -1;
@@ -217,9 +218,18 @@ k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, 
 // 2 WB columns per CTA through shared memory instead of two per CTA.
 constexpr int JB_THREADS = 512;
 
+// Convergence threshold of a sweep (see the element-wise FP64 kernels): in
+// FP64, pairs rotated with |g| <= 4 tol sqrt(a b) sit at the rounding floor of
+// the dot product and do not keep the sweep loop running.  The FP32 start of
+// the mixed method keeps its plain rule (its tol is far above FP32 rounding).
+template <class T>
+__host__ __device__ inline T conv_tol(T tol) {
+  return sizeof(T) == 8 ? T(4) * tol : tol;
+}
+
 template <class T, int WB>
 __global__ void __launch_bounds__(JB_THREADS)
-k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T amin, int step,
+k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T tol_conv, T amin, int step,
                     int first, int* __restrict__ rotated) {
   constexpr int C2 = 2 * WB;              // local columns
   constexpr int TP = JB_THREADS / WB;     // threads per pair
@@ -228,7 +238,7 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
   T* cols = (T*)jb_smem;                  // [C2][m]
   T* Q = cols + (int64_t)C2 * m;          // [C2][C2], column-major
   T* red = Q + C2 * C2;                   // [WB][WPG][3]
-  __shared__ int any;
+  __shared__ int any, major;
   const int nb = (n + WB - 1) / WB, nbp = nb + (nb & 1);
   const int bi = jp_player(blockIdx.x, step, nbp), bj = jp_player(nbp - 1 - blockIdx.x, step, nbp);
   const int t = threadIdx.x;
@@ -237,7 +247,7 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
     const int gc = blk * WB + (c < WB ? c : c - WB);
     return (blk < nb && gc < n) ? gc : -1;
   };
-  if (t == 0) any = 0;
+  if (t == 0) any = major = 0;
   for (int c = 0; c < C2; ++c) {
     const int gc = gcol(c);
     T* dst = cols + (int64_t)c * m;
@@ -308,7 +318,10 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
         Q[lt + p * C2] = c * x - sn * y;
         Q[lt + q * C2] = sn * x + c * y;
       }
-      if (lt == 0) any = 1;
+      if (lt == 0) {
+        any = 1;
+        if (fabs(gg) > tol_conv * sqrt(a) * sqrt(b)) major = 1;
+      }
     }
     __syncthreads();  // columns, Q and red are reused by the next round
   }
@@ -337,7 +350,7 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
       V[row + (int64_t)gcs[c] * n] = s;
     }
   }
-  if (t == 0) *rotated = 1;
+  if (t == 0 && major) *rotated = 1;
 }
 
 }  // namespace
@@ -352,6 +365,7 @@ int jacobi_aux_ints(int max_sweeps) { return 8 + max_sweeps; }
 // cooperative launch (the caller then uses per-step launches).
 template <class T, int RC>
 int launch_persist(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* aux) {
+  const T tol_conv = conv_tol(tol);
   int per_sm = 0;
   ITG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi_persist<T, RC>, JP_THREADS, 0));
   if (per_sm < 1) return ITG_ERR_UNSUPPORTED;
@@ -361,7 +375,7 @@ int launch_persist(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, i
   if ((int64_t)np / 2 < grid) grid = np / 2;
   if (grid < 1) grid = 1;
   void* args[] = {(void*)&W,   (void*)&m,          (void*)&n,  (void*)&V,
-                  (void*)&tol, (void*)&amin, (void*)&max_sweeps, (void*)&aux};
+                  (void*)&tol, (void*)&tol_conv, (void*)&amin, (void*)&max_sweeps, (void*)&aux};
   ITG_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_jacobi_persist<T, RC>, dim3((unsigned)grid),
                                           dim3(JP_THREADS), args, 0, h->stream));
   return ITG_OK;
@@ -408,7 +422,7 @@ int jb_run(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_s
   for (int sw = 0; sw < max_sweeps; ++sw) {
     ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
     for (int step = 0; step < nbp - 1; ++step)
-      k_jacobi_block_step<T, WB><<<nbp / 2, JB_THREADS, smem, h->stream>>>(W, m, n, V, tol, amin, step,
+      k_jacobi_block_step<T, WB><<<nbp / 2, JB_THREADS, smem, h->stream>>>(W, m, n, V, tol, conv_tol(tol), amin, step,
                                                                           step == 0, flag);
     ITG_CHECK_LAUNCH(h);
     ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));

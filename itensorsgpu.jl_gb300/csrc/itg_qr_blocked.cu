@@ -183,20 +183,21 @@ int skinny_vt_b(itg_handle* h, const double* Vh, int64_t m, int64_t jb, int bw, 
 
 namespace itg {
 
-// Blocked Householder QR of W (m x n, m >= n, ld m) in place: reflectors in
-// Vh (m x n, explicit unit diagonal, zeros above), tau, R's diagonal in rd,
-// its strict upper triangle in W; Tbuf holds QR_NB^2 doubles per panel and ws
-// 2 * QR_NB * n + QR_NB^2 doubles.
-int qr_blocked(itg_handle* h, double* W, int64_t m, int64_t n, double* Vh, double* tau, double* rd, double* Tbuf,
-               double* ws, int precision) {
+// Blocked Householder QR of W (m x n, ld m) in place with nref <= min(m, n)
+// reflectors (nref = n for the tall case, m for a wide matrix): reflectors in
+// Vh (m x nref, explicit unit diagonal, zeros above), tau, R's diagonal in rd,
+// the rest of R's rows above the diagonal in W; Tbuf holds QR_NB^2 doubles
+// per panel of reflectors and ws qr_blocked_ws_doubles(n) doubles.
+int qr_blocked(itg_handle* h, double* W, int64_t m, int64_t n, int64_t nref, double* Vh, double* tau, double* rd,
+               double* Tbuf, double* ws, int precision) {
   const int NB = QR_NB;
   double* Ym = ws;
   double* Z = ws + NB * NB;
   double* Z2 = Z + (int64_t)NB * n;
   double* part = Z2 + (int64_t)NB * n;
   const int64_t part_doubles = QR_PART_CHUNKS * 32 * n;
-  for (int64_t jb = 0, panel = 0; jb < n; jb += NB, ++panel) {
-    const int64_t bw = (n - jb < NB) ? n - jb : NB;
+  for (int64_t jb = 0, panel = 0; jb < nref; jb += NB, ++panel) {
+    const int64_t bw = (nref - jb < NB) ? nref - jb : NB;
     for (int64_t j = jb; j < jb + bw; ++j) house_step_launch(h, W, m, (int)j, (int)(jb + bw - j), Vh, tau, rd);
     ITG_CHECK_LAUNCH(h);
     const int64_t nt = n - jb - bw;

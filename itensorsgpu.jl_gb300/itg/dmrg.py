@@ -172,6 +172,76 @@ def _env_right(h, Rt, Rd, A, Ad, W, Wd, prec):
     return Rn, (a, w, a)
 
 
+def _contract_acc(h, alpha, A, dA, mA, B, dB, mB, out, dC, mC, precision):
+    """out = alpha * (A x B) + out."""
+    h.call("itg_contract", ITG_F64, C.c_double(alpha), _ptr(A), len(dA), i64arr(dA), i32arr(mA),
+           _ptr(B), len(dB), i64arr(dB), i32arr(mB), C.c_double(1.0), _ptr(out), len(dC),
+           i64arr(dC), i32arr(mC), int(precision))
+
+
+def _noise_split(h, phi, shape, Lt, Ld, W1, W1d, W2, W2d, Rt, Rd, ha, noise, maxdim, mindim, cutoff,
+                 legacy, precision):
+    """Bond split through the perturbed density matrix (the noise > 0 path).
+
+    ITensors 0.2's dmrg with noise adds noise * (nt nt^T) to the reduced
+    density matrix of phi, nt being phi with the environment and MPO tensor of
+    the side being kept applied and the MPO link left open (its noiseterm),
+    then keeps the leading eigenvectors of the sum (factorize with
+    which_decomp = "eigen", eigen(::Hermitian), src/tensor/culinearalgebra.jl:74-108).
+    Left-moving half (ha == 1): rho over (a d1), A_b = U, A_{b+1} = U^T phi.
+    Right-moving half: rho over (d2 c), A_{b+1} = V^T, A_b = phi V.
+    Returns (A_b, A_{b+1}, k, truncerr).
+    """
+    a, d1, d2, c = shape
+    w, x = W1d[0], W1d[3]
+    y = W2d[3]
+    if ha == 1:
+        m = a * d1
+        rho = _contract_raw(h, phi, shape, [1, 2, 3, 4], phi, shape, [5, 6, 3, 4], (a, d1, a, d1),
+                            [1, 2, 5, 6], precision)
+        # t1[w, a', s, d2, c] = L[a, w, a'] phi[a, s, d2, c]
+        t1 = _contract_raw(h, Lt, Ld, [1, 7, 5], phi, shape, [1, 2, 3, 4], (w, a, d1, d2, c), [7, 5, 2, 3, 4],
+                           precision)
+        # nt[a', t, x, d2, c] = t1[w, a', s, d2, c] W1[w, t, s, x]
+        nt = _contract_raw(h, t1, (w, a, d1, d2, c), [7, 5, 2, 3, 4], W1, W1d, [7, 6, 2, 8], (a, d1, x, d2, c),
+                           [5, 6, 8, 3, 4], precision)
+        ntd = (a, d1, x, d2, c)
+        _contract_acc(h, noise, nt, ntd, [5, 6, 8, 3, 4], nt, ntd, [9, 10, 8, 3, 4], rho, (a, d1, a, d1),
+                      [5, 6, 9, 10], precision)
+    else:
+        m = d2 * c
+        rho = _contract_raw(h, phi, shape, [1, 2, 3, 4], phi, shape, [1, 2, 5, 6], (d2, c, d2, c),
+                            [3, 4, 5, 6], precision)
+        # t1[a, d1, s, x, c'] = phi[a, d1, s, c] R[c, x, c']
+        t1 = _contract_raw(h, phi, shape, [1, 2, 3, 4], Rt, Rd, [4, 8, 6], (a, d1, d2, y, c), [1, 2, 3, 8, 6],
+                           precision)
+        # nt[t, c', a, d1, w] = t1[a, d1, s, x, c'] W2[w, t, s, x]
+        wm = W2d[0]
+        nt = _contract_raw(h, t1, (a, d1, d2, y, c), [1, 2, 3, 8, 6], W2, W2d, [7, 5, 3, 8],
+                           (d2, c, a, d1, wm), [5, 6, 1, 2, 7], precision)
+        ntd = (d2, c, a, d1, wm)
+        _contract_acc(h, noise, nt, ntd, [5, 6, 1, 2, 7], nt, ntd, [9, 10, 1, 2, 7], rho, (d2, c, d2, c),
+                      [5, 6, 9, 10], precision)
+    D = T.empty_dev(m)
+    U = T.empty_dev(m * m)
+    k = C.c_int64()
+    te = C.c_double()
+    dc = C.c_double()
+    h.call("itg_eigh_trunc", C.c_int64(m), _ptr(rho), C.c_int64(m), C.c_int64(maxdim), C.c_int64(mindim),
+           C.c_double(cutoff), 0, 1, int(legacy), _ptr(D), _ptr(U), C.byref(k), C.byref(te), C.byref(dc))
+    kk = int(k.value)
+    Uk = U[: m * kk]
+    if ha == 1:
+        Ab = Uk.clone()
+        Ab1 = _contract_raw(h, Uk, (a, d1, kk), [1, 2, 7], phi, shape, [1, 2, 3, 4], (kk, d2, c), [7, 3, 4],
+                            precision)
+    else:
+        Ab1 = _permute_raw(h, Uk, (d2, c, kk), [1, 2, 3], [3, 1, 2])
+        Ab = _contract_raw(h, phi, shape, [1, 2, 3, 4], Uk, (d2, c, kk), [3, 4, 7], (a, d1, kk), [1, 2, 7],
+                           precision)
+    return Ab, Ab1, kk, te.value
+
+
 def _orthogonalize_left_end(h, ch: _Chain):
     """Right-orthogonalise sites N-1..1 by QR (orthogonalize!(psi, 1)) and normalise site 0."""
     for j in range(ch.N - 1, 0, -1):
@@ -213,11 +283,12 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
     (itg_davidson_heff2_learned; falls back to the diagonal one when it stalls).
     bond_hook(ctx): called before every eigensolve with a dict of the bond's
     device tensors and dimensions (used to collect training data).
+
+    A sweep with noise(sweeps, sw) > 0 splits each bond through the perturbed
+    density matrix (ITensors' noise term) and itg_eigh_trunc instead of the SVD.
     """
     if isinstance(precision, str):
         precision = {"fp64": PREC_FP64, "split": PREC_SPLIT}[precision.lower()]
-    if any(sweeps.noise(i) > 0 for i in range(sweeps.nsweep)):
-        raise NotImplementedError("noise > 0 (density-matrix perturbation) is not supported")
     h = T._h()
     N = len(psi0)
     if len(H) != N:
@@ -294,6 +365,21 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
             energy = e.value
             nmv_tot += nmv.value
             tp = tick("eig", tp)
+            nz = sweeps.noise(sw)
+            if nz > 0:
+                Ab, Ab1, kk, te_v = _noise_split(h, phi, (a, d1, d2, c), Lt, Ld, W1, W1d, W2, W2d, Rt, Rd, ha,
+                                                 nz, maxdim, mindim, cutoff, legacy_gpu_truncate, precision)
+                tp = tick("svd", tp)
+                maxerr = max(maxerr, te_v)
+                schmidt[b + 1] = None
+                ch.A[b], ch.Ad[b] = Ab, (a, d1, kk)
+                ch.A[b + 1], ch.Ad[b + 1] = Ab1, (kk, d2, c)
+                if ha == 1:
+                    Lenv[b + 1] = _env_left(h, Lt, Ld, ch.A[b], ch.Ad[b], W1, W1d, precision)
+                else:
+                    Renv[b + 1] = _env_right(h, Rt, Rd, ch.A[b + 1], ch.Ad[b + 1], W2, W2d, precision)
+                tick("env", tp)
+                continue
             # bond split of phi as (a d1) x (d2 c): one orthonormal factor
             # (left-moving half: A_b; right-moving: A_{b+1}), the other one
             # carries S (itg_factorize_trunc)
@@ -350,7 +436,7 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
     links = [Index(1, "Link,l=0")] + [Index(ch.Ad[j][2], f"Link,l={j + 1}") for j in range(N - 1)] + \
             [Index(1, f"Link,l={N}")]
     ts = [ITensor(Dense(ch.A[j]), (links[j], psi0.sites[j], links[j + 1])) for j in range(N)]
-    psi = MPS(ts, psi0.sites, 0, 1)
+    psi = MPS(ts, psi0.sites, -1, 1)
     if return_result:
         res = DMRGResult(energy, psi, records)
         res.fallbacks = fallbacks_total

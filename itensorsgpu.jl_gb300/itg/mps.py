@@ -20,6 +20,7 @@ import ctypes as C
 import numpy as np
 
 from . import tensor as T
+from ._lib import DimensionMismatch
 from .tensor import ITensor, Index, Dense, cu, cpu
 
 
@@ -37,7 +38,67 @@ def spin_ops(d: int):
     return {"Id": np.eye(d), "Sz": Sz, "S+": Sp, "S-": Sm, "Sx": Sx}
 
 
-def siteinds(kind: str, N: int):
+_QUBIT_GATES = {
+    "X": np.array([[0.0, 1.0], [1.0, 0.0]]),
+    "Z": np.diag([1.0, -1.0]),
+    "H": np.array([[1.0, 1.0], [1.0, -1.0]]) / np.sqrt(2.0),
+    "I": np.eye(2),
+}
+
+
+def _two_site_gate(name: str) -> np.ndarray:
+    """4 x 4 matrix on (s1 s2) with s1 the slower index, basis |0>, |1>."""
+    if name in ("CNOT", "CX"):
+        g = np.eye(4)
+        g[2:, 2:] = [[0.0, 1.0], [1.0, 0.0]]
+        return g
+    if name == "CZ":
+        return np.diag([1.0, 1.0, 1.0, -1.0])
+    if name == "SWAP":
+        return np.eye(4)[[0, 2, 1, 3]]
+    raise KeyError(name)
+
+
+def op(name: str, *sites, matrix=None):
+    """Device operator ITensor with indices (s1', ..., sk', s1, ..., sk).
+
+    One-site names: the spin operators "Id", "Sz", "S+", "S-", "Sx" of the
+    site's spin and the qubit gates "X", "Z", "H", "I"; two-site qubit gates:
+    "CNOT" ("CX"), "CZ", "SWAP".  `matrix` gives any real d^k x d^k matrix
+    instead, rows and columns ordered with s1 the slowest index (the order of
+    a Kronecker product).  Mirrors op / op_matrix of examples/gate_evolution.jl.
+    """
+    k = len(sites)
+    d = [s.dim for s in sites]
+    if matrix is None:
+        if k == 1:
+            tab = dict(spin_ops(d[0]))
+            if d[0] == 2:
+                tab.update(_QUBIT_GATES)
+            matrix = tab[name]
+        elif k == 2 and d == [2, 2]:
+            matrix = _two_site_gate(name)
+        else:
+            raise KeyError(f"op: no built-in {name!r} on {k} sites of dimensions {d}")
+    M = np.asarray(matrix, dtype=np.float64).reshape(d + d)    # [s1'..sk', s1..sk], s1 slowest
+    return T.cuITensor(M, *[s.prime() for s in sites], *sites)
+
+
+def ops(sites, specs):
+    """[op(name, sites[n]) for (name, n) in specs] (n 0-based; a tuple of
+    site numbers for multi-site gates)."""
+    out = []
+    for name, n in specs:
+        ns = n if isinstance(n, (tuple, list)) else (n,)
+        out.append(op(name, *[sites[j] for j in ns]))
+    return out
+
+
+def siteinds(kind, N: int | None = None):
+    """N site indices of a named kind ("S=1/2", "S=1", "Qubit"), or the site
+    indices of an MPS / MPO when called with one."""
+    if isinstance(kind, (MPS, MPO)):
+        return list(kind.sites)
     d = {"S=1/2": 2, "S=1": 3, "Qubit": 2, "qubit": 2}[kind]
     return [Index(d, f"{kind},Site,n={j + 1}") for j in range(N)]
 
@@ -87,11 +148,25 @@ class MPS:
     def _cpu(self):
         return MPS([cpu(t) for t in self.tensors], self.sites, self.llim, self.rlim)
 
+    def prime(self, n: int = 1):
+        """Every index (sites and links) raised n prime levels."""
+        return MPS([T.prime(t, n) for t in self.tensors], [s.prime(n) for s in self.sites],
+                   self.llim, self.rlim)
+
+    def __str__(self):
+        return _show("MPS", self.tensors)
+
+    def __add__(self, other):
+        from .mpsops import add
+        return add(self, other)
+
 
 class MPO:
-    def __init__(self, tensors, sites):
+    def __init__(self, tensors, sites, llim: int = -1, rlim: int | None = None):
         self.tensors = list(tensors)
         self.sites = list(sites)
+        self.llim = llim
+        self.rlim = len(self.tensors) if rlim is None else rlim
 
     def __len__(self):
         return len(self.tensors)
@@ -99,25 +174,78 @@ class MPO:
     def __getitem__(self, j):
         return self.tensors[j]
 
+    def __setitem__(self, j, v):
+        self.tensors[j] = v
+
     @property
     def is_cuda(self):
         return all(t.is_cuda for t in self.tensors)
 
+    def linkdims(self):
+        return [t.dims[-1] for t in self.tensors[:-1]]
+
+    def maxlinkdim(self):
+        return max(self.linkdims(), default=1)
+
+    def copy(self):
+        return MPO([t.copy() for t in self.tensors], self.sites, self.llim, self.rlim)
+
+    def prime(self, n: int = 1):
+        """Every index (sites and links) raised n prime levels."""
+        return MPO([T.prime(t, n) for t in self.tensors], [s.prime(n) for s in self.sites],
+                   self.llim, self.rlim)
+
+    def __str__(self):
+        return _show("MPO", self.tensors)
+
+    def __add__(self, other):
+        from .mpsops import add
+        return add(self, other)
+
     def _cu(self):
-        return MPO([cu(t) for t in self.tensors], self.sites)
+        return MPO([cu(t) for t in self.tensors], self.sites, self.llim, self.rlim)
 
     def _cpu(self):
-        return MPO([cpu(t) for t in self.tensors], self.sites)
+        return MPO([cpu(t) for t in self.tensors], self.sites, self.llim, self.rlim)
 
 
-def cuMPS(x):
-    """Device copy of an MPS (cuMPS(::MPS), src/mps/cumps.jl:1-7)."""
-    return cu(x)
+def _show(kind, tensors):
+    """One header line, one line per site, and a closing newline (show(::MPS))."""
+    lines = [kind] + [f"[{j + 1}] " + ", ".join(f"({i.dim}|{i.tags}|{i.plev})" for i in t.inds)
+                      for j, t in enumerate(tensors)]
+    return "\n".join(lines) + "\n"
 
 
-def cuMPO(x):
-    """Device copy of an MPO (cuMPO(::MPO), src/mps/cumpo.jl:1-7)."""
-    return cu(x)
+def cuMPS(x=None, states=None):
+    """Device MPS (src/mps/cumps.jl:1-43,99-134).
+
+    cuMPS() is empty; cuMPS(psi) copies an MPS to the device; cuMPS(sites) is
+    the zero MPS with dimension-1 links; cuMPS(sites, states) is a product
+    state, and a states list of the wrong length raises DimensionMismatch.
+    """
+    if x is None:
+        return MPS([], [])
+    if isinstance(x, MPS):
+        return cu(x)
+    sites = list(x)
+    if states is not None:
+        return productCuMPS(sites, states)
+    N = len(sites)
+    L = _links(N, [1] * (N - 1))
+    return MPS([T.cuITensor(L[j], s, L[j + 1]) for j, s in enumerate(sites)], sites, -1, N)
+
+
+def cuMPO(x=None):
+    """Device MPO (src/mps/cumpo.jl:1-13): cuMPO() is empty, cuMPO(H) copies
+    an MPO to the device, cuMPO(sites) is the zero MPO with dimension-1 links."""
+    if x is None:
+        return MPO([], [])
+    if isinstance(x, MPO):
+        return cu(x)
+    sites = list(x)
+    N = len(sites)
+    W = [Index(1, f"Link,w={j}") for j in range(N + 1)]
+    return MPO([T.cuITensor(W[j], s.prime(), s, W[j + 1]) for j, s in enumerate(sites)], sites)
 
 
 def _links(N, dims):
@@ -139,8 +267,9 @@ def randomCuMPS(sites, linkdim: int = 1, seed: int = 1234):
     """Random device MPS (randomCuMPS, src/mps/cumps.jl:44-53).
 
     Site j is filled with N(0,1) numbers from the library's Philox stream
-    (seed, offset j), so the CPU oracle can rebuild the same tensors.  The
-    state is not normalised or orthogonalised here; dmrg() does both.
+    (seed, offset j), so the CPU oracle can rebuild the same tensors, and is
+    then scaled to unit norm (randn! + normalize! per site).  The state as a
+    whole is not normalised or orthogonalised here; dmrg() does both.
     """
     N = len(sites)
     ld = random_linkdims(sites, linkdim)
@@ -152,6 +281,9 @@ def randomCuMPS(sites, linkdim: int = 1, seed: int = 1234):
         n = T.dim(inds)
         t = T.empty_dev(n)
         h.call("itg_random_normal", C.c_int64(n), C.c_uint64(seed), C.c_uint64(j), T._ptr(t))
+        nrm = C.c_double()
+        h.call("itg_nrm2", C.c_int64(n), T._ptr(t), C.byref(nrm))
+        h.call("itg_scal", C.c_int64(n), C.c_double(1.0 / nrm.value), T._ptr(t))
         ts.append(ITensor(Dense(t), inds))
     return MPS(ts, sites, -1, N)
 
@@ -163,6 +295,8 @@ def productMPS_host(sites, states):
         states = [states(j + 1) for j in range(N)]
     if isinstance(states, str):
         states = [states] * N
+    if len(states) != N:
+        raise DimensionMismatch(2, f"{len(states)} initial states for {N} sites")
     L = _links(N, [1] * (N - 1))
     ts = []
     for j, s in enumerate(sites):

@@ -109,7 +109,10 @@ def dim(inds) -> int:
 
 
 def prime(x, n: int = 1):
+    """Raise every index of an Index, ITensor, MPS or MPO by n prime levels."""
     if isinstance(x, Index):
+        return x.prime(n)
+    if not isinstance(x, ITensor) and hasattr(x, "prime"):
         return x.prime(n)
     return x.replaceinds(x.inds, [i.prime(n) for i in x.inds])
 
@@ -366,6 +369,10 @@ def _axpby(alpha: float, a: ITensor, beta: float, b: ITensor) -> ITensor:
 
 
 def norm(t: ITensor) -> float:
+    """Frobenius norm of an ITensor, or the norm of an MPS."""
+    if not isinstance(t, ITensor):
+        from .mpsops import norm as _norm_chain
+        return _norm_chain(t)
     _require_cuda(t)
     if t.isdiag():
         d = t.store.data
@@ -390,8 +397,15 @@ def dense(t: ITensor) -> ITensor:
     return ITensor(Dense(out), t.inds)
 
 
-def contract(A: ITensor, B: ITensor, precision: int | None = None) -> ITensor:
-    """A * B: contract all common indices; result indices = A's uncommon then B's."""
+def contract(A: ITensor, B: ITensor, precision: int | None = None, **kw) -> ITensor:
+    """A * B: contract all common indices; result indices = A's uncommon then B's.
+
+    With an MPO first argument this is the MPO x MPS / MPO x MPO product of
+    itg.mpsops.contract (keywords method, maxdim, cutoff, ...).
+    """
+    if not isinstance(A, ITensor):
+        from .mpsops import contract as _contract_chain
+        return _contract_chain(A, B, **kw)
     _require_cuda(A, B)
     common = [i for i in A.inds if i in B.inds]
     out_inds = tuple([i for i in A.inds if i not in common] + [i for i in B.inds if i not in common])

@@ -426,6 +426,16 @@ def mpo_matrix(Ws):
     return M[:, :, 0]
 
 
+def mps_vector(As):
+    """Full state vector of a small MPS given as (l, s, r) arrays; site 0 is the
+    slowest index, as in mpo_matrix."""
+    v = As[0][0]                                    # (s, r)
+    for A in As[1:]:
+        v = np.einsum("ar,rsb->asb", v, A)
+        v = v.reshape(-1, A.shape[2])
+    return v[:, 0]
+
+
 # ------------------------------------------------------------ random MPS
 def random_mps(dims_site, linkdim, seed):
     N = len(dims_site)
@@ -439,7 +449,7 @@ def random_mps(dims_site, linkdim, seed):
     for j in range(N):
         shape = (chis[j], dims_site[j], chis[j + 1])
         x = philox_normal(int(np.prod(shape)), seed, j)
-        out.append(unflat(x, shape))
+        out.append(unflat(x / np.linalg.norm(x), shape))   # randn! + normalize!, cumps.jl:44-53
     return out
 
 
@@ -452,9 +462,34 @@ def _env_right(R, A, W):
     return np.einsum("asb,wtsx,bxd,ctd->awc", A, W, R, A, optimize=True)
 
 
+def _noise_split(M, phi, L, W1, W2, R, ha, noise, maxdim, mindim, cutoff, legacy):
+    """Bond split through the perturbed reduced density matrix (ITensors 0.2's
+    dmrg with noise > 0: noiseterm, then factorize with which_decomp="eigen").
+
+    Left-moving half: rho = M M^T + noise * nt nt^T over (a d1), with
+    nt[a', t, x, d2, c] = sum L[a, w, a'] W1[w, t, s, x] phi[a, s, d2, c].
+    Right-moving half: rho = M^T M + noise * nt nt^T over (d2 c), with
+    nt[t, c', a, d1, w] = sum phi[a, d1, s, c] W2[w, t, s, x] R[c, x, c'].
+    Returns (left factor, right factor, truncerr).
+    """
+    a, d1, d2, c = phi.shape
+    if ha == 1:
+        nt = np.einsum("awc,wtsx,asdb->ctxdb", L, W1, phi, optimize=True)
+        ntm = nt.reshape(a * d1, -1, order="F")
+        rho = M @ M.T + noise * (ntm @ ntm.T)
+        D, U, te, _ = eigh_trunc(rho, maxdim=maxdim, mindim=mindim, cutoff=cutoff, legacy_gpu=legacy)
+        return U, U.T @ M, te
+    nt = np.einsum("akdb,wtdx,bxe->tekaw", phi, W2, R, optimize=True)
+    ntm = nt.reshape(d2 * c, -1, order="F")
+    rho = M.T @ M + noise * (ntm @ ntm.T)
+    D, V, te, _ = eigh_trunc(rho, maxdim=maxdim, mindim=mindim, cutoff=cutoff, legacy_gpu=legacy)
+    return M @ V, V.T, te
+
+
 def dmrg(Ws, As, maxdims, cutoffs, nsweep, mindim=1, krylovdim=3, maxiter=2, tol=1e-14,
-         legacy_gpu_truncate=False, return_sweeps=False):
-    """Two-site DMRG, the same schedule and solver as itg.dmrg.dmrg."""
+         legacy_gpu_truncate=False, return_sweeps=False, noises=None):
+    """Two-site DMRG, the same schedule and solver as itg.dmrg.dmrg; a sweep
+    with noise > 0 splits bonds through the perturbed density matrix."""
     N = len(As)
     A = [a.copy() for a in As]
     # right-orthogonalise by QR from the right, normalise site 0
@@ -488,6 +523,19 @@ def dmrg(Ws, As, maxdims, cutoffs, nsweep, mindim=1, krylovdim=3, maxiter=2, tol
             energy, x, _ = davidson(mv, flat(phi), dg, krylovdim, maxiter, tol)
             a, d1, d2, c = shape
             M = unflat(x, (a * d1, d2 * c))
+            nz = at(noises, sw) if noises else 0.0
+            if nz > 0:
+                Lf, Rf, te = _noise_split(M, unflat(x, shape), L, W1, W2, R, ha, nz, maxdim, mindim, cutoff,
+                                          legacy_gpu_truncate)
+                maxerr = max(maxerr, te)
+                k = Lf.shape[1]
+                A[b] = Lf.reshape(a, d1, k, order="F")
+                A[b + 1] = Rf.reshape(k, d2, c, order="F")
+                if ha == 1:
+                    Lenv[b + 1] = _env_left(L, A[b], W1)
+                else:
+                    Renv[b + 1] = _env_right(R, A[b + 1], W2)
+                continue
             U, S, V, te, _ = svd_trunc(M, maxdim=maxdim, mindim=mindim, cutoff=cutoff,
                                        legacy_gpu=legacy_gpu_truncate)
             maxerr = max(maxerr, te)

@@ -6,8 +6,9 @@
   cutoff 1e-10, Davidson maxiter 2): energy vs the oracle's DMRG and vs exact
   diagonalisation;
 * the reference's own DMRG known answers (test/dmrg.jl): critical TFIM N=32
-  closed form within 1e-2 relative, S=1 Heisenberg N=10 energy < -12
-  (noise is 0 here: the density-matrix noise term is not implemented);
+  closed form within 1e-2 relative, S=1 Heisenberg N=10 energy < -12, with
+  noise 0 and with the reference's noise 1e-10 (density-matrix bond split);
+* the noise path against the oracle's restatement and exact diagonalisation;
 * MPS utilities: product states, inner, expectation energy.
 """
 import ctypes as C
@@ -211,6 +212,39 @@ def test_dmrg_spin1_bound(gpu):
     sw = gpu.Sweeps(g["nsweep"], maxdim=g["maxdim"], mindim=g["mindim"], cutoff=[g["cutoff"]])
     energy, psi = gpu.dmrg(H, psi0, sw)
     assert energy < g["energy_below"]
+
+
+def test_dmrg_noise_matches_oracle_and_ed(gpu):
+    """noise > 0: bonds split through the perturbed density matrix and
+    itg_eigh_trunc; the oracle restates ITensors' noise term in NumPy."""
+    N = 10
+    sites = gpu.siteinds("S=1/2", N)
+    H = gpu.cuMPO(gpu.heisenberg_mpo(sites))
+    noises = [1e-5, 1e-7, 1e-9, 0.0]
+    sw = gpu.Sweeps(5, maxdim=[10, 20, 40, 64], cutoff=[1e-12], noise=noises)
+    res = gpu.dmrg(H, gpu.randomCuMPS(sites, 4, seed=7), sw, return_result=True)
+    e_o, _ = O.dmrg(O.heisenberg_mpo(N), O.random_mps([2] * N, 4, 7), [10, 20, 40, 64], [1e-12], 5,
+                    noises=noises)
+    assert abs(res.energy - e_o) < 1e-9
+    assert abs(res.energy - O.heisenberg_ed_sz0(N)) < 1e-9
+    assert abs(gpu.expect_energy(H, res.psi) - res.energy) < 1e-9
+
+
+def test_dmrg_reference_cases_with_noise(gpu):
+    """test/dmrg.jl as written: both known answers with noise!(sweeps, 1E-10)."""
+    g = GOLD["dmrg"]["spin1_heisenberg"]
+    sites = gpu.siteinds("S=1", g["N"])
+    H = gpu.cuMPO(gpu.heisenberg_mpo(sites))
+    sw = gpu.Sweeps(g["nsweep"], maxdim=g["maxdim"], mindim=g["mindim"], cutoff=[g["cutoff"]], noise=[1e-10])
+    energy, _ = gpu.dmrg(H, gpu.randomCuMPS(sites, 1, seed=11), sw)
+    assert energy < g["energy_below"]
+    g = GOLD["dmrg"]["tfim"]
+    sites = gpu.siteinds("S=1/2", g["N"])
+    H = gpu.cuMPO(gpu.tfim_mpo(sites, h=g["h"], J=g["J"]))
+    sw = gpu.Sweeps(g["nsweep"], maxdim=g["maxdim"], cutoff=[g["cutoff"]], noise=[1e-10])
+    energy, _ = gpu.dmrg(H, gpu.randomCuMPS(sites, 1, seed=g["seed"]), sw)
+    exact = O.tfim_closed_form(g["N"])
+    assert abs((energy - exact) / exact) < g["rel_tol"]
 
 
 def test_product_state_and_inner(gpu):

@@ -125,3 +125,28 @@ def test_split_dmrg_energy_matches_fp64(gpu):
     e64, _ = gpu.dmrg(H, psi0, sw, precision="fp64")
     esp, _ = gpu.dmrg(H, psi0, sw, precision="split")
     assert abs(esp - e64) < 1e-9
+
+
+def test_chosen_form_keeps_mps_orthonormal(gpu):
+    """Split products + mixed SVD (bond splits through FP32 Jacobi, FP64
+    refinement and Newton-Schulz): every site right of the centre stays
+    right-orthonormal to 1e-13 after the sweeps.  Bond dimensions reach 256, so
+    the splits go through the blocked FP32 Jacobi on 512-column matrices; the
+    sweep builds its environments assuming this orthonormality, and a loss of
+    delta would show up as a relative energy error of about N * delta."""
+    N = 24
+    sites = gpu.siteinds("S=1/2", N)
+    H = gpu.cuMPO(gpu.heisenberg_mpo(sites))
+    sw = gpu.Sweeps(3, maxdim=[64, 256], cutoff=[0.0])
+    res = gpu.dmrg(H, gpu.randomCuMPS(sites, 16, seed=5), sw, precision="split", svd_method=2,
+                   return_result=True)
+    psi = res.psi
+    assert psi.maxlinkdim() == 256
+    worst = 0.0
+    for j in range(1, N):
+        t = psi[j]
+        l = t.inds[0]
+        P = (t * t.replaceinds([l], [l.prime()])).array(l, l.prime())
+        worst = max(worst, np.abs(P - np.eye(l.dim)).max())
+    assert worst < 1e-13, worst
+    assert abs(gpu.expect_energy(H, psi) - res.energy) < 1e-11

@@ -132,3 +132,17 @@ def test_oracle_dmrg_spin1_bound():
     A = O.random_mps([3] * N, 1, seed=11)
     e, _ = O.dmrg(Ws, A, g["maxdim"], [g["cutoff"]], g["nsweep"])
     assert e < g["energy_below"]
+
+
+@pytest.mark.slow
+def test_oracle_dmrg_noise_path_vs_ed():
+    """The density-matrix (noise > 0) bond split reaches the same ground state,
+    and the spin-1 known answer holds with the reference's noise 1e-10."""
+    N = 10
+    e, _ = O.dmrg(O.heisenberg_mpo(N), O.random_mps([2] * N, 4, 7), [10, 20, 40, 64], [1e-12], 5,
+                  noises=[1e-5, 1e-7, 1e-9, 0.0])
+    assert e == pytest.approx(O.heisenberg_ed_sz0(N), abs=1e-9)
+    g = GOLD["dmrg"]["spin1_heisenberg"]
+    e, _ = O.dmrg(O.heisenberg_mpo(g["N"], d=3), O.random_mps([3] * g["N"], 1, seed=11), g["maxdim"],
+                  [g["cutoff"]], g["nsweep"], noises=[1e-10])
+    assert e < g["energy_below"]
