@@ -561,12 +561,17 @@ def run_svd(args):
     prec = 1 if args.svd_method == 2 else 0
     h.call("itg_set_svd_options", int(args.svd_qr), 0)
 
+    converged = [True]
+
     def once():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        h.call("itg_factorize_trunc", C.c_int64(n), C.c_int64(n), p(A), C.c_int64(n), C.c_int64(n // 2),
-               C.c_int64(1), C.c_double(0.0), 0, 1, 0, 0, args.svd_method, prec, p(L), p(S), p(Cm), C.byref(k),
-               None, None)
+        try:
+            h.call("itg_factorize_trunc", C.c_int64(n), C.c_int64(n), p(A), C.c_int64(n), C.c_int64(n // 2),
+                   C.c_int64(1), C.c_double(0.0), 0, 1, 0, 0, args.svd_method, prec, p(L), p(S), p(Cm),
+                   C.byref(k), None, None)
+        except _lib.NotConverged:
+            converged[0] = False   # factors are still written; reported below
         torch.cuda.synchronize()
         return time.perf_counter() - t0
 
@@ -582,7 +587,8 @@ def run_svd(args):
     rec = float(np.abs(Lh @ Ch - M).max() / sv[kk])
     print(json.dumps({"metric": f"bond factorisation n={n}", "value": dt, "unit": "s", "higher_is_better": False,
                       "method": "mixed" if args.svd_method == 2 else "fp64 jacobi", "qr_precondition": args.svd_qr,
-                      "k": kk, "jacobi_sweeps": sw.value, "mixed_used": mu.value, "fallbacks": fb.value,
+                      "k": kk, "jacobi_sweeps": sw.value, "converged": converged[0], "mixed_used": mu.value,
+                      "fallbacks": fb.value,
                       "isometry_err": iso, "reconstruction_err_over_sigma_k": rec}), flush=True)
     return 0
 

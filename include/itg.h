@@ -51,7 +51,13 @@ enum {
   ITG_ERR_UNSUPPORTED = 7   /* valid request the library does not implement     */
 };
 
-enum { ITG_F64 = 0 };
+/* Element types.  ITG_C64 is complex FP64 stored interleaved (re, im): the
+ * layout of Julia's ComplexF64, C99 double _Complex and torch.complex128.
+ * itg_contract, itg_permute, itg_axpby_permuted and itg_diag_contract (a real
+ * diagonal times a complex dense tensor) take either; their real alpha and
+ * beta scale both parts.  Complex ranks are limited to 14 in contractions and
+ * 15 elsewhere (the re/im parts run as extra modes of the real engine). */
+enum { ITG_F64 = 0, ITG_C64 = 1 };
 
 /* Arithmetic used by itg_contract.
  *  ITG_PREC_FP64  : native FP64 FMA; relative Frobenius error ~ K * 2^-53.
@@ -153,6 +159,46 @@ ITG_API int itg_contract(itg_handle* h, int dtype, double alpha,
                  double beta,
                  void* C, int rankC, const int64_t* dimsC, const int32_t* modesC,
                  int precision);
+
+/* Complex and mixed contraction: dtypeA, dtypeB each ITG_F64 or ITG_C64 (C is
+ * ITG_C64 when either is); alpha and beta are complex, two doubles (re, im)
+ * each: C = alpha * A * B + beta * C.  A complex x complex product runs as one
+ * real contraction of twice the rows and depth (the smaller operand expanded
+ * into its 2 x 2 real representation); complex x real passes the re/im mode
+ * through.  Replaces contract!! on CuDense{ComplexF64} and mixed real/complex
+ * operands (src/tensor/cudense.jl:83-110; test/test_cucontract.jl:9,
+ * test/test_cudiag.jl:54). */
+ITG_API int itg_contract_z(itg_handle* h, int dtypeA, int dtypeB, const double* alpha,
+                   const void* A, int rankA, const int64_t* dimsA, const int32_t* modesA,
+                   const void* B, int rankB, const int64_t* dimsB, const int32_t* modesB,
+                   const double* beta,
+                   void* C, int rankC, const int64_t* dimsC, const int32_t* modesC,
+                   int precision);
+
+/* Truncated SVD of the complex m x n matrix A (ITG_C64, leading dimension
+ * lda): A ~ U diag(S) V^H with U m x r, V n x r complex, S real descending,
+ * r = min(m, n) columns written and *k kept (same truncation keywords as
+ * itg_svd_trunc).  One-sided complex Jacobi.  Replaces svd on
+ * CuDenseTensor{ComplexF64} (src/tensor/culinearalgebra.jl:33-72). */
+ITG_API int itg_svd_trunc_z(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
+                    int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff, int doRelCutoff,
+                    int legacy_gpu, double* U, double* S, double* V, int64_t* k, double* truncerr,
+                    double* docut);
+
+/* Thin QR of the complex m x n matrix A: A = Q R, Q m x r with orthonormal
+ * columns, R r x n, r = min(m, n) (complex Gram-Schmidt, re-orthogonalised
+ * once).  Replaces qr on CuDenseTensor{ComplexF64}
+ * (src/tensor/culinearalgebra.jl:110-121). */
+ITG_API int itg_qr_z(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda, double* Q, double* R);
+
+/* y = conj(x) for n complex elements (y may alias x): dag of a complex tensor. */
+ITG_API int itg_conj(itg_handle* h, int64_t n, const double* x, double* y);
+
+/* z = x + 0i for n elements (complex(::CuDense{Float64}), test/test_cudense.jl:60-70). */
+ITG_API int itg_real_to_complex(itg_handle* h, int64_t n, const double* x, double* z);
+
+/* x = alpha * x for n complex elements, alpha = (re, im). */
+ITG_API int itg_zscal(itg_handle* h, int64_t n, const double* alpha, double* x);
 
 /* Bound on |C_split - C_exact|_F / (|A|_F |B|_F) for ITG_PREC_SPLIT with the
  * library's slice count at contraction depth K (host-only arithmetic). */

@@ -700,7 +700,12 @@ extern "C" int itg_contract(itg_handle* h, int dtype, double alpha, const void* 
                             const int64_t* dimsB, const int32_t* modesB, double beta, void* C,
                             int rankC, const int64_t* dimsC, const int32_t* modesC, int precision) {
   if (!h) return ITG_ERR_INVALID;
-  if (dtype != ITG_F64) return itg_fail(h, ITG_ERR_UNSUPPORTED, "dtype %d not supported", dtype);
+  if (dtype != ITG_F64 && dtype != ITG_C64) return itg_fail(h, ITG_ERR_UNSUPPORTED, "dtype %d not supported", dtype);
+  if (dtype == ITG_C64) {
+    const double al[2] = {alpha, 0.0}, be[2] = {beta, 0.0};
+    return itg_contract_z(h, ITG_C64, ITG_C64, al, A, rankA, dimsA, modesA, B, rankB, dimsB, modesB, be, C, rankC,
+                          dimsC, modesC, precision);
+  }
   if (precision != ITG_PREC_FP64 && precision != ITG_PREC_SPLIT)
     return itg_fail(h, ITG_ERR_INVALID, "unknown precision %d", precision);
   if (rankA < 0 || rankB < 0 || rankC < 0 || rankA > ITG_MAX_RANK || rankB > ITG_MAX_RANK ||

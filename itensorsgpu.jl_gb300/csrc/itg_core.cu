@@ -144,6 +144,7 @@ extern "C" int itg_destroy(itg_handle* h) {
   if (h->dev_status) cudaFree(h->dev_status);
   if (h->gemv_part) cudaFree(h->gemv_part);
   if (h->tab_buf) cudaFree(h->tab_buf);
+  if (h->cplx_buf) cudaFree(h->cplx_buf);
   delete h;
   return ITG_OK;
 }

@@ -81,8 +81,27 @@ extern "C" int itg_diag_contract(itg_handle* h, int dtype, double alpha, const d
                                  const int64_t* dimsT, const int32_t* modesT, double beta, void* Cv,
                                  int rankC, const int64_t* dimsC, const int32_t* modesC) {
   if (!h) return ITG_ERR_INVALID;
-  if (dtype != ITG_F64) return itg_fail(h, ITG_ERR_UNSUPPORTED, "dtype %d", dtype);
+  if (dtype != ITG_F64 && dtype != ITG_C64) return itg_fail(h, ITG_ERR_UNSUPPORTED, "dtype %d", dtype);
   if (!d || !Tv || !Cv) return itg_fail(h, ITG_ERR_INVALID, "null pointer");
+  if (dtype == ITG_C64) {
+    // real diagonal x complex dense: the re/im mode of T passes to C
+    if (rankT + 1 > ITG_MAX_RANK || rankC + 1 > ITG_MAX_RANK || rankD < 1 || rankD > ITG_MAX_RANK || rankT < 0 ||
+        rankC < 0)
+      return itg_fail(h, ITG_ERR_UNSUPPORTED, "rank out of range");
+    int32_t c = 0;
+    for (int i = 0; i < rankD; ++i) c = modesD[i] > c ? modesD[i] : c;
+    for (int i = 0; i < rankT; ++i) c = modesT[i] > c ? modesT[i] : c;
+    for (int i = 0; i < rankC; ++i) c = modesC[i] > c ? modesC[i] : c;
+    ++c;
+    int64_t dT[ITG_MAX_RANK], dC[ITG_MAX_RANK];
+    int32_t mT[ITG_MAX_RANK], mC[ITG_MAX_RANK];
+    dT[0] = dC[0] = 2;
+    mT[0] = mC[0] = c;
+    for (int i = 0; i < rankT; ++i) { dT[i + 1] = dimsT[i]; mT[i + 1] = modesT[i]; }
+    for (int i = 0; i < rankC; ++i) { dC[i + 1] = dimsC[i]; mC[i + 1] = modesC[i]; }
+    return itg_diag_contract(h, ITG_F64, alpha, d, uniform, rankD, dimsD, modesD, Tv, rankT + 1, dT, mT, beta, Cv,
+                             rankC + 1, dC, mC);
+  }
   if (rankD < 1 || rankD > ITG_MAX_RANK || rankT < 0 || rankT > ITG_MAX_RANK || rankC < 0 ||
       rankC > ITG_MAX_RANK)
     return itg_fail(h, ITG_ERR_UNSUPPORTED, "rank out of range");

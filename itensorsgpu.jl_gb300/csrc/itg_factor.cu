@@ -185,14 +185,16 @@ __device__ __forceinline__ double warp_sum(double v) {
 // between polish pairs near the rounding floor of the dot product (about
 // eps sqrt(m) relative, i.e. tol itself), where they can repeat without
 // making progress; they must not keep the sweep loop running.
+// Pairs involving a column with squared norm <= amin_conv (rounding noise of
+// a rank-deficient input, see jacobi_run) are rotated like any other pair
+// but never keep the loop running either.
 constexpr double JACOBI_CONV = 4.0;
 
-__device__ __forceinline__ bool jacobi_significant(double a, double b, double g, double tol) {
-  return fabs(g) > JACOBI_CONV * tol * sqrt(a) * sqrt(b);
+__device__ __forceinline__ bool jacobi_significant(double a, double b, double g, double tol, double amin_conv) {
+  return a > amin_conv && b > amin_conv && fabs(g) > JACOBI_CONV * tol * sqrt(a) * sqrt(b);
 }
 
-__device__ __forceinline__ bool jacobi_rotation(double a, double b, double g, double tol,
-                                                double& c, double& s) {
+__device__ __forceinline__ bool jacobi_rotation(double a, double b, double g, double tol, double& c, double& s) {
   if (a == 0.0 || b == 0.0) return false;
   if (fabs(g) <= tol * sqrt(a) * sqrt(b)) return false;
   double zeta = (b - a) / (2.0 * g);
@@ -204,7 +206,7 @@ __device__ __forceinline__ bool jacobi_rotation(double a, double b, double g, do
 
 // Small problems: the whole sweep loop in one CTA; warps take pairs.
 __global__ void __launch_bounds__(1024)
-k_jacobi_onecta(double* __restrict__ W, int64_t m, int n, double* __restrict__ V, double tol,
+k_jacobi_onecta(double* __restrict__ W, int64_t m, int n, double* __restrict__ V, double tol, double amin_conv,
                 int max_sweeps, int* __restrict__ sweeps_out) {
   __shared__ int rotated;
   const int np = n + (n & 1);
@@ -242,7 +244,7 @@ k_jacobi_onecta(double* __restrict__ W, int64_t m, int n, double* __restrict__ V
             vp[i] = c * x - s * y;
             vq[i] = s * x + c * y;
           }
-          if (lane == 0 && jacobi_significant(a, b, g, tol)) rotated = 1;
+          if (lane == 0 && jacobi_significant(a, b, g, tol, amin_conv)) rotated = 1;
         }
       }
       __syncthreads();
@@ -256,7 +258,7 @@ k_jacobi_onecta(double* __restrict__ W, int64_t m, int n, double* __restrict__ V
 
 // Large problems: one launch per round-robin step, one CTA per pair.
 __global__ void __launch_bounds__(256)
-k_jacobi_step(double* __restrict__ W, int64_t m, int n, double* __restrict__ V, double tol,
+k_jacobi_step(double* __restrict__ W, int64_t m, int n, double* __restrict__ V, double tol, double amin_conv,
               int step, int* __restrict__ rotated) {
   __shared__ double sh[3][8];
   const int np = n + (n & 1);
@@ -293,7 +295,7 @@ k_jacobi_step(double* __restrict__ W, int64_t m, int n, double* __restrict__ V, 
     vp[i] = c * x - s * y;
     vq[i] = s * x + c * y;
   }
-  if (threadIdx.x == 0 && jacobi_significant(a, b, g, tol)) *rotated = 1;
+  if (threadIdx.x == 0 && jacobi_significant(a, b, g, tol, amin_conv)) *rotated = 1;
 }
 
 __global__ void k_identity(int n, double* __restrict__ V) {
@@ -498,8 +500,18 @@ int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* f
   ITG_CHECK_LAUNCH(h);
   const double tol = 2.220446049250313e-16 * sqrt((double)m);
   if (n <= 1) { *sweeps_done = 0; return ITG_OK; }
+  // Columns whose norm falls below 10 eps |W|_F carry only rounding noise of
+  // the rotations that touched them (a rank-deficient W, e.g. the bond
+  // matrices of a direct sum of two MPS): their pairs keep being rotated (so
+  // that W's columns stay as orthogonal as rounding allows) but do not count
+  // towards convergence, otherwise the sweeps never settle.
+  ITG_TRY(itg::nrm2_dev(h, m * n, W, h->gemv_part + 1024, h->gemv_part));
+  ITG_CUDA(h, cudaMemcpyAsync(h->pinned, h->gemv_part + 1024, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  const double fro = h->pinned[0];
+  const double amin_conv = (10.0 * 2.220446049250313e-16 * fro) * (10.0 * 2.220446049250313e-16 * fro);
   if (n <= ONECTA_MAX_N) {
-    k_jacobi_onecta<<<1, 1024, 0, h->stream>>>(W, m, (int)n, V, tol, JACOBI_MAX_SWEEPS, flag_dev);
+    k_jacobi_onecta<<<1, 1024, 0, h->stream>>>(W, m, (int)n, V, tol, amin_conv, JACOBI_MAX_SWEEPS, flag_dev);
     ITG_CHECK_LAUNCH(h);
     int* hp = (int*)h->pinned;
     ITG_CUDA(h, cudaMemcpyAsync(hp, flag_dev, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -509,11 +521,11 @@ int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* f
   }
   if (h->jacobi_mode == 0) {
     const int st = itg::jacobi_blocked<double>(h, W, m, (int)n, V, tol, 0.0, JACOBI_MAX_SWEEPS, flag_dev,
-                                               sweeps_done);
+                                               sweeps_done, amin_conv);
     if (st != ITG_ERR_UNSUPPORTED) return st;
   } else if (h->jacobi_mode == 2) {
     const int st = itg::jacobi_persistent<double>(h, W, m, (int)n, V, tol, 0.0, JACOBI_MAX_SWEEPS, flag_dev,
-                                                  sweeps_done);
+                                                  sweeps_done, amin_conv);
     if (st != ITG_ERR_UNSUPPORTED) return st;
   }
   // per-step launches (devices without cooperative launch)
@@ -522,7 +534,7 @@ int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* f
   for (int sweep = 0; sweep < JACOBI_MAX_SWEEPS; ++sweep) {
     ITG_CUDA(h, cudaMemsetAsync(flag_dev, 0, sizeof(int), h->stream));
     for (int step = 0; step < np - 1; ++step)
-      k_jacobi_step<<<np / 2, 256, 0, h->stream>>>(W, m, (int)n, V, tol, step, flag_dev);
+      k_jacobi_step<<<np / 2, 256, 0, h->stream>>>(W, m, (int)n, V, tol, amin_conv, step, flag_dev);
     ITG_CHECK_LAUNCH(h);
     ITG_CUDA(h, cudaMemcpyAsync(hp, flag_dev, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     ITG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -603,9 +615,11 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
   size_t off = 0;
   auto take = [&](size_t bytes) { size_t o = off; off += itg_align256(bytes); return o; };
   const bool mixed = method == ITG_SVD_MIXED || (method == ITG_SVD_AUTO && nn > ONECTA_MAX_N);
-  // QR preconditioning for large problems, and for the mixed method whenever
-  // a side must be exactly orthonormal
-  const bool pre = (h->svd_qr_precond && nn > ONECTA_MAX_N) || (mixed && iso != ISO_NONE);
+  // QR preconditioning for large problems, and whenever a side must be
+  // exactly orthonormal: that side is then Q times the rotations (or the
+  // refined eigenvectors), never U_J = J V_J / S, which loses orthogonality
+  // in columns whose S is small or rounding noise (rank-deficient inputs)
+  const bool pre = (h->svd_qr_precond && nn > ONECTA_MAX_N) || iso != ISO_NONE;
   const bool two = pre && iso == ISO_RIGHT;
   // the Jacobi problem: W itself (mj = mm rows) or J (nn x nn)
   const int64_t mj = pre ? nn : mm;
@@ -764,7 +778,11 @@ extern "C" int itg_factorize_trunc(itg_handle* h, int64_t m, int64_t n, const do
   }
   if (lda != m) return itg_fail(h, ITG_ERR_UNSUPPORTED, "factorize needs lda == m");
   // the isometric factor in L's slot (U for ortho left, V for right); the other
-  // SVD factor is scratch output in C's slot and replaced by the projection
+  // SVD factor is scratch output in C's slot and replaced by the projection.
+  // (A square right-isometric split could go through A^T with one QR instead
+  // of ISO_RIGHT's two; measured at chi = 1024 the second QR pays for itself:
+  // Jacobi on R2^T needs fewer sweeps; the FP64 N = 24 sweep took 20.6 s with
+  // two QRs and 26.9 s with one, the mixed one was unchanged.)
   const bool tr = m < n;
   const int iso = (ortho == ITG_ORTHO_LEFT) == !tr ? ISO_LEFT : ISO_RIGHT;
   double* Ubuf = ortho == ITG_ORTHO_LEFT ? L : C;

@@ -81,6 +81,8 @@ struct itg_handle {
   void* tune_buf = nullptr;   // throw-away outputs of tuning launches
   size_t tune_buf_bytes = 0;
   int64_t tune_runs = 0;
+  void* cplx_buf = nullptr;   // realified operands / temporaries of complex contractions
+  size_t cplx_buf_bytes = 0;
   int64_t* tab_buf = nullptr; // offset tables of the blocked QR's submatrix products
   int64_t tab_buf_elems = 0;
   int last_sweeps = 0;        // Jacobi sweeps of the last SVD / eigh call
@@ -105,7 +107,7 @@ namespace itg {
 int jacobi_aux_ints(int max_sweeps);
 template <class T>
 int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* aux,
-                      int* sweeps);
+                      int* sweeps, T amin_conv = T(0));
 // Blocked Householder QR (itg_qr_blocked.cu): panels of QR_NB columns, WY
 // trailing updates through the contraction engine at `precision`; nref
 // reflectors (nref <= min(m, n)) applied to all n columns.
@@ -119,7 +121,7 @@ size_t qr_blocked_t_doubles(int64_t n);
 // memory, one launch per block step; ITG_ERR_UNSUPPORTED when m is too large.
 template <class T>
 int jacobi_blocked(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* flag,
-                   int* sweeps);
+                   int* sweeps, T amin_conv = T(0));
 }  // namespace itg
 
 // Error helpers ---------------------------------------------------------------

@@ -116,7 +116,8 @@ __device__ __forceinline__ void jp_block_sum3(T& a, T& b, T& g, T (*sh)[JP_WARPS
 // pair's columns are read once per step; RC = 0 streams them (any m).
 template <class T, int RC>
 __global__ void __launch_bounds__(JP_THREADS)
-k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T tol_conv, T amin, int max_sweeps,
+k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T tol_conv, T amin, T amin_conv,
+                 int max_sweeps,
                  int* aux) {
   __shared__ T sh[3][JP_WARPS];
   unsigned* count = (unsigned*)aux;
@@ -189,7 +190,8 @@ k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, 
           __stcg(vp + i, c * x - s * y);
           __stcg(vq + i, s * x + c * y);
         }
-        if (t == 0 && fabs(g) > tol_conv * sqrt(a) * sqrt(b)) __stcg(rot + sweep, 1);
+        if (t == 0 && a > amin_conv && b > amin_conv && fabs(g) > tol_conv * sqrt(a) * sqrt(b))
+          __stcg(rot + sweep, 1);
       }
       if (!jp_grid_sync(count, gen, status, gridDim.x)) {
         done = -1;
@@ -229,8 +231,8 @@ __host__ __device__ inline T conv_tol(T tol) {
 
 template <class T, int WB>
 __global__ void __launch_bounds__(JB_THREADS)
-k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T tol_conv, T amin, int step,
-                    int first, int* __restrict__ rotated) {
+k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T tol_conv, T amin,
+                    T amin_conv, int step, int first, int* __restrict__ rotated) {
   constexpr int C2 = 2 * WB;              // local columns
   constexpr int TP = JB_THREADS / WB;     // threads per pair
   constexpr int WPG = TP / 32;            // warps per pair group
@@ -320,7 +322,7 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
       }
       if (lt == 0) {
         any = 1;
-        if (fabs(gg) > tol_conv * sqrt(a) * sqrt(b)) major = 1;
+        if (a > amin_conv && b > amin_conv && fabs(gg) > tol_conv * sqrt(a) * sqrt(b)) major = 1;
       }
     }
     __syncthreads();  // columns, Q and red are reused by the next round
@@ -364,7 +366,8 @@ int jacobi_aux_ints(int max_sweeps) { return 8 + max_sweeps; }
 // was hit (results usable), ITG_ERR_UNSUPPORTED when the device cannot run a
 // cooperative launch (the caller then uses per-step launches).
 template <class T, int RC>
-int launch_persist(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* aux) {
+int launch_persist(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, T amin_conv, int max_sweeps,
+                   int* aux) {
   const T tol_conv = conv_tol(tol);
   int per_sm = 0;
   ITG_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi_persist<T, RC>, JP_THREADS, 0));
@@ -375,7 +378,7 @@ int launch_persist(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, i
   if ((int64_t)np / 2 < grid) grid = np / 2;
   if (grid < 1) grid = 1;
   void* args[] = {(void*)&W,   (void*)&m,          (void*)&n,  (void*)&V,
-                  (void*)&tol, (void*)&tol_conv, (void*)&amin, (void*)&max_sweeps, (void*)&aux};
+                  (void*)&tol, (void*)&tol_conv, (void*)&amin, (void*)&amin_conv, (void*)&max_sweeps, (void*)&aux};
   ITG_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_jacobi_persist<T, RC>, dim3((unsigned)grid),
                                           dim3(JP_THREADS), args, 0, h->stream));
   return ITG_OK;
@@ -383,16 +386,16 @@ int launch_persist(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, i
 
 template <class T>
 int jacobi_persistent(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* aux,
-                      int* sweeps) {
+                      int* sweeps, T amin_conv) {
   int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device);
   if (!coop) return ITG_ERR_UNSUPPORTED;
   ITG_CUDA(h, cudaMemsetAsync(aux, 0, sizeof(int) * jacobi_aux_ints(max_sweeps), h->stream));
   int st;
-  if (m <= 4 * JP_THREADS) st = launch_persist<T, 4>(h, W, m, n, V, tol, amin, max_sweeps, aux);
-  else if (m <= 8 * JP_THREADS) st = launch_persist<T, 8>(h, W, m, n, V, tol, amin, max_sweeps, aux);
-  else if (m <= 16 * JP_THREADS) st = launch_persist<T, 16>(h, W, m, n, V, tol, amin, max_sweeps, aux);
-  else st = launch_persist<T, 0>(h, W, m, n, V, tol, amin, max_sweeps, aux);
+  if (m <= 4 * JP_THREADS) st = launch_persist<T, 4>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, aux);
+  else if (m <= 8 * JP_THREADS) st = launch_persist<T, 8>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, aux);
+  else if (m <= 16 * JP_THREADS) st = launch_persist<T, 16>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, aux);
+  else st = launch_persist<T, 0>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, aux);
   if (st != ITG_OK) return st;
   int* hp = (int*)h->pinned;
   ITG_CUDA(h, cudaMemcpyAsync(hp, aux, sizeof(int) * 4, cudaMemcpyDeviceToHost, h->stream));
@@ -409,7 +412,8 @@ size_t jb_smem_bytes(int64_t m) {
 }
 
 template <class T, int WB>
-int jb_run(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* flag, int* sweeps) {
+int jb_run(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, T amin_conv, int max_sweeps, int* flag,
+           int* sweeps) {
   const size_t smem = jb_smem_bytes<T, WB>(m);
   static bool attr = false;
   if (!attr) {
@@ -422,8 +426,8 @@ int jb_run(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_s
   for (int sw = 0; sw < max_sweeps; ++sw) {
     ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
     for (int step = 0; step < nbp - 1; ++step)
-      k_jacobi_block_step<T, WB><<<nbp / 2, JB_THREADS, smem, h->stream>>>(W, m, n, V, tol, conv_tol(tol), amin, step,
-                                                                          step == 0, flag);
+      k_jacobi_block_step<T, WB><<<nbp / 2, JB_THREADS, smem, h->stream>>>(W, m, n, V, tol, conv_tol(tol), amin,
+                                                                          amin_conv, step, step == 0, flag);
     ITG_CHECK_LAUNCH(h);
     ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     ITG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -440,23 +444,25 @@ int jb_run(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_s
 // shared memory; ITG_ERR_UNSUPPORTED when not even 2 + 2 columns fit.
 template <class T>
 int jacobi_blocked(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, int max_sweeps, int* flag,
-                   int* sweeps) {
+                   int* sweeps, T amin_conv) {
   constexpr size_t LIM = 200 * 1024;
   if (n < 2) {
     *sweeps = 0;
     return ITG_OK;
   }
-  if (jb_smem_bytes<T, 8>(m) <= LIM && n >= 64) return jb_run<T, 8>(h, W, m, n, V, tol, amin, max_sweeps, flag, sweeps);
-  if (jb_smem_bytes<T, 4>(m) <= LIM) return jb_run<T, 4>(h, W, m, n, V, tol, amin, max_sweeps, flag, sweeps);
-  if (jb_smem_bytes<T, 2>(m) <= LIM) return jb_run<T, 2>(h, W, m, n, V, tol, amin, max_sweeps, flag, sweeps);
+  if (jb_smem_bytes<T, 8>(m) <= LIM && n >= 64) return jb_run<T, 8>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, flag, sweeps);
+  if (jb_smem_bytes<T, 4>(m) <= LIM) return jb_run<T, 4>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, flag, sweeps);
+  if (jb_smem_bytes<T, 2>(m) <= LIM) return jb_run<T, 2>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, flag, sweeps);
   return ITG_ERR_UNSUPPORTED;
 }
 
-template int jacobi_blocked<float>(itg_handle*, float*, int64_t, int, float*, float, float, int, int*, int*);
-template int jacobi_blocked<double>(itg_handle*, double*, int64_t, int, double*, double, double, int, int*, int*);
+template int jacobi_blocked<float>(itg_handle*, float*, int64_t, int, float*, float, float, int, int*, int*, float);
+template int jacobi_blocked<double>(itg_handle*, double*, int64_t, int, double*, double, double, int, int*, int*,
+                                     double);
 
-template int jacobi_persistent<float>(itg_handle*, float*, int64_t, int, float*, float, float, int, int*, int*);
+template int jacobi_persistent<float>(itg_handle*, float*, int64_t, int, float*, float, float, int, int*, int*,
+                                       float);
 template int jacobi_persistent<double>(itg_handle*, double*, int64_t, int, double*, double, double, int, int*,
-                                        int*);
+                                        int*, double);
 
 }  // namespace itg

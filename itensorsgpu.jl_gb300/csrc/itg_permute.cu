@@ -198,13 +198,45 @@ static int permute_axpby(itg_handle* h, double alpha, const double* A, int rank,
   return ITG_OK;
 }
 
+namespace {
+// Complex tensors (ITG_C64, interleaved re/im) are permuted as real tensors
+// with one leading mode of length 2 that stays first.
+struct C64View {
+  int rank;
+  int64_t dims[ITG_MAX_RANK];
+  int32_t ma[ITG_MAX_RANK], mb[ITG_MAX_RANK];
+};
+
+int c64_view(itg_handle* h, int rank, const int64_t* dimsA, const int32_t* modesA, const int32_t* modesB,
+             C64View& v) {
+  if (rank + 1 > ITG_MAX_RANK) return itg_fail(h, ITG_ERR_UNSUPPORTED, "complex rank above %d", ITG_MAX_RANK - 1);
+  int32_t c = 0;
+  for (int i = 0; i < rank; ++i) c = modesA[i] > c ? modesA[i] : c;
+  ++c;
+  v.rank = rank + 1;
+  v.dims[0] = 2;
+  v.ma[0] = v.mb[0] = c;
+  for (int i = 0; i < rank; ++i) {
+    v.dims[i + 1] = dimsA[i];
+    v.ma[i + 1] = modesA[i];
+    v.mb[i + 1] = modesB[i];
+  }
+  return ITG_OK;
+}
+}  // namespace
+
 extern "C" int itg_permute(itg_handle* h, int dtype, double alpha, const void* A, int rank,
                            const int64_t* dimsA, const int32_t* modesA, void* B,
                            const int32_t* modesB) {
   if (!h) return ITG_ERR_INVALID;
-  if (dtype != ITG_F64) return itg_fail(h, ITG_ERR_UNSUPPORTED, "dtype %d", dtype);
+  if (dtype != ITG_F64 && dtype != ITG_C64) return itg_fail(h, ITG_ERR_UNSUPPORTED, "dtype %d", dtype);
   if (rank > 0 && (!dimsA || !modesA || !modesB)) return itg_fail(h, ITG_ERR_INVALID, "null array");
   if (!A || !B) return itg_fail(h, ITG_ERR_INVALID, "null tensor");
+  if (dtype == ITG_C64) {
+    C64View v;
+    ITG_TRY(c64_view(h, rank, dimsA, modesA, modesB, v));
+    return permute_axpby(h, alpha, (const double*)A, v.rank, v.dims, v.ma, 0.0, nullptr, v.mb, (double*)B);
+  }
   return permute_axpby(h, alpha, (const double*)A, rank, dimsA, modesA, 0.0, nullptr, modesB,
                        (double*)B);
 }
@@ -213,10 +245,16 @@ extern "C" int itg_axpby_permuted(itg_handle* h, int dtype, double alpha, const 
                                   const int64_t* dimsA, const int32_t* modesA, double beta,
                                   const void* B, const int32_t* modesB, void* C) {
   if (!h) return ITG_ERR_INVALID;
-  if (dtype != ITG_F64) return itg_fail(h, ITG_ERR_UNSUPPORTED, "dtype %d", dtype);
+  if (dtype != ITG_F64 && dtype != ITG_C64) return itg_fail(h, ITG_ERR_UNSUPPORTED, "dtype %d", dtype);
   if (rank > 0 && (!dimsA || !modesA || !modesB)) return itg_fail(h, ITG_ERR_INVALID, "null array");
   if (!A || !C || (beta != 0.0 && !B)) return itg_fail(h, ITG_ERR_INVALID, "null tensor");
   if (A == C) return itg_fail(h, ITG_ERR_INVALID, "C must not alias A");
+  if (dtype == ITG_C64) {
+    C64View v;
+    ITG_TRY(c64_view(h, rank, dimsA, modesA, modesB, v));
+    return permute_axpby(h, alpha, (const double*)A, v.rank, v.dims, v.ma, beta, (const double*)B, v.mb,
+                         (double*)C);
+  }
   return permute_axpby(h, alpha, (const double*)A, rank, dimsA, modesA, beta, (const double*)B,
                        modesB, (double*)C);
 }

@@ -22,6 +22,7 @@ LIB_PATH = Path(__file__).resolve().parent.parent / "libitg.so"
 ITG_OK, ITG_ERR_INVALID, ITG_ERR_SHAPE, ITG_ERR_ALLOC, ITG_ERR_CUDA = 0, 1, 2, 3, 4
 ITG_ERR_TIMEOUT, ITG_ERR_NOTCONVERGED, ITG_ERR_UNSUPPORTED = 5, 6, 7
 ITG_F64 = 0
+ITG_C64 = 1
 PREC_FP64, PREC_SPLIT = 0, 1
 KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_SPLIT_PREP = 0, 1, 2
 SVD_AUTO, SVD_JACOBI, SVD_MIXED = 0, 1, 2
@@ -71,6 +72,17 @@ SIGNATURES = {
                                C.c_double,
                                _P, C.c_int, _I64P, _I32P, C.c_int]),
     "itg_split_error_bound": (C.c_double, [C.c_int64]),
+    "itg_contract_z": (C.c_int, [_P, C.c_int, C.c_int, _DP,
+                                 _P, C.c_int, _I64P, _I32P,
+                                 _P, C.c_int, _I64P, _I32P,
+                                 _DP,
+                                 _P, C.c_int, _I64P, _I32P, C.c_int]),
+    "itg_conj": (C.c_int, [_P, C.c_int64, _P, _P]),
+    "itg_svd_trunc_z": (C.c_int, [_P, C.c_int64, C.c_int64, _P, C.c_int64, C.c_int64, C.c_int64,
+                                  C.c_double, C.c_int, C.c_int, C.c_int, _P, _P, _P, _I64P, _DP, _DP]),
+    "itg_qr_z": (C.c_int, [_P, C.c_int64, C.c_int64, _P, C.c_int64, _P, _P]),
+    "itg_real_to_complex": (C.c_int, [_P, C.c_int64, _P, _P]),
+    "itg_zscal": (C.c_int, [_P, C.c_int64, _DP, _P]),
     "itg_permute": (C.c_int, [_P, C.c_int, C.c_double, _P, C.c_int, _I64P, _I32P, _P, _I32P]),
     "itg_axpby_permuted": (C.c_int, [_P, C.c_int, C.c_double, _P, C.c_int, _I64P, _I32P,
                                      C.c_double, _P, _I32P, _P]),

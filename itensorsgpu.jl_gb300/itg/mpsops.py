@@ -76,9 +76,7 @@ def _mid(t: ITensor):
     return t.inds[1:-1]
 
 
-def dag(x):
-    """Complex conjugate; the identity for real FP64 storage."""
-    return x
+from .tensor import dag  # noqa: E402  (re-exported: conjugates complex site tensors)
 
 
 def linkind(M, j: int) -> Index:

@@ -24,7 +24,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from ._lib import DimensionMismatch, PREC_FP64, PREC_SPLIT, ITG_F64, i32arr, i64arr
+from ._lib import DimensionMismatch, PREC_FP64, PREC_SPLIT, ITG_C64, ITG_F64, i32arr, i64arr
 
 try:
     import torch
@@ -66,8 +66,27 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
-def empty_dev(n: int):
-    return torch.empty(int(n), dtype=torch.float64, device=_dev())
+def empty_dev(n: int, cplx: bool = False):
+    return torch.empty(int(n), dtype=torch.complex128 if cplx else torch.float64, device=_dev())
+
+
+def _is_cplx(data) -> bool:
+    if torch is not None and isinstance(data, torch.Tensor):
+        return data.is_complex()
+    return np.iscomplexobj(data)
+
+
+def _dt(t) -> int:
+    """Element-type code of an ITensor's storage (ITG_F64 / ITG_C64)."""
+    return ITG_C64 if t.is_complex else ITG_F64
+
+
+def _to_complex_data(d):
+    """Complex copy of real device data through itg_real_to_complex."""
+    out = empty_dev(len(d), True)
+    if len(d):
+        _h().call("itg_real_to_complex", C.c_int64(len(d)), _ptr(d), _ptr(out))
+    return out
 
 
 # ----------------------------------------------------------------- Index
@@ -120,7 +139,7 @@ def prime(x, n: int = 1):
 # --------------------------------------------------------------- storage
 @dataclass
 class Dense:
-    data: object  # torch.Tensor (cuda, 1-D float64) or numpy 1-D float64
+    data: object  # torch.Tensor (cuda, 1-D float64 or complex128) or numpy 1-D
 
     @property
     def is_cuda(self):
@@ -156,6 +175,11 @@ class ITensor:
     def dims(self):
         return tuple(i.dim for i in self.inds)
 
+    @property
+    def is_complex(self) -> bool:
+        """ComplexF64 storage (interleaved re, im)."""
+        return _is_cplx(self.store.data)
+
     def order(self) -> int:
         return len(self.inds)
 
@@ -189,12 +213,13 @@ class ITensor:
         flat = d.detach().cpu().numpy() if (torch is not None and isinstance(d, torch.Tensor)) else np.asarray(d)
         return flat.reshape(t.dims if t.dims else (), order="F")
 
-    def scalar(self) -> float:
+    def scalar(self):
         """T[] for an order-0 tensor; one device->host read (cudense.jl:25-26)."""
         if self.order() != 0:
             raise DimensionMismatch(2, "scalar() needs an order-0 tensor")
         d = self.store.data
-        return float(d[0].item() if (torch is not None and isinstance(d, torch.Tensor)) else d[0])
+        v = d[0].item() if (torch is not None and isinstance(d, torch.Tensor)) else d[0]
+        return complex(v) if self.is_complex else float(v)
 
     def norm(self) -> float:
         return norm(self)
@@ -203,13 +228,13 @@ class ITensor:
     def __mul__(self, other):
         if isinstance(other, ITensor):
             return contract(self, other)
-        return _scale(self, float(other))
+        return _scale(self, other)
 
     def __rmul__(self, other):
-        return _scale(self, float(other))
+        return _scale(self, other)
 
     def __truediv__(self, x):
-        return _scale(self, 1.0 / float(x))
+        return _scale(self, 1.0 / x)
 
     def __neg__(self):
         return _scale(self, -1.0)
@@ -219,6 +244,12 @@ class ITensor:
 
     def __sub__(self, other):
         return _axpby(-1.0, other, 1.0, self)
+
+
+def _require_real(A, what):
+    if A.is_complex:
+        raise TypeError(f"{what} of a ComplexF64 tensor is not implemented (complex storage supports "
+                        "contraction, permutation, sums, scaling, norm, dag, svd and qr)")
 
 
 def _require_cuda(*ts):
@@ -236,8 +267,9 @@ def _host_permute(t: ITensor, inds) -> ITensor:
 
 # --------------------------------------------------------- constructors
 def ITensor_host(arr: np.ndarray, *inds) -> ITensor:
-    """CPU ITensor holding `arr` (n-d, index order `inds`)."""
-    arr = np.asarray(arr, dtype=np.float64)
+    """CPU ITensor holding `arr` (n-d, index order `inds`; float64 or complex128)."""
+    arr = np.asarray(arr)
+    arr = arr.astype(np.complex128 if np.iscomplexobj(arr) else np.float64, copy=False)
     if tuple(arr.shape) != tuple(i.dim for i in inds):
         raise DimensionMismatch(2, f"array shape {arr.shape} != index dims")
     return ITensor(Dense(arr.ravel(order="F").copy()), inds)
@@ -246,18 +278,24 @@ def ITensor_host(arr: np.ndarray, *inds) -> ITensor:
 def cuITensor(x=None, *inds) -> ITensor:
     """Device ITensor: from an ITensor, an n-d array with inds, a number (filled), or zeros.
 
-    Mirrors src/cuitensor.jl:1-27.
+    A leading element type (float or complex) makes zeros of that type
+    (cuITensor(SType, inds...)).  Mirrors src/cuitensor.jl:1-27.
     """
     if isinstance(x, ITensor):
         return cu(x)
+    if x is float or x is complex:
+        tdt = torch.complex128 if x is complex else torch.float64
+        return ITensor(Dense(torch.zeros(dim(inds), dtype=tdt, device=_dev())), inds)
     if isinstance(x, Index):
         inds = (x,) + inds
         return ITensor(Dense(torch.zeros(dim(inds), dtype=torch.float64, device=_dev())), inds)
     if x is None:
         return ITensor(Dense(torch.zeros(dim(inds), dtype=torch.float64, device=_dev())), inds)
     if np.isscalar(x):
-        return ITensor(Dense(torch.full((dim(inds),), float(x), dtype=torch.float64, device=_dev())), inds)
-    arr = np.asarray(x, dtype=np.float64)
+        tdt = torch.complex128 if np.iscomplexobj(x) else torch.float64
+        return ITensor(Dense(torch.full((dim(inds),), x, dtype=tdt, device=_dev())), inds)
+    arr = np.asarray(x)
+    arr = arr.astype(np.complex128 if np.iscomplexobj(arr) else np.float64, copy=False)
     if arr.ndim == 1 and len(inds) != 1:
         if arr.size != dim(inds):
             raise DimensionMismatch(2, "flat data length != dim(inds)")
@@ -270,17 +308,33 @@ def cuITensor(x=None, *inds) -> ITensor:
 
 
 def randomCuITensor(*inds, seed: int | None = None) -> ITensor:
-    """Entries i.i.d. N(0,1) from the library's Philox generator (src/cuitensor.jl:35-49)."""
+    """Entries i.i.d. N(0,1) from the library's Philox generator (src/cuitensor.jl:35-49).
+
+    A leading `complex` (randomCuITensor(ComplexF64, inds...)) draws complex
+    entries with independent N(0, 1/2) real and imaginary parts.
+    """
+    cplx = False
+    if inds and (inds[0] is complex or inds[0] is float):
+        cplx = inds[0] is complex
+        inds = inds[1:]
     n = dim(inds)
-    t = torch.empty(max(n, 1), dtype=torch.float64, device=_dev())
     s = next(_seed_counter) if seed is None else int(seed)
-    _h().call("itg_random_normal", C.c_int64(n), C.c_uint64(s), C.c_uint64(0), _ptr(t))
+    if not cplx:
+        t = torch.empty(max(n, 1), dtype=torch.float64, device=_dev())
+        _h().call("itg_random_normal", C.c_int64(n), C.c_uint64(s), C.c_uint64(0), _ptr(t))
+        return ITensor(Dense(t[:n]), inds)
+    t = torch.empty(max(n, 1), dtype=torch.complex128, device=_dev())
+    _h().call("itg_random_normal", C.c_int64(2 * n), C.c_uint64(s), C.c_uint64(0), _ptr(t))
+    if n:
+        _h().call("itg_scal", C.c_int64(2 * n), C.c_double(0.5 ** 0.5), _ptr(t))
     return ITensor(Dense(t[:n]), inds)
 
 
 def diagITensor(d, *inds, uniform: bool = False) -> ITensor:
-    """Device Diag ITensor (CuDiag).  `d` is the diagonal (or one value if uniform)."""
-    arr = np.atleast_1d(np.asarray(d, dtype=np.float64))
+    """Device Diag ITensor (CuDiag).  `d` is the diagonal (or one value if
+    uniform), real or complex."""
+    arr = np.atleast_1d(np.asarray(d))
+    arr = arr.astype(np.complex128 if np.iscomplexobj(arr) else np.float64, copy=False)
     return ITensor(Diag(torch.from_numpy(arr.copy()).to(_dev()), uniform), inds)
 
 
@@ -294,7 +348,9 @@ def cu(x):
     if isinstance(x, ITensor):
         if x.is_cuda:
             return x
-        d = torch.from_numpy(np.ascontiguousarray(np.asarray(x.store.data, dtype=np.float64))).to(_dev())
+        hd = np.asarray(x.store.data)
+        hd = hd.astype(np.complex128 if np.iscomplexobj(hd) else np.float64, copy=False)
+        d = torch.from_numpy(np.ascontiguousarray(hd)).to(_dev())
         st = Dense(d) if isinstance(x.store, Dense) else Diag(d, x.store.uniform)
         return ITensor(st, x.inds)
     if hasattr(x, "_cu"):
@@ -325,13 +381,51 @@ def _labels(*indsets):
     return lab
 
 
-def _scale(t: ITensor, x: float) -> ITensor:
+def _scale(t: ITensor, x) -> ITensor:
+    """x * t for a real or complex number x (itg_scal / itg_zscal)."""
     _require_cuda(t)
+    cx = isinstance(x, complex) or np.iscomplexobj(x)
+    if cx and t.isdiag():
+        raise TypeError("complex scaling of Diag storage is not supported")
+    if t.is_complex or cx:
+        out = t.store.data.clone() if t.is_complex else _to_complex_data(t.store.data)
+        if len(out):
+            a = (C.c_double * 2)(complex(x).real, complex(x).imag)
+            _h().call("itg_zscal", C.c_int64(len(out)), a, _ptr(out))
+        return ITensor(Dense(out), t.inds)
     out = t.store.data.clone()
     if len(out):
-        _h().call("itg_scal", C.c_int64(len(out)), C.c_double(x), _ptr(out))
+        _h().call("itg_scal", C.c_int64(len(out)), C.c_double(float(x)), _ptr(out))
     st = Dense(out) if isinstance(t.store, Dense) else Diag(out, t.store.uniform)
     return ITensor(st, t.inds)
+
+
+def dag(x):
+    """Complex conjugate (dag); a real tensor is returned as is.  For an MPS or
+    MPO every site tensor is conjugated."""
+    if not isinstance(x, ITensor):
+        if hasattr(x, "tensors"):
+            y = x.copy()
+            y.tensors = [dag(t) for t in x.tensors]
+            return y
+        return x
+    if not x.is_complex:
+        return x
+    _require_cuda(x)
+    out = torch.empty_like(x.store.data)
+    if len(out):
+        _h().call("itg_conj", C.c_int64(len(out)), _ptr(x.store.data), _ptr(out))
+    return ITensor(Dense(out), x.inds)
+
+
+def complex_(t: ITensor) -> ITensor:
+    """ComplexF64 copy of a tensor (complex(::ITensor), test/test_cuitensor.jl:77-81)."""
+    _require_cuda(t)
+    if t.isdiag():
+        t = dense(t)
+    if t.is_complex:
+        return t.copy()
+    return ITensor(Dense(_to_complex_data(t.store.data)), t.inds)
 
 
 def permute(t: ITensor, *inds) -> ITensor:
@@ -344,9 +438,9 @@ def permute(t: ITensor, *inds) -> ITensor:
         return ITensor(t.store, inds)
     _require_cuda(t)
     lab = _labels(t.inds)
-    out = empty_dev(dim(inds))
+    out = empty_dev(dim(inds), t.is_complex)
     if dim(inds) > 0:
-        _h().call("itg_permute", ITG_F64, C.c_double(1.0), _ptr(t.store.data), len(t.inds),
+        _h().call("itg_permute", _dt(t), C.c_double(1.0), _ptr(t.store.data), len(t.inds),
                   i64arr(t.dims), i32arr([lab[i] for i in t.inds]), _ptr(out),
                   i32arr([lab[i] for i in inds]))
     return ITensor(Dense(out), inds)
@@ -359,10 +453,12 @@ def _axpby(alpha: float, a: ITensor, beta: float, b: ITensor) -> ITensor:
         raise DimensionMismatch(2, "ITensor +/-: index sets differ")
     a = dense(a) if a.isdiag() else a
     b = dense(b) if b.isdiag() else b
+    if a.is_complex != b.is_complex:
+        a, b = (a, complex_(b)) if a.is_complex else (complex_(a), b)
     lab = _labels(b.inds)
-    out = empty_dev(dim(b.inds))
+    out = empty_dev(dim(b.inds), b.is_complex)
     if dim(b.inds) > 0:
-        _h().call("itg_axpby_permuted", ITG_F64, C.c_double(alpha), _ptr(a.store.data), len(a.inds),
+        _h().call("itg_axpby_permuted", _dt(b), C.c_double(alpha), _ptr(a.store.data), len(a.inds),
                   i64arr(a.dims), i32arr([lab[i] for i in a.inds]), C.c_double(beta),
                   _ptr(b.store.data), i32arr([lab[i] for i in b.inds]), _ptr(out))
     return ITensor(Dense(out), b.inds)
@@ -380,7 +476,7 @@ def norm(t: ITensor) -> float:
             return abs(float(d[0].item())) * np.sqrt(min(t.dims) if t.dims else 1)
         t = ITensor(Dense(d), (Index(len(d)),))
     r = C.c_double()
-    n = len(t.store.data)
+    n = len(t.store.data) * (2 if t.is_complex else 1)
     _h().call("itg_nrm2", C.c_int64(n), _ptr(t.store.data), C.byref(r))
     return r.value
 
@@ -390,6 +486,9 @@ def dense(t: ITensor) -> ITensor:
     if not t.isdiag():
         return t
     _require_cuda(t)
+    if t.is_complex:
+        Dr, Di = _diag_parts(t)
+        return _axpby(1.0, _scale(dense(Di), 1j), 1.0, complex_(dense(Dr)))
     out = empty_dev(dim(t.inds))
     if dim(t.inds) > 0:
         _h().call("itg_diag_to_dense", _ptr(t.store.data), int(t.store.uniform), len(t.inds),
@@ -416,6 +515,17 @@ def contract(A: ITensor, B: ITensor, precision: int | None = None, **kw) -> ITen
         D, T = (A, B) if A.isdiag() else (B, A)
         return _diag_dense(D, T, out_inds)
     lab = _labels(A.inds, B.inds)
+    if A.is_complex or B.is_complex:
+        out = empty_dev(dim(out_inds), True)
+        if dim(out_inds) > 0:
+            one = (C.c_double * 2)(1.0, 0.0)
+            zero = (C.c_double * 2)(0.0, 0.0)
+            _h().call("itg_contract_z", _dt(A), _dt(B), one,
+                      _ptr(A.store.data), len(A.inds), i64arr(A.dims), i32arr([lab[i] for i in A.inds]),
+                      _ptr(B.store.data), len(B.inds), i64arr(B.dims), i32arr([lab[i] for i in B.inds]),
+                      zero, _ptr(out), len(out_inds), i64arr([i.dim for i in out_inds]),
+                      i32arr([lab[i] for i in out_inds]), int(prec))
+        return ITensor(Dense(out), out_inds)
     out = empty_dev(dim(out_inds))
     if dim(out_inds) > 0:
         _h().call("itg_contract", ITG_F64, C.c_double(1.0),
@@ -427,11 +537,45 @@ def contract(A: ITensor, B: ITensor, precision: int | None = None, **kw) -> ITen
     return ITensor(Dense(out), out_inds)
 
 
+def _split_cplx(d):
+    """Real parts (re, im) of complex device data: the interleaved vector, read
+    as the real (2, n) array, permuted to (n, 2) (itg_permute)."""
+    n = len(d)
+    out = empty_dev(2 * n)
+    if n:
+        _h().call("itg_permute", ITG_F64, C.c_double(1.0), _ptr(d), 2, i64arr([2, n]), i32arr([1, 2]), _ptr(out),
+                  i32arr([2, 1]))
+    return out[:n], out[n:]
+
+
+def _join_cplx(re, im):
+    """Complex device data re + i im (the inverse permutation of _split_cplx)."""
+    n = len(re)
+    buf = torch.cat([re, im]) if n else re
+    out = empty_dev(n, True)
+    if n:
+        _h().call("itg_permute", ITG_F64, C.c_double(1.0), _ptr(buf), 2, i64arr([n, 2]), i32arr([1, 2]), _ptr(out),
+                  i32arr([2, 1]))
+    return out
+
+
+def _diag_parts(D: ITensor):
+    """(real part, imaginary part or None) of a Diag tensor, as real Diags."""
+    if not D.is_complex:
+        return D, None
+    re, im = _split_cplx(D.store.data)
+    return ITensor(Diag(re, D.store.uniform), D.inds), ITensor(Diag(im, D.store.uniform), D.inds)
+
+
 def _diag_dense(D: ITensor, T: ITensor, out_inds) -> ITensor:
+    if D.is_complex:
+        # (Dr + i Di) T = Dr T + i (Di T)
+        Dr, Di = _diag_parts(D)
+        return _axpby(1.0, _scale(_diag_dense(Di, T, out_inds), 1j), 1.0, complex_(_diag_dense(Dr, T, out_inds)))
     lab = _labels(D.inds, T.inds)
-    out = empty_dev(dim(out_inds))
+    out = empty_dev(dim(out_inds), T.is_complex)
     if dim(out_inds) > 0:
-        _h().call("itg_diag_contract", ITG_F64, C.c_double(1.0), _ptr(D.store.data),
+        _h().call("itg_diag_contract", _dt(T), C.c_double(1.0), _ptr(D.store.data),
                   int(D.store.uniform), len(D.inds), i64arr(D.dims), i32arr([lab[i] for i in D.inds]),
                   _ptr(T.store.data), len(T.inds), i64arr(T.dims), i32arr([lab[i] for i in T.inds]),
                   C.c_double(0.0), _ptr(out), len(out_inds), i64arr([i.dim for i in out_inds]),
@@ -440,6 +584,32 @@ def _diag_dense(D: ITensor, T: ITensor, out_inds) -> ITensor:
 
 
 def _diag_diag(A: ITensor, B: ITensor, common, out_inds) -> ITensor:
+    if A.is_complex or B.is_complex:
+        # (Ar + i Ai)(Br + i Bi) elementwise, from real products
+        Ar, Ai = _diag_parts(A)
+        Br, Bi = _diag_parts(B)
+        parts = [(1.0, Ar, Br, 0)]
+        if Ai is not None and Bi is not None:
+            parts.append((-1.0, Ai, Bi, 0))
+        if Bi is not None:
+            parts.append((1.0, Ar, Bi, 1))
+        if Ai is not None:
+            parts.append((1.0, Ai, Br, 1))
+        acc = [None, None]
+        for sgn, X, Y, k in parts:
+            Z = _diag_diag(X, Y, common, out_inds)
+            Zd = ITensor(Dense(Z.store.data), (Index(len(Z.store.data)),))
+            if acc[k] is None:
+                acc[k] = _scale(Zd, sgn) if sgn != 1.0 else Zd
+            else:
+                acc[k] = _axpby(sgn, Zd, 1.0, acc[k].replaceinds(acc[k].inds, Zd.inds))
+        re = acc[0].store.data
+        im = acc[1].store.data if acc[1] is not None else torch.zeros_like(re)
+        z = _join_cplx(re, im)
+        if len(out_inds) == 0:
+            return ITensor(Dense(z), ())
+        uni = A.store.uniform and B.store.uniform
+        return ITensor(Diag(z, uni), out_inds)
     na = 1 if A.store.uniform else len(A.store.data)
     nb = 1 if B.store.uniform else len(B.store.data)
     lens = [n for n, u in ((na, A.store.uniform), (nb, B.store.uniform)) if not u]
@@ -449,8 +619,11 @@ def _diag_diag(A: ITensor, B: ITensor, common, out_inds) -> ITensor:
     _h().call("itg_diag_diag", C.c_int64(n), C.c_double(1.0), _ptr(A.store.data),
               int(A.store.uniform), _ptr(B.store.data), int(B.store.uniform), _ptr(out))
     if len(out_inds) == 0:
-        s = out[:n].sum().reshape(1)  # full contraction of two diagonals
-        return ITensor(Dense(s), ())
+        # full contraction of two diagonals: the sum of the products
+        ones = torch.ones(max(n, 1), dtype=torch.float64, device=_dev())
+        r = C.c_double()
+        _h().call("itg_dot", C.c_int64(n), _ptr(out), _ptr(ones), C.byref(r))
+        return ITensor(Dense(torch.full((1,), r.value, dtype=torch.float64, device=_dev())), ())
     uni = A.store.uniform and B.store.uniform
     return ITensor(Diag(out[: (1 if uni else n)], uni), out_inds)
 
@@ -492,14 +665,17 @@ def svd(A: ITensor, *left_inds, **kw):
         Am = dense(Am)
     m, n = dim(left), dim(right)
     r = min(m, n)
-    U = empty_dev(m * r)
+    cplx = Am.is_complex
+    U = empty_dev(m * r, cplx)
     S = empty_dev(r)
-    V = empty_dev(n * r)
+    V = empty_dev(n * r, cplx)
     k = C.c_int64()
     te = C.c_double()
     dc = C.c_double()
     maxdim, mindim, cutoff, ab, rel, legacy = _trunc_args(m, n, kw)
-    _h().call("itg_svd_trunc", C.c_int64(m), C.c_int64(n), _ptr(Am.store.data), C.c_int64(m),
+    # complex: A ~ U S V^H (so U * S * dag(V) rebuilds A, test/test_cuitensor.jl:100-106)
+    _h().call("itg_svd_trunc_z" if cplx else "itg_svd_trunc", C.c_int64(m), C.c_int64(n), _ptr(Am.store.data),
+              C.c_int64(m),
               C.c_int64(maxdim), C.c_int64(mindim), C.c_double(cutoff), ab, rel, legacy,
               _ptr(U), _ptr(S), _ptr(V), C.byref(k), C.byref(te), C.byref(dc))
     kk = int(k.value)
@@ -522,6 +698,7 @@ def factorize(A: ITensor, *left_inds, ortho: str = "left", **kw):
     precision ("fp64" / "split") of the products.  Returns (L, R, spec).
     """
     _require_cuda(A)
+    _require_real(A, "factorize")
     if len(left_inds) == 1 and isinstance(left_inds[0], (list, tuple)):
         left_inds = tuple(left_inds[0])
     left = [i for i in A.inds if i in left_inds]
@@ -568,6 +745,7 @@ def eigen(A: ITensor, left_inds, right_inds, **kw):
     indices (*right_inds, r), so that M ~ U D U^T.
     """
     _require_cuda(A)
+    _require_real(A, "eigen")
     left, right = list(left_inds), list(right_inds)
     Am = permute(A, *left, *right)
     n = dim(left)
@@ -600,8 +778,10 @@ def qr(A: ITensor, *left_inds):
     Am = permute(A, *left, *right)
     m, n = dim(left), dim(right)
     r = min(m, n)
-    Q = empty_dev(m * r)
-    R = empty_dev(r * n)
-    _h().call("itg_qr", C.c_int64(m), C.c_int64(n), _ptr(Am.store.data), C.c_int64(m), _ptr(Q), _ptr(R))
+    cplx = Am.is_complex
+    Q = empty_dev(m * r, cplx)
+    R = empty_dev(r * n, cplx)
+    _h().call("itg_qr_z" if cplx else "itg_qr", C.c_int64(m), C.c_int64(n), _ptr(Am.store.data), C.c_int64(m),
+              _ptr(Q), _ptr(R))
     q = Index(r, "Link,qr")
     return ITensor(Dense(Q), (*left, q)), ITensor(Dense(R), (q, *right))

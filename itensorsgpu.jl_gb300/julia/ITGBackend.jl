@@ -51,50 +51,55 @@ end
 _dims(T) = Int64[dims(inds(T))...]
 _labels(l) = Int32[l...]
 
+# element types: ITG_F64 = 0, ITG_C64 = 1 (ComplexF64, interleaved like Julia's own layout)
+const ITGElT = Union{Float64,ComplexF64}
+_dt(::Type{Float64}) = Cint(0)
+_dt(::Type{ComplexF64}) = Cint(1)
+_vptr(T) = reinterpret(CuPtr{Cvoid}, pointer(data(store(T))))
+
 # contract!! (src/tensor/cudense.jl:83-110): one call covers the scalar,
-# outer-product and general cases.
-function contract!!(R::CuDenseTensor{Float64,NR}, labelsR::NTuple{NR},
-                    T1::CuDenseTensor{Float64,N1}, labelsT1::NTuple{N1},
-                    T2::CuDenseTensor{Float64,N2}, labelsT2::NTuple{N2}) where {NR,N1,N2}
-    st = ccall((:itg_contract, libitg), Cint,
-               (Ptr{Cvoid}, Cint, Cdouble,
-                CuPtr{Float64}, Cint, Ptr{Int64}, Ptr{Int32},
-                CuPtr{Float64}, Cint, Ptr{Int64}, Ptr{Int32},
-                Cdouble,
-                CuPtr{Float64}, Cint, Ptr{Int64}, Ptr{Int32}, Cint),
-               handle(), 0, 1.0,
-               pointer(data(store(T1))), N1, _dims(T1), _labels(labelsT1),
-               pointer(data(store(T2))), N2, _dims(T2), _labels(labelsT2),
-               0.0,
-               pointer(data(store(R))), NR, _dims(R), _labels(labelsR), precision[])
-    check(st, "itg_contract")
+# outer-product and general cases, real, complex and mixed operands (R is
+# ComplexF64 when either operand is).
+function contract!!(R::CuDenseTensor{<:ITGElT,NR}, labelsR::NTuple{NR},
+                    T1::CuDenseTensor{E1,N1}, labelsT1::NTuple{N1},
+                    T2::CuDenseTensor{E2,N2}, labelsT2::NTuple{N2}) where {NR,N1,N2,E1<:ITGElT,E2<:ITGElT}
+    st = ccall((:itg_contract_z, libitg), Cint,
+               (Ptr{Cvoid}, Cint, Cint, Ptr{Cdouble},
+                CuPtr{Cvoid}, Cint, Ptr{Int64}, Ptr{Int32},
+                CuPtr{Cvoid}, Cint, Ptr{Int64}, Ptr{Int32},
+                Ptr{Cdouble},
+                CuPtr{Cvoid}, Cint, Ptr{Int64}, Ptr{Int32}, Cint),
+               handle(), _dt(E1), _dt(E2), Cdouble[1.0, 0.0],
+               _vptr(T1), N1, _dims(T1), _labels(labelsT1),
+               _vptr(T2), N2, _dims(T2), _labels(labelsT2),
+               Cdouble[0.0, 0.0],
+               _vptr(R), NR, _dims(R), _labels(labelsR), precision[])
+    check(st, "itg_contract_z")
     return R
 end
 
 # permute! (src/tensor/cudense.jl:447-500)
-function Base.permute!(B::CuDenseTensor{Float64,N}, A::CuDenseTensor{Float64,N}) where {N}
+function Base.permute!(B::CuDenseTensor{ElT,N}, A::CuDenseTensor{ElT,N}) where {ElT<:ITGElT,N}
     ia = inds(A); ib = inds(B)
     la = Int32[1:N...]
     lb = Int32[findfirst(==(i), ia) for i in ib]
     st = ccall((:itg_permute, libitg), Cint,
-               (Ptr{Cvoid}, Cint, Cdouble, CuPtr{Float64}, Cint, Ptr{Int64}, Ptr{Int32},
-                CuPtr{Float64}, Ptr{Int32}),
-               handle(), 0, 1.0, pointer(data(store(A))), N, _dims(A), la,
-               pointer(data(store(B))), lb)
+               (Ptr{Cvoid}, Cint, Cdouble, CuPtr{Cvoid}, Cint, Ptr{Int64}, Ptr{Int32},
+                CuPtr{Cvoid}, Ptr{Int32}),
+               handle(), _dt(ElT), 1.0, _vptr(A), N, _dims(A), la, _vptr(B), lb)
     check(st, "itg_permute")
     return vec(data(store(B)))
 end
 
 # Base.:+ on CuDense tensors (src/tensor/cudense.jl:333-361): B .= A(permuted) + B
-function Base.:+(B::CuDenseTensor{Float64,N}, A::CuDenseTensor{Float64,N}) where {N}
+function Base.:+(B::CuDenseTensor{ElT,N}, A::CuDenseTensor{ElT,N}) where {ElT<:ITGElT,N}
     ia = inds(A); ib = inds(B)
     la = Int32[findfirst(==(i), ib) for i in ia]
     lb = Int32[1:N...]
     st = ccall((:itg_axpby_permuted, libitg), Cint,
-               (Ptr{Cvoid}, Cint, Cdouble, CuPtr{Float64}, Cint, Ptr{Int64}, Ptr{Int32},
-                Cdouble, CuPtr{Float64}, Ptr{Int32}, CuPtr{Float64}),
-               handle(), 0, 1.0, pointer(data(store(A))), N, _dims(A), la,
-               1.0, pointer(data(store(B))), lb, pointer(data(store(B))))
+               (Ptr{Cvoid}, Cint, Cdouble, CuPtr{Cvoid}, Cint, Ptr{Int64}, Ptr{Int32},
+                Cdouble, CuPtr{Cvoid}, Ptr{Int32}, CuPtr{Cvoid}),
+               handle(), _dt(ElT), 1.0, _vptr(A), N, _dims(A), la, 1.0, _vptr(B), lb, _vptr(B))
     check(st, "itg_axpby_permuted")
     return B
 end

@@ -343,3 +343,44 @@ def test_factorize_trunc(gpu, m, n, method, prec, ortho):
         # by a small multiple of the smallest kept singular value
         assert np.abs(prod - ref).max() < 10 * Sf[kk - 1]
         assert abs(te.value - float(np.sum(Sf[kk:] ** 2))) < 1e-13 * (r - kk + 1) * So[0] ** 2
+
+
+@pytest.mark.parametrize("pre", [1, 0])
+@pytest.mark.parametrize("shape", [(40, 30), (6, 20), (50, 300)])
+def test_jacobi_rank_deficient_converges(gpu, pre, shape):
+    """Exactly rank-deficient inputs (the bond matrices of a direct sum of two
+    MPS or MPO): the FP64 Jacobi must settle (noise-level columns are not
+    rotated) and the rotation factor must stay orthonormal."""
+    from itg import _lib
+    import torch
+    h = _lib.handle(0)
+    m, n = shape
+    rng = np.random.default_rng(m * n + pre)
+    X = rng.standard_normal((m, 3)) @ rng.standard_normal((3, n))          # rank 3
+    X[:, : n // 2] = np.round(X[:, : n // 2])                              # integer block, still low rank
+    X = np.concatenate([X[:, : n // 2], X[:, : n - n // 2]], axis=1)       # duplicated columns
+    p = lambda t: C.c_void_p(t.data_ptr())
+    A = torch.from_numpy(np.asfortranarray(X).ravel(order="F").copy()).cuda()
+    r = min(m, n)
+    L = torch.empty(max(m, n) * r, dtype=torch.float64, device="cuda")
+    S = torch.empty(r, dtype=torch.float64, device="cuda")
+    Cm = torch.empty(max(m, n) * r, dtype=torch.float64, device="cuda")
+    k = C.c_int64()
+    h.call("itg_set_svd_options", pre, 0)
+    try:
+        for ortho in (0, 1):
+            h.call("itg_factorize_trunc", C.c_int64(m), C.c_int64(n), p(A), C.c_int64(m), C.c_int64(r), C.c_int64(1),
+                   C.c_double(0.0), 0, 1, 0, ortho, 1, 0, p(L), p(S), p(Cm), C.byref(k), None, None)
+            kk = k.value
+            if ortho == 0:
+                Lh = L[: m * kk].cpu().numpy().reshape(kk, m).T
+                Ch = Cm[: kk * n].cpu().numpy().reshape(n, kk).T
+                rec = Lh @ Ch
+            else:
+                Lh = L[: n * kk].cpu().numpy().reshape(kk, n).T
+                Ch = Cm[: m * kk].cpu().numpy().reshape(kk, m).T
+                rec = Ch @ Lh.T
+            assert np.abs(Lh.T @ Lh - np.eye(kk)).max() < 1e-13
+            assert np.abs(rec - X).max() < 1e-12 * np.abs(X).max()
+    finally:
+        h.call("itg_set_svd_options", 1, 0)
