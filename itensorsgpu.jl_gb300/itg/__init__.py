@@ -8,7 +8,7 @@ the first operation.
 from ._lib import (DimensionMismatch, ITGError, NotConverged, PREC_FP64, PREC_SPLIT, Handle,
                    handle, load_library)
 from .tensor import (Diag, Dense, ITensor, ITensor_host, Index, Spectrum, contract, cpu, cu,
-                     cuITensor, dag, delta, dense, diagITensor, dim, eigen, get_precision, norm, permute,
+                     cuITensor, dag, delta, dense, diagITensor, dim, eigen, factorize, get_precision, norm, permute,
                      prime, qr, randomCuITensor, set_precision, svd)
 from .mps import (MPO, MPS, cuMPO, cuMPS, heisenberg_mpo, j1j2_mpo, mpo_dense_matrix, op, ops,
                   productCuMPS, productMPS_host, randomCuMPS, siteinds, spin_ops, tfim_mpo, xxz_mpo)
