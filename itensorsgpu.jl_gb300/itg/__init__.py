@@ -18,6 +18,7 @@ from .batched import dmrg_batched
 from .mpsops import (ArgumentError, add, apply, inner, leftlim, linkind, maxlinkdim, normalize_,
                      orthogonalize_, randomCuMPO, replacebond_, rightlim, siteind, truncate_)
 
+from .solvers import ITensorMap, davidson
 from .tensor import complex_
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -204,3 +204,26 @@ def test_diag_contractions_mixed_types(gpu, t1, t2):
     # UniformDiag * Matrix
     C4 = gpu.diagITensor([2.0 + (0j if t2 is complex else 0)], i, i.prime(), uniform=True) * Aij
     assert rel(C4.array(i.prime(), j), 2.0 * a) < 1e-14
+
+
+@pytest.mark.parametrize("cplx_start", [False, True])
+def test_davidson_itensor_map(gpu, cplx_start):
+    """test/test_cuiterativesolvers.jl: davidson on the Hermitian map
+    v -> noprime(A * v) with A = B * dag(B) (complex), from a real or complex
+    start; plus a real symmetric map."""
+    i = gpu.Index(10, "i")
+    rng = np.random.default_rng(3)
+    B = crand(rng, (10, 10))
+    Hm = B @ B.conj().T
+    A = gpu.cuITensor(Hm, i, i.prime())
+    M = gpu.ITensorMap(A)
+    v0 = gpu.randomCuITensor(complex, i, seed=5) if cplx_start else gpu.randomCuITensor(i, seed=5)
+    lam, v = gpu.davidson(M, v0, maxiter=10)
+    assert rel(M(v).array(), lam * v.array()) < 1e-10
+    assert lam == pytest.approx(np.linalg.eigvalsh(Hm.T)[0], rel=1e-10)
+    S = rng.standard_normal((12, 12))
+    S = S + S.T
+    j = gpu.Index(12, "j")
+    lam, v = gpu.davidson(gpu.ITensorMap(gpu.cuITensor(S, j, j.prime())), gpu.randomCuITensor(j, seed=6), maxiter=12)
+    assert lam == pytest.approx(np.linalg.eigvalsh(S)[0], rel=1e-10)
+    assert not v.is_complex
