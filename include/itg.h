@@ -185,6 +185,14 @@ ITG_API int itg_svd_trunc_z(itg_handle* h, int64_t m, int64_t n, const double* A
                     int legacy_gpu, double* U, double* S, double* V, int64_t* k, double* truncerr,
                     double* docut);
 
+/* Eigendecomposition of the Hermitian complex n x n matrix A: A = U diag(D)
+ * U^H with D real descending, U n x n complex, then truncation of D as a
+ * spectrum (as itg_eigh_trunc).  Replaces eigen(::Hermitian) on ComplexF64
+ * (src/tensor/culinearalgebra.jl:74-108). */
+ITG_API int itg_eigh_trunc_z(itg_handle* h, int64_t n, const double* A, int64_t lda,
+                     int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff, int doRelCutoff,
+                     int legacy_gpu, double* D, double* U, int64_t* k, double* truncerr, double* docut);
+
 /* Thin QR of the complex m x n matrix A: A = Q R, Q m x r with orthonormal
  * columns, R r x n, r = min(m, n) (complex Gram-Schmidt, re-orthogonalised
  * once).  Replaces qr on CuDenseTensor{ComplexF64}

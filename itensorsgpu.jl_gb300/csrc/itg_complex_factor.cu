@@ -1,7 +1,9 @@
 // Factorisations of complex (ITG_C64, interleaved re/im) matrices: truncated
-// SVD by one-sided complex Jacobi and thin QR by complex Gram-Schmidt with one
-// full re-orthogonalisation.  Replace svd / qr on CuDenseTensor{ComplexF64}
-// (src/tensor/culinearalgebra.jl:33-72,110-121; test/test_cuitensor.jl:100-130).
+// SVD and Hermitian eigendecomposition by one-sided complex Jacobi, thin QR
+// by complex Gram-Schmidt with one full re-orthogonalisation.  Replace svd /
+// eigen / qr on CuDenseTensor{ComplexF64} (src/tensor/culinearalgebra.jl:33-121,
+// whose eigen takes the Hermitian route for complex input at :84-85;
+// test/test_cuitensor.jl:100-130).
 //
 // Complex Jacobi rotation of the column pair (a_p, a_q) with alpha = |a_p|^2,
 // beta = |a_q|^2, gamma = a_p^H a_q = |gamma| e^{i phi}: scaling a_q by
@@ -155,6 +157,47 @@ __global__ void k_zgather(const double* __restrict__ src, int64_t rows, const in
     d[i] = s[i] * f;
 }
 
+// max over rows of sum_j |A_ij| (complex modulus): a bound on |eigenvalues|
+__global__ void k_zgershgorin(const double* __restrict__ A, int64_t lda, int64_t n, double* out) {
+  __shared__ double sh[32];
+  double best = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    double s = 0.0;
+    for (int64_t j = 0; j < n; ++j) s += hypot(A[2 * (i + j * lda)], A[2 * (i + j * lda) + 1]);
+    best = fmax(best, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = best;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) b = fmax(b, sh[i]);
+    *out = b;
+  }
+}
+
+// W[i, i] += shift (real part), complex n x n
+__global__ void k_zshift_diag(double* __restrict__ W, int64_t n, double shift) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    W[2 * (i + i * n)] += shift;
+}
+
+// D[r] = sig[order[r]] - shift (descending), P = D
+__global__ void k_zshift_rank(const double* __restrict__ sig, int n, double shift, int* __restrict__ order,
+                              double* __restrict__ D, double* __restrict__ P) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const double v = sig[j];
+    int r = 0;
+    for (int i = 0; i < n; ++i) {
+      const double u = sig[i];
+      r += (u > v) || (u == v && i < j);
+    }
+    order[r] = j;
+    D[r] = v - shift;
+    P[r] = v - shift;
+  }
+}
+
 // ---- complex CGS2 QR
 // hc[i] = Q[:, i]^H q for i < blockIdx range (one block per i)
 __global__ void __launch_bounds__(256)
@@ -284,6 +327,84 @@ extern "C" int itg_svd_trunc_z(itg_handle* h, int64_t m, int64_t n, const double
   if (docut) *docut = h->pinned[2];
   if (sweeps >= ZJ_MAX_SWEEPS && nn > 1)
     return itg_fail(h, ITG_ERR_NOTCONVERGED, "complex Jacobi SVD did not converge in %d sweeps", sweeps);
+  return ITG_OK;
+}
+
+// Hermitian eigendecomposition: B = A + c I with c = max row sum of |A| is
+// positive semidefinite, so its one-sided Jacobi B V = W gives |w_j| =
+// lambda_j + c with V the eigenvectors (the route of the real itg_eigh_trunc).
+extern "C" int itg_eigh_trunc_z(itg_handle* h, int64_t n, const double* A, int64_t lda, int64_t maxdim,
+                                int64_t mindim, double cutoff, int absoluteCutoff, int doRelCutoff, int legacy_gpu,
+                                double* D, double* U, int64_t* k, double* truncerr, double* docut) {
+  if (!h || n < 0 || lda < n || !A || !D || !U) return ITG_ERR_INVALID;
+  if (n == 0) {
+    if (k) *k = 0;
+    if (truncerr) *truncerr = 0;
+    if (docut) *docut = 0;
+    return ITG_OK;
+  }
+  if (n > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "complex eigh: n too large");
+  size_t off = 0;
+  auto take = [&](size_t bytes) { size_t o = off; off += itg_align256(bytes); return o; };
+  const size_t oW = take(16 * n * n), oV = take(16 * n * n), oSig = take(8 * n), oP = take(8 * n),
+               oOrd = take(sizeof(int) * n), oOut = take(4 * 8), oFlag = take(sizeof(int)), oC = take(8),
+               oRed = take(8 * 1024);
+  ITG_TRY(itg_scratch_reserve(h, off));
+  char* base = (char*)h->scratch;
+  double* W = (double*)(base + oW);
+  double* Vw = (double*)(base + oV);
+  double* sig = (double*)(base + oSig);
+  double* P = (double*)(base + oP);
+  int* order = (int*)(base + oOrd);
+  double* out3 = (double*)(base + oOut);
+  int* flag = (int*)(base + oFlag);
+  double* cdev = (double*)(base + oC);
+  double* red = (double*)(base + oRed);
+  k_zgershgorin<<<1, 1024, 0, h->stream>>>(A, lda, n, cdev);
+  ITG_CHECK_LAUNCH(h);
+  ITG_CUDA(h, cudaMemcpyAsync(h->pinned, cdev, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  const double shift = h->pinned[0] > 0.0 ? h->pinned[0] : 1.0;
+  k_zload<<<itg_blocks_for(n * n, 256, h->num_sms * 16), 256, 0, h->stream>>>(A, lda, n, n, 0, W);
+  k_zshift_diag<<<itg_blocks_for(n, 256, 64), 256, 0, h->stream>>>(W, n, shift);
+  k_zidentity<<<itg_blocks_for(n * n, 256, h->num_sms * 8), 256, 0, h->stream>>>((int)n, Vw);
+  ITG_CHECK_LAUNCH(h);
+  ITG_TRY(itg::nrm2_dev(h, 2 * n * n, W, red + 1000, red));
+  ITG_CUDA(h, cudaMemcpyAsync(h->pinned, red + 1000, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  const double fro = h->pinned[0];
+  const double tol = EPS * sqrt((double)n);
+  const double amin_conv = (10.0 * EPS * fro) * (10.0 * EPS * fro);
+  const int np = (int)(n + (n & 1));
+  int* hp = (int*)h->pinned;
+  int sweeps = n > 1 ? ZJ_MAX_SWEEPS : 0;
+  for (int sw = 0; sw < ZJ_MAX_SWEEPS && n > 1; ++sw) {
+    ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+    for (int step = 0; step < np - 1; ++step)
+      k_zjacobi_step<<<np / 2, 256, 0, h->stream>>>(W, n, (int)n, Vw, tol, amin_conv, step, flag);
+    ITG_CHECK_LAUNCH(h);
+    ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hp[0] == 0) {
+      sweeps = sw + 1;
+      break;
+    }
+  }
+  k_zcol_norms<<<(unsigned)n, 256, 0, h->stream>>>(W, n, sig);
+  k_zshift_rank<<<itg_blocks_for(n, 256, 1024), 256, 0, h->stream>>>(sig, (int)n, shift, order, D, P);
+  ITG_CHECK_LAUNCH(h);
+  ITG_TRY(itg::truncate_dev(h, P, n, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, out3));
+  dim3 g2(itg_blocks_for(2 * n, 256, 64), (unsigned)n);
+  k_zgather<<<g2, 256, 0, h->stream>>>(Vw, n, order, sig, 0, (int)n, U);
+  ITG_CHECK_LAUNCH(h);
+  h->last_sweeps = sweeps;
+  ITG_CUDA(h, cudaMemcpyAsync(h->pinned, out3, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (k) *k = (int64_t)h->pinned[0];
+  if (truncerr) *truncerr = h->pinned[1];
+  if (docut) *docut = h->pinned[2];
+  if (sweeps >= ZJ_MAX_SWEEPS)
+    return itg_fail(h, ITG_ERR_NOTCONVERGED, "complex Jacobi eigensolver did not converge in %d sweeps", sweeps);
   return ITG_OK;
 }
 

@@ -81,6 +81,8 @@ SIGNATURES = {
     "itg_svd_trunc_z": (C.c_int, [_P, C.c_int64, C.c_int64, _P, C.c_int64, C.c_int64, C.c_int64,
                                   C.c_double, C.c_int, C.c_int, C.c_int, _P, _P, _P, _I64P, _DP, _DP]),
     "itg_qr_z": (C.c_int, [_P, C.c_int64, C.c_int64, _P, C.c_int64, _P, _P]),
+    "itg_eigh_trunc_z": (C.c_int, [_P, C.c_int64, _P, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_int,
+                                   C.c_int, C.c_int, _P, _P, _I64P, _DP, _DP]),
     "itg_real_to_complex": (C.c_int, [_P, C.c_int64, _P, _P]),
     "itg_zscal": (C.c_int, [_P, C.c_int64, _DP, _P]),
     "itg_permute": (C.c_int, [_P, C.c_int, C.c_double, _P, C.c_int, _I64P, _I32P, _P, _I32P]),

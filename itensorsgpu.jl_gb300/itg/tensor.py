@@ -249,7 +249,7 @@ class ITensor:
 def _require_real(A, what):
     if A.is_complex:
         raise TypeError(f"{what} of a ComplexF64 tensor is not implemented (complex storage supports "
-                        "contraction, permutation, sums, scaling, norm, dag, svd and qr)")
+                        "contraction, permutation, sums, scaling, norm, dag, svd, eigen and qr)")
 
 
 def _require_cuda(*ts):
@@ -740,24 +740,27 @@ def factorize(A: ITensor, *left_inds, ortho: str = "left", **kw):
 def eigen(A: ITensor, left_inds, right_inds, **kw):
     """Hermitian eigendecomposition (culinearalgebra.jl:74-108).
 
-    A is viewed as the matrix M[left, right] (symmetric).  Returns (D, U, spec)
-    with D a CuDiag tensor on (l, r) holding descending eigenvalues, and U with
-    indices (*right_inds, r), so that M ~ U D U^T.
+    A is viewed as the matrix M[left, right] (symmetric, or Hermitian for
+    ComplexF64).  Returns (D, U, spec) with D a real CuDiag tensor on (l, r)
+    holding descending eigenvalues, and U with indices (*right_inds, r), so
+    that M ~ U D U^H (M U = U D).
     """
     _require_cuda(A)
-    _require_real(A, "eigen")
     left, right = list(left_inds), list(right_inds)
     Am = permute(A, *left, *right)
     n = dim(left)
     if dim(right) != n:
         raise DimensionMismatch(2, "eigen: square matrix required")
+    cplx = Am.is_complex
+    if "maxdim" not in kw and "cutoff" not in kw:
+        kw = dict(kw, mindim=n)   # no truncation keywords: keep every eigenvalue, negative ones too
     D = empty_dev(n)
-    U = empty_dev(n * n)
+    U = empty_dev(n * n, cplx)
     k = C.c_int64()
     te = C.c_double()
     dc = C.c_double()
     maxdim, mindim, cutoff, ab, rel, legacy = _trunc_args(n, n, kw)
-    _h().call("itg_eigh_trunc", C.c_int64(n), _ptr(Am.store.data), C.c_int64(n),
+    _h().call("itg_eigh_trunc_z" if cplx else "itg_eigh_trunc", C.c_int64(n), _ptr(Am.store.data), C.c_int64(n),
               C.c_int64(maxdim), C.c_int64(mindim), C.c_double(cutoff), ab, rel, legacy,
               _ptr(D), _ptr(U), C.byref(k), C.byref(te), C.byref(dc))
     kk = int(k.value)

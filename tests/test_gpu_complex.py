@@ -227,3 +227,24 @@ def test_davidson_itensor_map(gpu, cplx_start):
     lam, v = gpu.davidson(gpu.ITensorMap(gpu.cuITensor(S, j, j.prime())), gpu.randomCuITensor(j, seed=6), maxiter=12)
     assert lam == pytest.approx(np.linalg.eigvalsh(S)[0], rel=1e-10)
     assert not v.is_complex
+
+
+def test_complex_hermitian_eigen(gpu):
+    """eigen on a ComplexF64 Hermitian matrix (culinearalgebra.jl:84-85): M U = U D,
+    U unitary, eigenvalues as LAPACK's; truncation keeps the largest."""
+    n = 24
+    rng = np.random.default_rng(9)
+    B = crand(rng, (n, n))
+    Hm = B + B.conj().T
+    i = gpu.Index(n, "i")
+    A = gpu.cuITensor(Hm, i, i.prime())
+    D, U, spec = gpu.eigen(A, [i], [i.prime()])
+    r = U.inds[-1]
+    Um = U.array(i.prime(), r)
+    d = gpu.dense(D).array().diagonal()
+    assert np.abs(Um.conj().T @ Um - np.eye(n)).max() < 1e-13
+    assert rel(Hm @ Um, Um * d[None, :]) < 1e-13
+    assert np.abs(d - np.linalg.eigvalsh(Hm)[::-1]).max() < 1e-12 * np.abs(d).max()
+    D5, U5, _ = gpu.eigen(A, [i], [i.prime()], maxdim=5)
+    assert U5.inds[-1].dim == 5
+    assert np.abs(gpu.dense(D5).array().diagonal() - d[:5]).max() < 1e-12 * np.abs(d).max()
