@@ -718,7 +718,9 @@ def run_learned(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    # 200 matvecs (~0.8 s of split-form device time) so that the 200 ms clock
+    # sampler sees several samples inside the timed region
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="itg", choices=["itg", "reference"])
     ap.add_argument("--precision", default="both", choices=["both", "fp64", "split"])

@@ -36,7 +36,7 @@ import ctypes as C
 import numpy as np
 
 from . import tensor as T
-from ._lib import DimensionMismatch
+from ._lib import PREC_FP64, DimensionMismatch, i32arr, i64arr
 from .dmrg import _contract_raw, inner as _inner2
 from .mps import MPO, MPS
 from .tensor import Dense, ITensor, Index
@@ -62,6 +62,14 @@ def _pc(A: ITensor, la, B: ITensor, lb, lc):
                 raise DimensionMismatch(2, f"dimension of {lab!r} differs between operands")
     code = {lab: k + 1 for k, lab in enumerate(dims)}
     dC = tuple(dims[lab] for lab in lc)
+    if A.is_complex or B.is_complex:
+        out = T.empty_dev(int(np.prod(dC)) if dC else 1, True)
+        one, zero = (C.c_double * 2)(1.0, 0.0), (C.c_double * 2)(0.0, 0.0)
+        T._h().call("itg_contract_z", T._dt(A), T._dt(B), one, T._ptr(A.store.data), len(la), i64arr(A.dims),
+                    i32arr([code[x] for x in la]), T._ptr(B.store.data), len(lb), i64arr(B.dims),
+                    i32arr([code[x] for x in lb]), zero, T._ptr(out), len(lc), i64arr(dC),
+                    i32arr([code[x] for x in lc]), PREC_FP64)
+        return out, dC
     out = _contract_raw(T._h(), A.store.data, A.dims, [code[x] for x in la], B.store.data, B.dims,
                         [code[x] for x in lb], dC, [code[x] for x in lc])
     return out, dC
@@ -262,7 +270,17 @@ def inner(*args):
         for j in range(len(psi)):
             if phi[j].inds[1].dim != psi[j].inds[1].dim:
                 raise DimensionMismatch(2, f"inner: site {j} dimensions differ")
-        return _inner2(phi, psi)
+        phi, psi = T.cu(phi), T.cu(psi)
+        if not any(t.is_complex for t in phi.tensors + psi.tensors):
+            return _inner2(phi, psi)
+        # complex: E[a, b] -> sum conj(phi[a, s, a2]) E[a, b] psi[b, s, b2]
+        E = ITensor(Dense(T.empty_dev(1).fill_(1.0)), (Index(1), Index(1)))
+        for j in range(len(psi)):
+            t1, d1 = _pc(E, ("a", "b"), psi[j], ("b", "s", "b2"), ("a", "s", "b2"))
+            t1 = ITensor(Dense(t1), tuple(Index(d) for d in d1))
+            e, de = _pc(T.dag(phi[j]), ("a", "s", "a2"), t1, ("a", "s", "b2"), ("a2", "b2"))
+            E = ITensor(Dense(e), tuple(Index(d) for d in de))
+        return complex(E.store.data[0].item())
     if len(args) != 3:
         raise ArgumentError("inner takes (phi, psi) or (phi, A, psi)")
     phi, A, psi = (T.cu(x) for x in args)
@@ -277,9 +295,10 @@ def inner(*args):
         t1 = ITensor(Dense(t1), tuple(Index(d) for d in d1))
         t2, d2 = _pc(t1, ("a", "wl", "k", "b2"), W, tuple(wl), ("a", "o", "b2", "wr"))
         t2 = ITensor(Dense(t2), tuple(Index(d) for d in d2))
-        e, de = _pc(t2, ("a", "o", "b2", "wr"), P, ("a", "o", "a2"), ("a2", "wr", "b2"))
+        e, de = _pc(t2, ("a", "o", "b2", "wr"), T.dag(P), ("a", "o", "a2"), ("a2", "wr", "b2"))
         E = ITensor(Dense(e), tuple(Index(d) for d in de))
-    return float(E.store.data[0].item())
+    v = E.store.data[0].item()
+    return complex(v) if E.is_complex else float(v)
 
 
 def _mpo_roles(W: ITensor, ket_site: Index, phi_site: Index | None = None):
@@ -451,7 +470,8 @@ def add(A, B, **kw):
                 pos = [cur.index(w) for w in want]
                 t = T.permute(src, *[src.inds[p] for p in pos])
             parts.append(_with_inds(t, (links[j],) + tuple(mid) + (links[j + 1],)))
-        out.append(T._axpby(1.0, parts[1], 1.0, parts[0]))
+        out.append(T._axpby(1.0, parts[1], 1.0, parts[0]) if parts[0].is_complex == parts[1].is_complex
+                   else T._axpby(1.0, T.complex_(parts[1]), 1.0, T.complex_(parts[0])))
     if isinstance(A, MPS):
         C = MPS(out, A.sites, -1, N)
     else:

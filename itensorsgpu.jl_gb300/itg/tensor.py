@@ -246,12 +246,6 @@ class ITensor:
         return _axpby(-1.0, other, 1.0, self)
 
 
-def _require_real(A, what):
-    if A.is_complex:
-        raise TypeError(f"{what} of a ComplexF64 tensor is not implemented (complex storage supports "
-                        "contraction, permutation, sums, scaling, norm, dag, svd, eigen and qr)")
-
-
 def _require_cuda(*ts):
     for t in ts:
         if not t.is_cuda:
@@ -698,9 +692,22 @@ def factorize(A: ITensor, *left_inds, ortho: str = "left", **kw):
     precision ("fp64" / "split") of the products.  Returns (L, R, spec).
     """
     _require_cuda(A)
-    _require_real(A, "factorize")
     if len(left_inds) == 1 and isinstance(left_inds[0], (list, tuple)):
         left_inds = tuple(left_inds[0])
+    if A.is_complex:
+        # complex: through the complex SVD, A = U S V^H
+        if ortho not in ("left", "right"):
+            raise ValueError("factorize: ortho must be 'left' or 'right'")
+        skw = {k: v for k, v in kw.items() if k not in ("method", "precision", "tags")}
+        U, S, V, spec = svd(A, *left_inds, **skw)
+        u, v = U.inds[-1], V.inds[-1]
+        l = Index(u.dim, kw.get("tags", "Link,fac"))
+        right = [i for i in A.inds if i not in left_inds]
+        if ortho == "left":
+            Rt = contract(S, dag(V))                              # (u, right...)
+            return U.replaceinds([u], [l]), permute(Rt.replaceinds([u], [l]), l, *right), spec
+        Lt = contract(U, S)                                       # (left..., v)
+        return Lt.replaceinds([v], [l]), dag(V).replaceinds([v], [l]), spec
     left = [i for i in A.inds if i in left_inds]
     if len(left) != len(left_inds):
         raise DimensionMismatch(2, "factorize: left index not in tensor")

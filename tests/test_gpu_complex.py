@@ -135,8 +135,10 @@ def test_complex_itensor_ops(gpu):
     assert rel((A * Ck).array(), np.einsum("ijk,kl->ijl", a, Ck.array())) < 1e-14
     Rk = gpu.randomCuITensor(l, k, seed=8)
     assert rel((A * Rk).array(), np.einsum("ijk,lk->ijl", a, Rk.array())) < 1e-14
-    with pytest.raises(TypeError):
-        gpu.factorize(A, i, j)
+    L, R, spec = gpu.factorize(A, i, j, ortho="left")
+    assert rel((L * R).array(i, j, k), a) < 1e-13
+    L, R, spec = gpu.factorize(A, i, j, ortho="right", maxdim=2)
+    assert R.inds[-1].dim == 2
 
 
 @pytest.mark.parametrize("split", [("j", "l"), ("i", "l"), ("i", "j", "k")])
@@ -248,3 +250,37 @@ def test_complex_hermitian_eigen(gpu):
     D5, U5, _ = gpu.eigen(A, [i], [i.prime()], maxdim=5)
     assert U5.inds[-1].dim == 5
     assert np.abs(gpu.dense(D5).array().diagonal() - d[:5]).max() < 1e-12 * np.abs(d).max()
+
+
+def test_complex_mps_operations(gpu):
+    """MPS/MPO operations on complex site tensors: gauge moves, overlaps with
+    conjugated bras, MPO products, sums and truncation against dense vectors."""
+    N = 6
+    sites = [gpu.Index(2, "Site") for _ in range(N)]
+    rng = np.random.default_rng(4)
+
+    def cmps(seed, chi):
+        links = [gpu.Index(1)] + [gpu.Index(chi, "Link") for _ in range(N - 1)] + [gpu.Index(1)]
+        ts = [gpu.randomCuITensor(complex, links[j], sites[j], links[j + 1], seed=seed + j) for j in range(N)]
+        return gpu.MPS(ts, sites, -1, N)
+
+    def vec(psi):
+        return O.mps_vector([t.array() for t in gpu.cpu(psi).tensors])
+
+    phi, psi = cmps(10, 3), cmps(20, 4)
+    vphi, vpsi = vec(phi), vec(psi)
+    assert gpu.inner(phi, psi) == pytest.approx(np.vdot(vphi, vpsi), rel=1e-12)
+    gpu.orthogonalize_(psi, 2)
+    assert rel(vec(psi), vpsi) < 1e-12
+    gpu.orthogonalize_(psi, 0, maxdim=4)
+    assert rel(vec(psi), vpsi) < 1e-12
+    K = gpu.randomCuMPO(sites, seed=40)
+    Kc = gpu.MPO([t * (1 + 0.5j) for t in K.tensors], sites)
+    Km = O.mpo_matrix([t.array() for t in gpu.cpu(Kc).tensors])
+    assert gpu.inner(phi, Kc, psi) == pytest.approx(vphi.conj() @ Km @ vpsi, rel=1e-12)
+    out = gpu.contract(Kc, psi)
+    assert rel(vec(out), Km @ vpsi) < 1e-12
+    s = gpu.add(phi, psi)
+    assert rel(vec(s), vphi + vpsi) < 1e-12
+    gpu.truncate_(s, maxdim=7)
+    assert s.maxlinkdim() <= 7 and rel(vec(s), vphi + vpsi) < 1e-12
