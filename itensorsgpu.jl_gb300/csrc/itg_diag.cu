@@ -10,6 +10,8 @@
 // Every output element is written once; traffic is |C| + |T| + |d| doubles.
 #include "itg_internal.cuh"
 
+#include <algorithm>
+
 namespace {
 
 struct DiagDesc {
@@ -56,6 +58,52 @@ __global__ void k_diag_dense(const double* __restrict__ d, int uniform, const do
     v *= alpha;
     if (beta != 0.0) v = fma(beta, C[c], v);
     C[c] = v;
+  }
+}
+
+// Row form of k_diag_dense for the usual shape (one Df mode in C): C is
+// walked row by row along its mode 0, whose T stride is 1 (row_df = 0: the
+// diagonal index is fixed along the row) or which is the Df mode itself with
+// the diagonal's T stride sumDc (row_df = 1).  The index arithmetic runs
+// once per row, so the element loop is a plain scaled stream.
+struct RowDesc {
+  int n;                        // C modes 1.. (the row index decomposition)
+  int64_t dims[ITG_MAX_RANK];
+  int64_t strT[ITG_MAX_RANK];
+  int64_t strC[ITG_MAX_RANK];
+  int df;                       // position among them of the Df mode, -1 when it is mode 0
+};
+
+__global__ void k_diag_rows(const double* __restrict__ d, int uniform, const double* __restrict__ T,
+                            double* __restrict__ C, int64_t len, int64_t nrows, RowDesc r, int64_t sumDc,
+                            int64_t ndiag, double alpha, double beta) {
+  for (int64_t row = blockIdx.x; row < nrows; row += gridDim.x) {
+    int64_t rem = row, toff = 0, coff = 0, di = -1;
+    for (int k = 0; k < r.n; ++k) {
+      const int64_t q = rem / r.dims[k];
+      const int64_t idx = rem - q * r.dims[k];
+      rem = q;
+      coff += idx * r.strC[k];
+      if (k == r.df) di = idx;
+      else toff += idx * r.strT[k];
+    }
+    double* c = C + coff;
+    if (r.df >= 0) {  // diagonal index fixed along the row, T contiguous
+      const double dv = di < ndiag ? alpha * (uniform ? d[0] : d[di]) : 0.0;
+      const double* t = T + toff + di * sumDc;
+      for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+        double v = di < ndiag ? dv * t[i] : 0.0;
+        if (beta != 0.0) v = fma(beta, c[i], v);
+        c[i] = v;
+      }
+    } else {          // the row runs along the diagonal index
+      const double* t = T + toff;
+      for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+        double v = i < ndiag ? alpha * (uniform ? d[0] : d[i]) * t[i * sumDc] : 0.0;
+        if (beta != 0.0) v = fma(beta, c[i], v);
+        c[i] = v;
+      }
+    }
   }
 }
 
@@ -158,6 +206,32 @@ extern "C" int itg_diag_contract(itg_handle* h, int dtype, double alpha, const d
     }
   }
   if (totalC == 0) return ITG_OK;
+  // Row form: exactly one Df mode in C, and C's mode 0 either a T mode of
+  // stride 1 or that Df mode itself.
+  int ndf = 0;
+  for (int k = 0; k < rankC; ++k) ndf += desc.isDf[k];
+  const bool row0_t = rankC > 0 && !desc.isDf[0] && desc.strT[0] == 1;
+  const bool row0_df = rankC > 0 && desc.isDf[0];
+  if (ndf == 1 && (row0_t || row0_df) && dimsC[0] >= 32) {
+    RowDesc r;
+    r.n = 0;
+    r.df = -1;
+    int64_t sc = dimsC[0];
+    for (int k = 1; k < rankC; ++k) {
+      r.dims[r.n] = dimsC[k];
+      r.strT[r.n] = desc.strT[k];
+      r.strC[r.n] = sc;
+      if (desc.isDf[k]) r.df = r.n;
+      sc *= dimsC[k];
+      r.n++;
+    }
+    const int64_t len = dimsC[0], nrows = totalC / len;
+    const int threads = len >= 256 ? 256 : (len >= 64 ? 64 : 32);
+    const int blocks = (int)std::min<int64_t>(nrows, (int64_t)h->num_sms * 64);
+    k_diag_rows<<<blocks, threads, 0, h->stream>>>(d, uniform, T, C, len, nrows, r, desc.sumDc, ndiag, alpha, beta);
+    ITG_CHECK_LAUNCH(h);
+    return ITG_OK;
+  }
   k_diag_dense<<<itg_blocks_for(totalC, 256, h->num_sms * 16), 256, 0, h->stream>>>(
       d, uniform, T, C, totalC, desc, alpha, beta);
   ITG_CHECK_LAUNCH(h);
