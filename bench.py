@@ -437,6 +437,107 @@ def run_dmrg(args):
 
 
 # ------------------------------------------------------ HBM-bound operators + SVD
+def _contract_cases(count, seed):
+    """Seeded random pairwise contractions: ranks 3-6, random mode orders,
+    dims 2..2048 (powers of two), M, N, K groups of about 2^11 each."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+
+    def split_group(total_log2, nmodes):
+        # nmodes dims (powers of two, 2..2048) whose product is 2^total_log2
+        while True:
+            cuts = np.sort(rng.integers(0, total_log2 + 1, nmodes - 1))
+            parts = np.diff(np.concatenate([[0], cuts, [total_log2]]))
+            if np.all(parts >= 1) and np.all(parts <= 11):
+                return [1 << int(x) for x in parts]
+
+    cases = []
+    while len(cases) < count:
+        rA, rB = (int(x) for x in rng.integers(3, 7, 2))
+        nc = int(rng.integers(1, min(rA, rB)))
+        fa, fb = rA - nc, rB - nc
+        lm, ln, lk = (int(x) for x in rng.integers(10, 13, 3))
+        if not (fa <= lm <= 11 * fa and fb <= ln <= 11 * fb and nc <= lk <= 11 * nc):
+            continue
+        dm, dn, dk = split_group(lm, fa), split_group(ln, fb), split_group(lk, nc)
+        modes = list(range(1, fa + fb + nc + 1))
+        mM, mN, mK = modes[:fa], modes[fa:fa + fb], modes[fa + fb:]
+        dims = dict(zip(mM + mN + mK, dm + dn + dk))
+        mA = [int(x) for x in rng.permutation(mM + mK)]
+        mB = [int(x) for x in rng.permutation(mN + mK)]
+        mC = [int(x) for x in rng.permutation(mM + mN)]
+        cases.append((mA, mB, mC, dims, 2 ** (lm + ln + lk)))
+    return cases
+
+
+def run_contract(args):
+    """Config 2's random pairwise contractions: seeded rank 3-6 tensors with
+    random index orders and dims 2..2048, M, N, K ~ 2^10..2^12 (operands up to
+    ~270 MB, far above L2), each timed FP64 and split with CUDA events (warm, L2
+    flushed between launches).  FLOP = 2MNK; bound = max(FLOP / peak, bytes /
+    HBM) with bytes = 8 (|A| + |B| + |C|); split vs FP64 relative Frobenius
+    difference reported per case."""
+    import numpy as np
+    import torch
+    from itg import _lib
+    h = _lib.handle(0)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    peaks, src = measured_peaks()
+    fp64_peak = json.loads((REPO / "profiles" / "fp64_peak.json").read_text())["fp64_tflops"]
+    flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device="cuda")
+    out = []
+    for ci, (mA, mB, mC, dims, mnk) in enumerate(_contract_cases(args.contract_cases, 1234 + 2)):
+        dA, dB, dC = ([dims[m] for m in ms] for ms in (mA, mB, mC))
+        nA, nB, nC = (int(np.prod(d)) for d in (dA, dB, dC))
+        g = torch.Generator(device="cuda").manual_seed(ci)
+        A = torch.randn(nA, dtype=torch.float64, device="cuda", generator=g)
+        B = torch.randn(nB, dtype=torch.float64, device="cuda", generator=g)
+        res = {}
+        for name, prec in (("fp64", 0), ("split", 1)):
+            Cc = torch.empty(nC, dtype=torch.float64, device="cuda")
+
+            def launch():
+                h.call("itg_contract", 0, C.c_double(1.0), p(A), len(mA), _lib.i64arr(dA), _lib.i32arr(mA),
+                       p(B), len(mB), _lib.i64arr(dB), _lib.i32arr(mB), C.c_double(0.0), p(Cc), len(mC),
+                       _lib.i64arr(dC), _lib.i32arr(mC), prec)
+
+            for _ in range(2):
+                launch()
+            torch.cuda.synchronize()
+            reps = 3 if name == "fp64" else 10
+            ms = 0.0
+            for _ in range(reps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                launch()
+                e1.record()
+                torch.cuda.synchronize()
+                ms += e0.elapsed_time(e1)
+            ms /= reps
+            flop = 2.0 * mnk
+            tf = flop / (ms / 1e3) / 1e12
+            byts = 8.0 * (nA + nB + nC)
+            peak = fp64_peak if name == "fp64" else peaks["bf16_tflops"] / 28.0
+            bound_ms = max(flop / (peak * 1e12), byts / (peaks["hbm_gbs"] * 1e9)) * 1e3
+            res[name] = {"ms": ms, "tflops": tf, "frac_roofline": bound_ms / ms}
+            res[name + "_out"] = Cc
+        diff = torch.linalg.vector_norm(res["split_out"] - res["fp64_out"]) / torch.linalg.vector_norm(res["fp64_out"])
+        del res["split_out"], res["fp64_out"]
+        out.append({"A": list(zip(mA, dA)), "B": list(zip(mB, dB)), "C": list(zip(mC, dC)), "gflop": 2.0 * mnk / 1e9,
+                    **res, "split_vs_fp64": float(diff.item())})
+        del A, B
+    gm = lambda xs: float(np.exp(np.mean(np.log(xs))))
+    print(json.dumps({"metric": "random pairwise contractions (rank 3-6), TFLOP/s geometric mean, split form",
+                      "value": gm([c["split"]["tflops"] for c in out]), "unit": "TFLOP/s", "higher_is_better": True,
+                      "fp64_tflops_geomean": gm([c["fp64"]["tflops"] for c in out]),
+                      "fp64_peak_tflops": fp64_peak, "split_peak_fp64_equiv_tflops": peaks["bf16_tflops"] / 28.0,
+                      "peak_source": src, "cases": out,
+                      "config": {"workload": "random contractions", "cases": len(out), "seed": 1234 + 2},
+                      "dtype": "f64", "data": "synthetic (torch randn, seeded)"}), flush=True)
+    return 0
+
+
 def run_ops(args):
     """Rooflines of the HBM-bound operators and of the SVD kernels (config 2).
 
@@ -729,7 +830,9 @@ def main():
     ap.add_argument("--chi", type=int, default=CHI)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="heff", choices=["heff", "dmrg", "batched", "learned", "ops", "svd"])
+    ap.add_argument("--workload", default="heff",
+                    choices=["heff", "dmrg", "batched", "learned", "ops", "svd", "contract"])
+    ap.add_argument("--contract-cases", type=int, default=8)
     ap.add_argument("--dmrg-n", type=int, default=24)
     ap.add_argument("--dmrg-sweeps", type=int, default=2)
     ap.add_argument("--dmrg-cutoff", type=float, default=0.0)
@@ -759,6 +862,8 @@ def main():
         return run_batched(args)
     if args.workload == "learned":
         return run_learned(args)
+    if args.workload == "contract":
+        return run_contract(args)
     if args.workload == "ops":
         return run_ops(args)
     if args.workload == "svd":
