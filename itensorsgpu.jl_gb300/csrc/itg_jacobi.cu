@@ -229,12 +229,19 @@ __host__ __device__ inline T conv_tol(T tol) {
   return sizeof(T) == 8 ? T(4) * tol : tol;
 }
 
-template <class T, int WB>
-__global__ void __launch_bounds__(JB_THREADS)
+// Short FP64 columns (m <= JB_SMALL_M) run one warp per pair (THREADS =
+// 32 WB): the pair's sums then come from warp shuffles alone, which saves a
+// shared-memory reduction and one of the two barriers of every round
+// (measured at n = 378: 104 -> 82 ms per FP64 split; the FP32 Jacobi of the
+// mixed method was slower that way, 20.4 -> 22.7 ms, and keeps 512 threads).
+constexpr int64_t JB_SMALL_M = 1024;
+
+template <class T, int WB, int THREADS>
+__global__ void __launch_bounds__(THREADS)
 k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T tol_conv, T amin,
                     T amin_conv, int step, int first, int* __restrict__ rotated) {
   constexpr int C2 = 2 * WB;              // local columns
-  constexpr int TP = JB_THREADS / WB;     // threads per pair
+  constexpr int TP = THREADS / WB;        // threads per pair
   constexpr int WPG = TP / 32;            // warps per pair group
   extern __shared__ __align__(16) unsigned char jb_smem[];
   T* cols = (T*)jb_smem;                  // [C2][m]
@@ -255,12 +262,12 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
     T* dst = cols + (int64_t)c * m;
     if (gc >= 0) {
       const T* src = W + (int64_t)gc * m;
-      for (int64_t i = t; i < m; i += JB_THREADS) dst[i] = src[i];
+      for (int64_t i = t; i < m; i += THREADS) dst[i] = src[i];
     } else {
-      for (int64_t i = t; i < m; i += JB_THREADS) dst[i] = T(0);
+      for (int64_t i = t; i < m; i += THREADS) dst[i] = T(0);
     }
   }
-  for (int i = t; i < C2 * C2; i += JB_THREADS) Q[i] = (i % (C2 + 1) == 0) ? T(1) : T(0);
+  for (int i = t; i < C2 * C2; i += THREADS) Q[i] = (i % (C2 + 1) == 0) ? T(1) : T(0);
   __syncthreads();
   const int g = t / TP, lt = t % TP, wg = lt / 32, lane = t & 31;
   const int rounds = first ? C2 - 1 : WB;
@@ -290,20 +297,22 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
     a = jp_warp_sum(a);
     b = jp_warp_sum(b);
     gg = jp_warp_sum(gg);
-    if (lane == 0) {
-      red[(g * WPG + wg) * 3 + 0] = a;
-      red[(g * WPG + wg) * 3 + 1] = b;
-      red[(g * WPG + wg) * 3 + 2] = gg;
-    }
-    __syncthreads();
-    a = 0;
-    b = 0;
-    gg = 0;
+    if constexpr (WPG > 1) {
+      if (lane == 0) {
+        red[(g * WPG + wg) * 3 + 0] = a;
+        red[(g * WPG + wg) * 3 + 1] = b;
+        red[(g * WPG + wg) * 3 + 2] = gg;
+      }
+      __syncthreads();
+      a = 0;
+      b = 0;
+      gg = 0;
 #pragma unroll
-    for (int w = 0; w < WPG; ++w) {
-      a += red[(g * WPG + w) * 3 + 0];
-      b += red[(g * WPG + w) * 3 + 1];
-      gg += red[(g * WPG + w) * 3 + 2];
+      for (int w = 0; w < WPG; ++w) {
+        a += red[(g * WPG + w) * 3 + 0];
+        b += red[(g * WPG + w) * 3 + 1];
+        gg += red[(g * WPG + w) * 3 + 2];
+      }
     }
     const bool rot = !(a <= amin || b <= amin || fabs(gg) <= tol * sqrt(a) * sqrt(b));
     if (rot) {
@@ -333,13 +342,13 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
     if (gc < 0) continue;
     const T* src = cols + (int64_t)c * m;
     T* dst = W + (int64_t)gc * m;
-    for (int64_t i = t; i < m; i += JB_THREADS) dst[i] = src[i];
+    for (int64_t i = t; i < m; i += THREADS) dst[i] = src[i];
   }
   // V[:, cols] <- V[:, cols] Q, one row per thread
   int gcs[C2];
 #pragma unroll
   for (int c = 0; c < C2; ++c) gcs[c] = gcol(c);
-  for (int row = t; row < n; row += JB_THREADS) {
+  for (int row = t; row < n; row += THREADS) {
     T v[C2];
 #pragma unroll
     for (int c = 0; c < C2; ++c) v[c] = gcs[c] >= 0 ? V[row + (int64_t)gcs[c] * n] : T(0);
@@ -411,14 +420,14 @@ size_t jb_smem_bytes(int64_t m) {
   return sizeof(T) * ((size_t)2 * WB * m + (size_t)4 * WB * WB + (size_t)WB * (JB_THREADS / WB / 32) * 3);
 }
 
-template <class T, int WB>
-int jb_run(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, T amin_conv, int max_sweeps, int* flag,
-           int* sweeps) {
+template <class T, int WB, int THREADS>
+int jb_run_t(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, T amin_conv, int max_sweeps, int* flag,
+             int* sweeps) {
   const size_t smem = jb_smem_bytes<T, WB>(m);
   static bool attr = false;
   if (!attr) {
-    ITG_CUDA(h, cudaFuncSetAttribute(k_jacobi_block_step<T, WB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
+    ITG_CUDA(h, cudaFuncSetAttribute(k_jacobi_block_step<T, WB, THREADS>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr = true;
   }
   const int nb = (n + WB - 1) / WB, nbp = nb + (nb & 1);
@@ -426,8 +435,9 @@ int jb_run(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, T amin_co
   for (int sw = 0; sw < max_sweeps; ++sw) {
     ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
     for (int step = 0; step < nbp - 1; ++step)
-      k_jacobi_block_step<T, WB><<<nbp / 2, JB_THREADS, smem, h->stream>>>(W, m, n, V, tol, conv_tol(tol), amin,
-                                                                          amin_conv, step, step == 0, flag);
+      k_jacobi_block_step<T, WB, THREADS><<<nbp / 2, THREADS, smem, h->stream>>>(W, m, n, V, tol, conv_tol(tol),
+                                                                                 amin, amin_conv, step, step == 0,
+                                                                                 flag);
     ITG_CHECK_LAUNCH(h);
     ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     ITG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -438,6 +448,14 @@ int jb_run(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, T amin_co
   }
   *sweeps = max_sweeps;
   return ITG_ERR_NOTCONVERGED;
+}
+
+template <class T, int WB>
+int jb_run(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, T amin_conv, int max_sweeps, int* flag,
+           int* sweeps) {
+  if (sizeof(T) == 8 && m <= JB_SMALL_M)
+    return jb_run_t<T, WB, 32 * WB>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, flag, sweeps);
+  return jb_run_t<T, WB, JB_THREADS>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, flag, sweeps);
 }
 
 // Blocked Jacobi with the widest block whose column pair fits in 200 KB of
