@@ -538,6 +538,64 @@ def run_contract(args):
     return 0
 
 
+def run_libs(args):
+    """The vendor-library route on the same GB300, beside this library's kernels:
+    what the reference's cuTENSOR / cuSOLVER calls would stand on.  H_eff at
+    chi = 1024 as the same four tensordot steps through torch (cuBLAS FP64
+    GEMMs + permute copies), a 8192^3 cuBLAS DGEMM, and torch.linalg.svd
+    (cuSOLVER) of the 2048 x 2048 bond matrix of `--workload svd`; CUDA events,
+    warm, inputs far above L2."""
+    import numpy as np
+    import torch
+    dev = "cuda"
+    g = torch.Generator(device=dev).manual_seed(7)
+    chi, d, w = args.chi, 2, 5
+    L = torch.randn(chi, w, chi, dtype=torch.float64, device=dev, generator=g)
+    R = torch.randn(chi, w, chi, dtype=torch.float64, device=dev, generator=g)
+    W1 = torch.randn(w, d, d, w, dtype=torch.float64, device=dev, generator=g)
+    W2 = torch.randn(w, d, d, w, dtype=torch.float64, device=dev, generator=g)
+    psi = torch.randn(chi, d, d, chi, dtype=torch.float64, device=dev, generator=g)
+
+    def heff():
+        t = torch.tensordot(L, psi, dims=([0], [0]))
+        t = torch.tensordot(t, W1, dims=([0, 2], [0, 2]))
+        t = torch.tensordot(t, W2, dims=([4, 1], [0, 2]))
+        return torch.tensordot(t, R, dims=([1, 4], [0, 1]))
+
+    def timed(fn, reps):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps / 1e3
+
+    t_heff = timed(heff, 3)
+    n = 8192
+    A = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+    B = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+    t_gemm = timed(lambda: A @ B, 3)
+    del A, B
+    rng = np.random.default_rng(7)
+    nn = args.svd_n
+    Q1, _ = np.linalg.qr(rng.standard_normal((nn, nn)))
+    Q2, _ = np.linalg.qr(rng.standard_normal((nn, nn)))
+    M = torch.from_numpy((Q1 * np.exp(-np.arange(nn) / 60.0)) @ Q2.T).to(dev)
+    t_svd = timed(lambda: torch.linalg.svd(M, full_matrices=False), 2)
+    print(json.dumps({"metric": "vendor-library route on the same GPU", "value": flops(chi) / t_heff / 1e12,
+                      "unit": "TFLOP/s", "higher_is_better": True,
+                      "heff_torch_cublas_fp64": {"chi": chi, "ms": t_heff * 1e3, "tflops": flops(chi) / t_heff / 1e12},
+                      "dgemm_8192_cublas": {"ms": t_gemm * 1e3, "tflops": 2 * n ** 3 / t_gemm / 1e12},
+                      "svd_cusolver": {"n": nn, "s": t_svd},
+                      "torch": torch.__version__, "dtype": "f64", "data": "synthetic (torch randn, seeded)"}),
+          flush=True)
+    return 0
+
+
 def run_ops(args):
     """Rooflines of the HBM-bound operators and of the SVD kernels (config 2).
 
@@ -831,7 +889,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="heff",
-                    choices=["heff", "dmrg", "batched", "learned", "ops", "svd", "contract"])
+                    choices=["heff", "dmrg", "batched", "learned", "ops", "svd", "contract", "libs"])
     ap.add_argument("--contract-cases", type=int, default=8)
     ap.add_argument("--dmrg-n", type=int, default=24)
     ap.add_argument("--dmrg-sweeps", type=int, default=2)
@@ -864,6 +922,8 @@ def main():
         return run_learned(args)
     if args.workload == "contract":
         return run_contract(args)
+    if args.workload == "libs":
+        return run_libs(args)
     if args.workload == "ops":
         return run_ops(args)
     if args.workload == "svd":
