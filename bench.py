@@ -701,7 +701,7 @@ def run_ops(args):
 def run_svd(args):
     """One itg_factorize_trunc of an n x n matrix A = Q1 diag(exp(-k/60)) Q2^T (Haar Q1, Q2
     from numpy, seed 7), keeping n/2 columns: the DMRG bond split at chi = n/2.  Used as the
-    small driver of the SVD profiles; prints time, Jacobi sweeps and the method used."""
+    program behind the SVD profiles; prints time, Jacobi sweeps and the method used."""
     import numpy as np
     import torch
     from itg import _lib

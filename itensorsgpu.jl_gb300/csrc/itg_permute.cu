@@ -114,7 +114,7 @@ int make_perm(itg_handle* h, int rank, const int32_t* modesA, const int32_t* mod
 
 }  // namespace
 
-// Shared driver: Bin may be null (pure permute) or alias B.
+// Shared host routine: Bin may be null (pure permute) or alias B.
 static int permute_axpby(itg_handle* h, double alpha, const double* A, int rank,
                          const int64_t* dimsA, const int32_t* modesA, double beta,
                          const double* Bin, const int32_t* modesB, double* B) {

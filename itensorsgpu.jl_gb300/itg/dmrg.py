@@ -1,4 +1,4 @@
-"""Two-site DMRG driver over libitg.so (the dmrg(H, psi, sweeps) entry point).
+"""Two-site DMRG sweeps over libitg.so (the dmrg(H, psi, sweeps) entry point).
 
 ITensors.jl's ``dmrg`` (ITensors 0.2, called at examples/dmrg.jl:25 and
 test/dmrg.jl:27,75 of the reference) sweeps bonds b = 1..N-1 and back

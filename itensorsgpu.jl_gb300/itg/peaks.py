@@ -2,7 +2,7 @@
 
 Builds csrc/probes/peaks.cu for sm_103a, runs it on device 0 and writes the
 result to profiles/fp64_peak.json (FP64 DFMA / DMMA and legacy bf16 mma.sync
-throughput).  The driver-measured HBM and cuBLAS bf16 peaks live in
+throughput).  The measured HBM and cuBLAS bf16 peaks live in
 MEASURED_PEAKS.json; this file adds the FP64 figure those do not cover.
 
 Usage: python -m itg.peaks   (from itensorsgpu.jl_gb300/, on a GPU machine)

@@ -174,7 +174,7 @@ function factorize_svd(T::CuDenseTensor{Float64,2,IndsT}; ortho::String="left", 
     return Lt, Rt, Spectrum(Array(S[1:dk]) .^ 2, te[])
 end
 
-# ProjMPO product + eigensolver for the two-site update: the dmrg driver calls
+# ProjMPO product + eigensolver for the two-site update: the dmrg sweep calls
 # this with the device buffers of L, W1, W2, R and phi.
 function davidson_heff2!(phi::CuVector{Float64}, L, W1, W2, R, chiL, chiR, d, wL, wM, wR;
                          krylovdim::Int=3, maxiter::Int=2, tol::Float64=1e-14)

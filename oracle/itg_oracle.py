@@ -1,6 +1,6 @@
 """CPU oracle for the two-site DMRG hot path — TEST INFRASTRUCTURE ONLY.
 
-This module is the checker.  Only tests/, __graft_entry__.smoke() and the
+This module is test infrastructure.  Only tests/, __graft_entry__.smoke() and the
 cpu_baseline / --impl reference legs of bench.py may import it.  The product
 (libitg.so and the itg package) never calls it.
 

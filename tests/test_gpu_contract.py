@@ -1,7 +1,7 @@
 """Contraction parity (GPU vs oracle), mirroring test/test_cucontract.jl.
 
 Tolerance: relative Frobenius error <= 1e-12 for the FP64 path (the
-the benchmark spec bar; the reference's own tests use rtol = sqrt(eps) ~ 1.5e-8).
+parity bar of this path; the reference's own tests use rtol = sqrt(eps) ~ 1.5e-8).
 """
 import itertools
 import random
