@@ -144,6 +144,59 @@ function LinearAlgebra.svd(T::CuDenseTensor{Float64,2,IndsT}; maxdim::Int=minimu
     return Ut, St, Vt, Spectrum(Array(S[1:dS]) .^ 2, te[])
 end
 
+# svd / qr / eigen of order-2 ComplexF64 tensors (itg_svd_trunc_z, itg_qr_z,
+# itg_eigh_trunc_z): A = U S V^H, A = Q R, A = U D U^H (Hermitian).
+function LinearAlgebra.svd(T::CuDenseTensor{ComplexF64,2,IndsT}; maxdim::Int=minimum(dims(T)),
+                           mindim::Int=1, cutoff::Float64=0.0, absoluteCutoff::Bool=false,
+                           doRelCutoff::Bool=true, legacy_gpu::Bool=false, kwargs...) where {IndsT}
+    m, n = dims(T); r = min(m, n)
+    U = CuVector{ComplexF64}(undef, m * r); S = CuVector{Float64}(undef, r)
+    V = CuVector{ComplexF64}(undef, n * r)
+    k = Ref{Int64}(); te = Ref{Cdouble}(); dc = Ref{Cdouble}()
+    st = ccall((:itg_svd_trunc_z, libitg), Cint,
+               (Ptr{Cvoid}, Int64, Int64, CuPtr{Cvoid}, Int64, Int64, Int64, Cdouble, Cint,
+                Cint, Cint, CuPtr{Cvoid}, CuPtr{Float64}, CuPtr{Cvoid}, Ref{Int64},
+                Ref{Cdouble}, Ref{Cdouble}),
+               handle(), m, n, _vptr(T), m, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff,
+               legacy_gpu, reinterpret(CuPtr{Cvoid}, pointer(U)), pointer(S),
+               reinterpret(CuPtr{Cvoid}, pointer(V)), k, te, dc)
+    check(st, "itg_svd_trunc_z")
+    dS = k[]
+    u = eltype(IndsT)(dS); v = eltype(IndsT)(dS)
+    Ut = Tensor(Dense(U[1:m*dS]), IndsT((ind(T, 1), u)))
+    St = Tensor(Diag(S[1:dS]), IndsT((u, v)))
+    Vt = Tensor(Dense(V[1:n*dS]), IndsT((ind(T, 2), v)))
+    return Ut, St, Vt, Spectrum(Array(S[1:dS]) .^ 2, te[])
+end
+
+function LinearAlgebra.qr(T::CuDenseTensor{ElT,2,IndsT}) where {ElT<:ITGElT,IndsT}
+    m, n = dims(T); r = min(m, n)
+    Q = CuVector{ElT}(undef, m * r); R = CuVector{ElT}(undef, r * n)
+    st = ccall((ElT === ComplexF64 ? :itg_qr_z : :itg_qr, libitg), Cint,
+               (Ptr{Cvoid}, Int64, Int64, CuPtr{Cvoid}, Int64, CuPtr{Cvoid}, CuPtr{Cvoid}),
+               handle(), m, n, _vptr(T), m, reinterpret(CuPtr{Cvoid}, pointer(Q)),
+               reinterpret(CuPtr{Cvoid}, pointer(R)))
+    check(st, "itg_qr")
+    q = eltype(IndsT)(r)
+    return Tensor(Dense(Q), IndsT((ind(T, 1), q))), Tensor(Dense(R), IndsT((q, ind(T, 2))))
+end
+
+function LinearAlgebra.eigen(T::Hermitian{ElT,<:CuDenseTensor{ElT,2,IndsT}}; maxdim::Int=size(T, 1),
+                             mindim::Int=size(T, 1), cutoff::Float64=0.0, kwargs...) where {ElT<:ITGElT,IndsT}
+    A = parent(T); n = dims(A)[1]
+    D = CuVector{Float64}(undef, n); U = CuVector{ElT}(undef, n * n)
+    k = Ref{Int64}(); te = Ref{Cdouble}(); dc = Ref{Cdouble}()
+    st = ccall((ElT === ComplexF64 ? :itg_eigh_trunc_z : :itg_eigh_trunc, libitg), Cint,
+               (Ptr{Cvoid}, Int64, CuPtr{Cvoid}, Int64, Int64, Int64, Cdouble, Cint, Cint, Cint,
+                CuPtr{Float64}, CuPtr{Cvoid}, Ref{Int64}, Ref{Cdouble}, Ref{Cdouble}),
+               handle(), n, _vptr(A), n, maxdim, mindim, cutoff, 0, 1, 0, pointer(D),
+               reinterpret(CuPtr{Cvoid}, pointer(U)), k, te, dc)
+    check(st, "itg_eigh_trunc")
+    dk = k[]; l = eltype(IndsT)(dk); r = eltype(IndsT)(dk)
+    return Tensor(Diag(D[1:dk]), IndsT((l, r))), Tensor(Dense(U[1:n*dk]), IndsT((ind(A, 2), r))),
+           Spectrum(Array(D[1:dk]), te[])
+end
+
 # factorize of an order-2 CuDense tensor (the two-site bond split of dmrg,
 # ITensors' factorize with which_decomp = "svd"): ortho = "left" returns L with
 # orthonormal columns and R = S V^T, ortho = "right" returns L = U S and R
