@@ -274,7 +274,8 @@ def run_gpu(args):
             roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                     "frac": (achieved / peaks["bf16_tflops"]) if achieved else None,
                     "traffic": traffic.get("k_split_gemm"),
-                    "traffic_source": "ncu capture, profiles/k_split_gemm_heff2_chi1024.md" if traffic else None,
+                    "traffic_source": ("ncu capture, profiles/k_split_gemm_heff2_chi1024.md"
+                                       if traffic.get("k_split_gemm") else None),
                     "peak_source": f"MEASURED_PEAKS.json bf16_tflops (burst, {src})",
                     "kernel": "k_split_gemm", "launches": kn, "kernel_ms_per_launch": kms / max(kn, 1),
                     "kernel_flop_per_launch": slices * 40 * chi ** 3,
@@ -288,7 +289,8 @@ def run_gpu(args):
             roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                     "frac": (achieved / fp64_peak) if (achieved and fp64_peak) else None,
                     "traffic": traffic.get("k_gemm_gather_f64"),
-                    "traffic_source": "ncu capture, profiles/k_gemm_gather_f64_heff2_chi1024.md" if traffic else None,
+                    "traffic_source": ("ncu capture, profiles/k_gemm_gather_f64_heff2_chi1024.md"
+                                       if traffic.get("k_gemm_gather_f64") else None),
                     "peak_source": "profiles/fp64_peak.json (project DFMA probe, measured)",
                     "kernel": "k_gemm_gather_f64", "launches": kn, "kernel_ms_per_launch": kms / max(kn, 1),
                     "kernel_flop_per_launch": 40 * chi ** 3, "gemm_share_of_step": kms / ms}

@@ -114,9 +114,13 @@ ITG_API int itg_profile_read(itg_handle* h, int kernel, double* total_ms, int64_
  * (heuristic choice only). */
 enum { ITG_TILE_128x128 = 0, ITG_TILE_128x64 = 1, ITG_TILE_64x64 = 2 };
 /* Split-precision tile variants (split_bn below): 128 and 256 columns, and
- * 256 columns computed by a 2-CTA cluster that shares its B tile through TMA
- * multicast. */
-enum { ITG_SPLIT_BN_128 = 128, ITG_SPLIT_BN_256 = 256, ITG_SPLIT_BN_256_PAIR = 257 };
+ * 256 columns computed by a 2-CTA (PAIR) or 4-CTA (QUAD) cluster whose CTAs
+ * share one B tile through TMA multicast.  Any of them | ITG_SPLIT_STREAMK:
+ * one persistent CTA (cluster) per resident slot, the launch's work divided
+ * evenly between them, a tile shared by consecutive ones at level boundaries
+ * and summed with exact integer atomics (same bits as without). */
+enum { ITG_SPLIT_BN_128 = 128, ITG_SPLIT_BN_256 = 256, ITG_SPLIT_BN_256_PAIR = 257, ITG_SPLIT_BN_256_QUAD = 258,
+       ITG_SPLIT_STREAMK = 0x1000 };
 ITG_API int itg_set_autotune(itg_handle* h, int enable);
 /* entries: size of the process-wide cache; tunings: tuning runs by this handle. */
 ITG_API int itg_autotune_info(itg_handle* h, int64_t* entries, int64_t* tunings);

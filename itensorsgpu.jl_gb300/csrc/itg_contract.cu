@@ -629,7 +629,13 @@ int choose_split(itg_handle* h, const ContractPlan& p, const double* A, const do
   float best = 1e30f;
   int best_bn = bn;
   int st = ITG_OK;
-  for (int cand : {ITG_SPLIT_BN_256_PAIR, ITG_SPLIT_BN_256, ITG_SPLIT_BN_128}) {
+  // one tile per cluster, or stream-K (persistent clusters, the last partial
+  // wave split at level boundaries): each wins on some shapes
+  const int cands[] = {ITG_SPLIT_BN_256_PAIR, ITG_SPLIT_BN_256_PAIR | ITG_SPLIT_STREAMK,
+                       ITG_SPLIT_BN_256_QUAD | ITG_SPLIT_STREAMK, ITG_SPLIT_BN_256 | ITG_SPLIT_STREAMK,
+                       ITG_SPLIT_BN_128};
+  for (int cand : cands) {
+    if ((cand & ~ITG_SPLIT_STREAMK) == ITG_SPLIT_BN_256_QUAD && p.M <= 3 * 128) continue;  // mostly zero-filled partners
     float ms = 0.f;
     st = time_variant(h, [&]() { return itg_split_gemm(h, p, A, B, out, alpha, 0.0, cand); }, ms);
     if (st != ITG_OK) break;
@@ -961,8 +967,9 @@ extern "C" int itg_autotune_force(itg_handle* h, int rankA, const int64_t* dimsA
                                   const int64_t* dimsC, const int32_t* modesC, int tile, int split_bn) {
   if (!h) return ITG_ERR_INVALID;
   if (tile > ITG_TILE_64x64 ||
-      (split_bn > 0 && split_bn != ITG_SPLIT_BN_128 && split_bn != ITG_SPLIT_BN_256 &&
-       split_bn != ITG_SPLIT_BN_256_PAIR))
+      (split_bn > 0 && (split_bn & ~ITG_SPLIT_STREAMK) != ITG_SPLIT_BN_128 &&
+       (split_bn & ~ITG_SPLIT_STREAMK) != ITG_SPLIT_BN_256 && (split_bn & ~ITG_SPLIT_STREAMK) != ITG_SPLIT_BN_256_PAIR &&
+       (split_bn & ~ITG_SPLIT_STREAMK) != ITG_SPLIT_BN_256_QUAD))
     return itg_fail(h, ITG_ERR_INVALID, "unknown variant (tile %d, split_bn %d)", tile, split_bn);
   if (rankA < 0 || rankB < 0 || rankC < 0 || rankA > ITG_MAX_RANK || rankB > ITG_MAX_RANK || rankC > ITG_MAX_RANK)
     return itg_fail(h, ITG_ERR_UNSUPPORTED, "rank outside 0..%d", ITG_MAX_RANK);

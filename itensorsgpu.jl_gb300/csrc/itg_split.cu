@@ -179,6 +179,29 @@ __device__ __forceinline__ void tc_ld_32x32b_x32_nowait(uint32_t taddr, uint32_t
         "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
 }
+__device__ __forceinline__ void tc_ld_32x32b_x16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_ld_32x32b_x16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tc_st_32x32b_x16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+      "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tc_st_32x32b_x32(uint32_t taddr, const uint32_t (&r)[32]) {
   asm volatile(
@@ -233,6 +256,14 @@ struct Sched {
     first_in_group = true;
     used = cost();
   }
+  // Jump to the first item of level L0 (a group always starts there).
+  __host__ __device__ void seek(int L0) {
+    L = L0;
+    p = 0;
+    kb = 0;
+    first_in_group = true;
+    used = L < S ? cost() : 0;
+  }
   __host__ __device__ int q() const { return L - p; }
   __host__ __device__ int64_t cost() const {
     return (int64_t)BK << (digit_log2(p) + digit_log2(L - p));
@@ -282,8 +313,80 @@ struct GemmArgs {
   const int64_t* offCn;
   double* C;
   double alpha, beta;
-  long long* acc;
+  long long* acc;    // one private int64 tile accumulator per CTA
+  long long* tacc;   // shared accumulators of tiles split between clusters (one per CTA)
+  int* cnt;          // contributions received by each shared accumulator
+  int64_t W;         // tail work units: T * (cluster tiles mod G)
+  int G;             // clusters in the grid
+  int q;             // whole tiles per cluster before the tail
   int* err;
+};
+
+// Work partition over G clusters.  With q, r = divmod(cluster tiles, G),
+// cluster g first computes the whole tiles g, g + G, ..., g + (q - 1) G (in
+// waves, so the tiles in flight at any time are neighbours and share operand
+// panels in L2), then its share of the last r tiles: their units
+// (cluster tile ct, level L) in tile-major order, unit (ct, L) costing L + 1
+// (its k-blocks number (L + 1) * nkb) and starting at offset
+// T * (ct - q G) + L (L + 1) / 2, T = S (S + 1) / 2.  Cluster g owns the tail
+// units whose start offset lies in [lo(g), lo(g + 1)), lo(g) = floor(g W / G),
+// W = T r, so a tail tile may be shared by consecutive clusters, always at a
+// level boundary.  With G equal to the number of cluster tiles every cluster
+// computes exactly one whole tile.
+struct Part {
+  int64_t W;  // tail units
+  int G, S, T, q;
+  __device__ int base() const { return q * G; }  // first tail tile
+  __device__ int64_t lo(int g) const { return (int64_t)g * W / G; }
+  // first tail unit whose start offset is >= x
+  __device__ void unit_at(int64_t x, int& ct, int& L) const {
+    ct = (int)(x / T);
+    const int r = (int)(x - (int64_t)T * ct);
+    ct += base();
+    L = 0;
+    while (L < S && L * (L + 1) / 2 < r) ++L;
+    if (L == S) {
+      ++ct;
+      L = 0;
+    }
+  }
+  // cluster owning the tail unit that starts at offset s: the largest g with lo(g) <= s
+  __device__ int owner(int64_t s) const {
+    const int64_t g = ((s + 1) * G + W - 1) / W - 1;
+    return g < 0 ? 0 : (g >= G ? G - 1 : (int)g);
+  }
+  // Segment idx of cluster g (tile ct, levels [L0, Le)); (tb, lb) and (te, le)
+  // are unit_at(lo(g)) and unit_at(lo(g + 1)).  False past the last one.
+  __device__ bool seg(int g, int idx, int tb, int lb, int te, int le, int& ct, int& L0, int& Le) const {
+    if (idx < q) {
+      ct = g + idx * G;
+      L0 = 0;
+      Le = S;
+      return true;
+    }
+    const int j = idx - q;
+    ct = tb + j;
+    L0 = j == 0 ? lb : 0;
+    if (!(ct < te || (ct == te && L0 < le))) return false;
+    Le = ct == te ? le : S;
+    return true;
+  }
+  // clusters contributing to tile ct (the distinct owners of its units)
+  __device__ int contributors(int ct, int& first) const {
+    if (ct < base()) {
+      first = 0;
+      return 1;
+    }
+    const int64_t s0 = (int64_t)T * (ct - base());
+    first = owner(s0);
+    int n = 1;
+    for (int L = 1, prev = first; L < S; ++L) {
+      const int o = owner(s0 + L * (L + 1) / 2);
+      n += o != prev;
+      prev = o;
+    }
+    return n;
+  }
 };
 
 // v * 2^exp2 rounded to nearest even, built with integer instructions.
@@ -330,15 +433,46 @@ struct Smem {
   static constexpr int TOTAL = 1024 /*align slack*/ + NSTAGE * STAGE_BYTES + 256;
 };
 
-// MC: 2-CTA cluster along M.  The pair shares its B tile: each CTA loads one
-// half of it with a TMA multicast into both CTAs' stage, so every stage's B
-// bytes come half from each CTA and a stage is refilled only when the MMAs of
-// both CTAs have released it (empty barriers count two commits, sent to both
-// CTAs).  Halves the L2 -> SM traffic of B.
-template <int BN, bool MC>
+// 16 values of a CTA's private int64 accumulator (columns c0 .. c0 + 15 of
+// this thread's row): TMEM columns 256 + c (low words) and 384 + c (high
+// words) when TACC, else global memory.  Warp-collective when TACC.
+template <bool TACC>
+__device__ __forceinline__ void load_acc16(uint32_t lane_base, const long long* acc, int c0, int row,
+                                           long long (&v)[16]) {
+  if (TACC) {
+    uint32_t lo[16], hi[16];
+    const uint32_t tlo = lane_base + 256u + (uint32_t)c0;
+    tc_ld_32x32b_x16_nowait(tlo, lo);
+    tc_ld_32x32b_x16_nowait(tlo + 128u, hi);
+    tc_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = (long long)(((unsigned long long)hi[j] << 32) | lo[j]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = acc[(size_t)(c0 + j) * BM + row];
+  }
+}
+
+// CS: cluster of CS CTAs (1, 2 or 4) along M sharing one B tile.  Each CTA
+// loads 1/CS of the B tile with a TMA multicast into every CTA's stage, so a
+// stage's B bytes come in equal parts from all CTAs of the cluster and a stage
+// is refilled only when the MMAs of all of them have released it (empty
+// barriers count CS commits, each sent to every CTA).  Cuts the L2 -> SM
+// traffic of B by CS.  All CTAs of a cluster walk the same units (Part).
+//
+// A CTA walks its cluster's units tile segment by tile segment; the pipeline
+// state (stage ring, TMEM buffers) carries over from one segment to the next.
+// A tile owned by one cluster is converted to FP64 straight from the CTA's
+// private accumulator.  A shared tile: every contributor adds its private
+// accumulator into the tile's shared one with 64-bit integer atomics (exact,
+// so the result does not depend on their order), then counts itself in; the
+// last one to arrive converts.  Nobody waits for anybody else.
+template <int BN, int CS>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
              GemmArgs args) {
+  constexpr bool MC = CS > 1;
+  constexpr uint16_t CMASK = (uint16_t)((1u << CS) - 1u);
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int NST = Smem<BN>::NSTAGE;
@@ -352,28 +486,26 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
   uint64_t* done_bar = bars + 2 * NST + 4;  // [1]
   volatile int* abort_flag = (volatile int*)(bars + 2 * NST + 5);
   uint32_t* tmem_slot = (uint32_t*)(bars + 2 * NST + 6);
+  volatile int* decision = (volatile int*)(bars + 2 * NST + 7);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int m_tile, n_tile;
-  uint32_t rank = 0;
-  if (MC) {
-    rank = cluster_ctarank();
-    const int pair = blockIdx.x >> 1;
-    const int m_pair = pair / args.tiles_n;
-    n_tile = pair - m_pair * args.tiles_n;
-    m_tile = 2 * m_pair + (int)rank;  // may be one past the last tile (a zero-filled partner)
-  } else {
-    m_tile = blockIdx.x / args.tiles_n;
-    n_tile = blockIdx.x - m_tile * args.tiles_n;
-  }
-  const int tile = m_tile * args.tiles_n + n_tile;  // accumulator slot
-  const int m0 = m_tile * BM, n0 = n_tile * BN;
+  const uint32_t rank = MC ? cluster_ctarank() : 0u;
+  const int gcl = (int)(blockIdx.x / CS);  // this CTA's cluster
+  Part part;
+  part.W = args.W;
+  part.G = args.G;
+  part.S = args.S;
+  part.T = args.S * (args.S + 1) / 2;
+  part.q = args.q;
+  int tb, lb, te, le;  // tail units [ (tb, lb), (te, le) )
+  part.unit_at(part.lo(gcl), tb, lb);
+  part.unit_at(part.lo(gcl + 1), te, le);
   constexpr uint32_t TMEM_COLS = TACC ? 512 : 2 * BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], MC ? 2 : 1);
+      mbar_init(&empty[s], CS);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
@@ -392,33 +524,48 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (MC) cluster_sync_all();  // the partner's barriers exist before any multicast reaches them
+  if (MC) cluster_sync_all();  // the partners' barriers exist before any multicast reaches them
   const uint32_t tmem_base = *tmem_slot;
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
-      Sched sc;
-      sc.begin(args.S, args.nkb);
       int it = 0;
-      while (sc.valid() && !*abort_flag) {
-        const int s = it % NST;
-        if (it >= NST) {
-          if (!mbar_wait(&empty[s], ((it / NST) - 1) & 1, args.err, abort_flag)) break;
+      bool ok = true;
+      int ct, L0, Le;
+      for (int si = 0; ok && part.seg(gcl, si, tb, lb, te, le, ct, L0, Le); ++si) {
+        const int m_grp = ct / args.tiles_n;
+        const int n_tile = ct - m_grp * args.tiles_n;
+        const int m0 = (CS * m_grp + (int)rank) * BM, n0 = n_tile * BN;
+        Sched sc;
+        sc.begin(args.S, args.nkb);
+        sc.seek(L0);
+        while (sc.valid() && sc.L < Le) {
+          if (*abort_flag) {
+            ok = false;
+            break;
+          }
+          const int s = it % NST;
+          if (it >= NST) {
+            if (!mbar_wait(&empty[s], ((it / NST) - 1) & 1, args.err, abort_flag)) {
+              ok = false;
+              break;
+            }
+          }
+          uint8_t* sa = stage_mem + s * Smem<BN>::STAGE_BYTES;
+          uint8_t* sb = sa + Smem<BN>::A_BYTES;
+          mbar_arrive_expect_tx(&full[s], Smem<BN>::STAGE_BYTES);
+          tma_load_2d(sa, &mapA, sc.kb * BK, sc.p * args.Mpad + m0, &full[s]);
+          if (MC) {
+            // this CTA's part of the B tile, into every CTA (rows rank*BN/CS .. +BN/CS)
+            tma_load_2d_mc(sb + rank * (Smem<BN>::B_BYTES / CS), &mapB, sc.kb * BK,
+                           sc.q() * args.Npad + n0 + (int)rank * (BN / CS), &full[s], CMASK);
+          } else {
+            tma_load_2d(sb, &mapB, sc.kb * BK, sc.q() * args.Npad + n0, &full[s]);
+          }
+          sc.advance();
+          ++it;
         }
-        uint8_t* sa = stage_mem + s * Smem<BN>::STAGE_BYTES;
-        uint8_t* sb = sa + Smem<BN>::A_BYTES;
-        mbar_arrive_expect_tx(&full[s], Smem<BN>::STAGE_BYTES);
-        tma_load_2d(sa, &mapA, sc.kb * BK, sc.p * args.Mpad + m0, &full[s]);
-        if (MC) {
-          // this CTA's half of the B tile, into both CTAs (rows rank*BN/2 .. +BN/2)
-          tma_load_2d_mc(sb + rank * (Smem<BN>::B_BYTES / 2), &mapB, sc.kb * BK,
-                         sc.q() * args.Npad + n0 + (int)rank * (BN / 2), &full[s], (uint16_t)0x3);
-        } else {
-          tma_load_2d(sb, &mapB, sc.kb * BK, sc.q() * args.Npad + n0, &full[s]);
-        }
-        sc.advance();
-        ++it;
       }
       // make sure no copy is still landing in shared memory when we leave
       for (int j = std::max(0, it - NST); j < it; ++j)
@@ -428,36 +575,42 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
     // ---------------------------------------------------------- MMA issuer
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16(BM, BN);
-      Sched sc;
-      sc.begin(args.S, args.nkb);
-      int it = 0;
+      int it = 0, lg = 0;  // items and groups issued by this CTA
       bool ok = true;
-      while (sc.valid() && ok) {
-        const int g = sc.group;
-        const int b = g & 1;
-        if (sc.first_in_group && g >= 2) {
-          ok = mbar_wait(&acc_empty[b], ((g >> 1) - 1) & 1, args.err, abort_flag);
-          tc_fence_after();
+      int ct, L0, Le;
+      for (int si = 0; ok && part.seg(gcl, si, tb, lb, te, le, ct, L0, Le); ++si) {
+        Sched sc;
+        sc.begin(args.S, args.nkb);
+        sc.seek(L0);
+        while (sc.valid() && sc.L < Le) {
+          const int b = lg & 1;
+          const bool first = sc.first_in_group;
+          if (first && lg >= 2) {
+            ok = mbar_wait(&acc_empty[b], ((lg >> 1) - 1) & 1, args.err, abort_flag);
+            tc_fence_after();
+            if (!ok) break;
+          }
+          const int s = it % NST;
+          ok = mbar_wait(&full[s], (it / NST) & 1, args.err, abort_flag);
           if (!ok) break;
-        }
-        const int s = it % NST;
-        ok = mbar_wait(&full[s], (it / NST) & 1, args.err, abort_flag);
-        if (!ok) break;
-        tc_fence_after();
-        const uint32_t sa = smem_u32(stage_mem + s * Smem<BN>::STAGE_BYTES);
-        const uint32_t sb = sa + Smem<BN>::A_BYTES;
-        const uint64_t ad = sdesc_sw128(sa), bd = sdesc_sw128(sb);
-        const uint32_t tmem_d = tmem_base + (uint32_t)(b * BN);
+          tc_fence_after();
+          const uint32_t sa = smem_u32(stage_mem + s * Smem<BN>::STAGE_BYTES);
+          const uint32_t sb = sa + Smem<BN>::A_BYTES;
+          const uint64_t ad = sdesc_sw128(sa), bd = sdesc_sw128(sb);
+          const uint32_t tmem_d = tmem_base + (uint32_t)(b * BN);
 #pragma unroll
-        for (int kk = 0; kk < BK / 16; ++kk) {
-          const uint32_t accum = (sc.first_in_group && kk == 0) ? 0u : 1u;
-          tc_mma_bf16(tmem_d, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), idesc, accum);
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            const uint32_t accum = (first && kk == 0) ? 0u : 1u;
+            tc_mma_bf16(tmem_d, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), idesc, accum);
+          }
+          if (MC) tc_commit_mc(&empty[s], CMASK);
+          else tc_commit(&empty[s]);
+          if (sc.advance()) {
+            tc_commit(&acc_full[b]);
+            ++lg;
+          }
+          ++it;
         }
-        if (MC) tc_commit_mc(&empty[s], (uint16_t)0x3);
-        else tc_commit(&empty[s]);
-        const bool closes = sc.advance();
-        if (closes) tc_commit(&acc_full[b]);
-        ++it;
       }
       // all MMAs issued by this thread complete before TMEM is released
       tc_commit(done_bar);
@@ -465,105 +618,169 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
     }
   } else {
     // ------------------------------------------------------ drain/epilogue
+    // Each thread owns one row and NCOL columns.  A group's FP32 values are
+    // exact integers below 2^24 in magnitude; the groups of one level are
+    // summed in int32 registers (exact for up to 127 groups) and only a level
+    // end (or the 127th group) touches the int64 fixed-point accumulator.  The
+    // TMEM buffer goes back to the MMA issuer as soon as it has been read.
+    constexpr int NCOL = BN / 2;
+    constexpr int NCH = NCOL / 32;
     const int quarter = warp & 3;
-    const int col_lo = ((warp - 2) / 4) * (BN / 2), col_hi = col_lo + BN / 2;
+    const int col_lo = ((warp - 2) / 4) * NCOL;
     const int row = quarter * 32 + lane;
-    const int64_t m = (int64_t)m0 + row;
-    const int em = (m < args.M) ? args.eA[m] - 1022 : 0;
-    long long* acc = args.acc + (size_t)tile * BN * BM;
-    Sched sc;
-    sc.begin(args.S, args.nkb);
-    int g_done = -1;
-    bool first_drain = true;
-    while (sc.valid()) {
-      // walk to the end of the current group
-      const int L = sc.L;
-      const int g = sc.group;
-      bool last;
-      for (;;) {
-        const bool closes = sc.advance();
-        if (closes) break;
-      }
-      last = !sc.valid();
-      const int b = g & 1;
-      // every lane polls; the outcome is made warp-uniform because the TMEM
-      // loads below are .sync.aligned
-      const bool ok_lane = mbar_wait(&acc_full[b], (g >> 1) & 1, args.err, abort_flag);
-      if (!__all_sync(0xffffffffu, ok_lane)) break;
-      tc_fence_after();
-      const int sh = args.F - 7 * L;
-      const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * BN);
-#pragma unroll 1
-      for (int c0 = col_lo; c0 < col_hi; c0 += 32) {
-        uint32_t r[32];
-        long long old[32];
-        long long* ap = TACC ? nullptr : acc + (size_t)c0 * BM + row;
-        // TMEM-resident accumulator: low words in columns 256 + c, high words in 384 + c
-        const uint32_t tlo = tmem_base + ((uint32_t)(quarter * 32) << 16) + 256u + (uint32_t)c0;
-        const uint32_t thi = tlo + 128u;
-        if (TACC && !first_drain) {
-          uint32_t lo[32], hi[32];
-          tc_ld_32x32b_x32_nowait(tbase + (uint32_t)c0, r);
-          tc_ld_32x32b_x32_nowait(tlo, lo);
-          tc_ld_32x32b_x32_nowait(thi, hi);
-          tc_wait_ld();
+    long long* acc = args.acc + (size_t)blockIdx.x * BN * BM;  // private: global (BN 256) or TMEM (BN 128)
+    const uint32_t lane_base = tmem_base + ((uint32_t)(quarter * 32) << 16);
+    int lg = 0;  // groups drained by this CTA
+    int ct, L0, Le;
+    for (int si = 0; part.seg(gcl, si, tb, lb, te, le, ct, L0, Le); ++si) {
+      int32_t sum[NCOL];
+      int nsum = 0;
+      bool have_acc = false, complete = false;
+      Sched sc;
+      sc.begin(args.S, args.nkb);
+      sc.seek(L0);
+      while (sc.valid() && sc.L < Le) {
+        const int L = sc.L;
+        while (!sc.advance()) {
+        }
+        const bool seg_last = !sc.valid() || sc.L >= Le;
+        const bool flush = seg_last || sc.L != L || nsum + 1 == 127;
+        const int b = lg & 1;
+        // every lane polls; the outcome is made warp-uniform because the TMEM
+        // loads below are .sync.aligned
+        const bool ok_lane = mbar_wait(&acc_full[b], (lg >> 1) & 1, args.err, abort_flag);
+        if (!__all_sync(0xffffffffu, ok_lane)) break;
+        tc_fence_after();
 #pragma unroll
-          for (int j = 0; j < 32; ++j) old[j] = (long long)(((unsigned long long)hi[j] << 32) | lo[j]);
-        } else {
-          tc_ld_32x32b_x32(tbase + (uint32_t)c0, r);
-          if (!TACC && !first_drain) {
+        for (int c = 0; c < NCOL / 16; ++c) {
+          uint32_t r[16];
+          tc_ld_32x32b_x16(lane_base + (uint32_t)(b * BN + col_lo + 16 * c), r);
 #pragma unroll
-            for (int j = 0; j < 32; ++j) old[j] = ap[(size_t)j * BM];
-          } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) old[j] = 0;
+          for (int j = 0; j < 16; ++j) {
+            const int32_t v = __float2int_rn(__uint_as_float(r[j]));
+            sum[16 * c + j] = nsum ? sum[16 * c + j] + v : v;
           }
         }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[b]);
+        ++lg;
+        ++nsum;
+        if (flush) {
+          const int sh = args.F - 7 * L;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          long long t = (long long)__float2int_rn(__uint_as_float(r[j]));
-          t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
-          old[j] += t;
-        }
-        if (!last) {
-          if (TACC) {
-            uint32_t lo[32], hi[32];
+          for (int c = 0; c < NCH; ++c) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-              lo[j] = (uint32_t)((unsigned long long)old[j] & 0xFFFFFFFFull);
-              hi[j] = (uint32_t)((unsigned long long)old[j] >> 32);
+            for (int h = 0; h < 2; ++h) {
+              const int c0 = col_lo + 32 * c + 16 * h;
+              if (TACC) {
+                // int64 accumulator in TMEM: low words in columns 256 + c, high words in 384 + c
+                const uint32_t tlo = lane_base + 256u + (uint32_t)c0, thi = tlo + 128u;
+                uint32_t lo[16], hi[16];
+                if (have_acc) {
+                  tc_ld_32x32b_x16_nowait(tlo, lo);
+                  tc_ld_32x32b_x16_nowait(thi, hi);
+                  tc_wait_ld();
+                } else {
+#pragma unroll
+                  for (int j = 0; j < 16; ++j) lo[j] = hi[j] = 0u;
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                  long long t = (long long)sum[32 * c + 16 * h + j];
+                  t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
+                  const unsigned long long u = (((unsigned long long)hi[j] << 32) | lo[j]) + (unsigned long long)t;
+                  lo[j] = (uint32_t)(u & 0xFFFFFFFFull);
+                  hi[j] = (uint32_t)(u >> 32);
+                }
+                tc_st_32x32b_x16(tlo, lo);
+                tc_st_32x32b_x16(thi, hi);
+              } else {
+                long long* ap = acc + (size_t)c0 * BM + row;
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                  long long old[8];
+#pragma unroll
+                  for (int j = 0; j < 8; ++j) old[j] = have_acc ? ap[(size_t)(8 * q + j) * BM] : 0ll;
+#pragma unroll
+                  for (int j = 0; j < 8; ++j) {
+                    long long t = (long long)sum[32 * c + 16 * h + 8 * q + j];
+                    t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
+                    ap[(size_t)(8 * q + j) * BM] = old[j] + t;
+                  }
+                }
+              }
             }
-            tc_st_32x32b_x32(tlo, lo);
-            tc_st_32x32b_x32(thi, hi);
-            tc_wait_st();
-          } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) ap[(size_t)j * BM] = old[j];
           }
-        } else if (m < args.M) {
-          // final drain: convert to FP64 with integer instructions, scatter through the plan
-          const int64_t cm = args.offCm[m];
+          if (TACC) tc_wait_st();
+          nsum = 0;
+          have_acc = true;
+          complete = seg_last;
+        }
+        if (__any_sync(0xffffffffu, *abort_flag != 0)) break;
+      }
+      // Segment end.  Every epilogue warp arrives here (a warp that stopped on
+      // an abort included), so the decision below is the same for all of them.
+      int first_owner;
+      const int contributors = part.contributors(ct, first_owner);
+      const bool shared_tile = contributors > 1;
+      const int slot = first_owner * CS + (int)rank;
+      long long* tile_acc = args.tacc + (size_t)slot * BN * BM;
+      if (shared_tile && complete) {
+#pragma unroll 1
+        for (int c0 = col_lo; c0 < col_lo + NCOL; c0 += 16) {
+          long long v[16];
+          load_acc16<TACC>(lane_base, acc, c0, row, v);
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int64_t n = (int64_t)n0 + c0 + j;
-            if (n >= args.N) continue;
-            const int fn = args.eB[n] - 1022;
-            double v = i64_to_double_scaled(old[j], em + fn - 14 - args.F);
-            if (args.alpha != 1.0) v *= args.alpha;
-            double* cp = args.C + cm + args.offCn[n];
-            if (args.beta != 0.0) v = fma(args.beta, *cp, v);
-            *cp = v;
+          for (int j = 0; j < 16; ++j)
+            atomicAdd((unsigned long long*)(tile_acc + (size_t)(c0 + j) * BM + row), (unsigned long long)v[j]);
+        }
+        __threadfence();
+      }
+      asm volatile("bar.sync 1, %0;" ::"n"(32 * NUM_EPI_WARPS) : "memory");
+      if (warp == 2 && lane == 0) {
+        int d;
+        if (*abort_flag || !complete) d = 2;
+        else if (!shared_tile) d = 1;
+        else d = atomicAdd(&args.cnt[slot], 1) == contributors - 1 ? 1 : 0;
+        *decision = d;
+      }
+      asm volatile("bar.sync 1, %0;" ::"n"(32 * NUM_EPI_WARPS) : "memory");
+      const int d = *decision;
+      if (d == 2) break;
+      if (d == 1) {
+        // the int64 accumulator is complete: convert to FP64 with integer
+        // instructions and scatter C through the plan's offset tables
+        if (shared_tile) __threadfence();
+        const int m_grp = ct / args.tiles_n;
+        const int n0 = (ct - m_grp * args.tiles_n) * BN;
+        const int64_t m = (int64_t)(CS * m_grp + (int)rank) * BM + row;
+        const int64_t cm = m < args.M ? args.offCm[m] : 0;
+        const int em = m < args.M ? args.eA[m] - 1022 : 0;
+#pragma unroll 1
+        for (int c0 = col_lo; c0 < col_lo + NCOL; c0 += 16) {
+          long long v[16];
+          if (shared_tile) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = __ldcg(tile_acc + (size_t)(c0 + j) * BM + row);
+          } else {
+            load_acc16<TACC>(lane_base, acc, c0, row, v);
+          }
+          if (m < args.M) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int64_t n = (int64_t)n0 + c0 + j;
+              if (n >= args.N) continue;
+              double x = i64_to_double_scaled(v[j], em + args.eB[n] - 1022 - 14 - args.F);
+              if (args.alpha != 1.0) x *= args.alpha;
+              double* cp = args.C + cm + args.offCn[n];
+              if (args.beta != 0.0) x = fma(args.beta, *cp, x);
+              *cp = x;
+            }
           }
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[b]);
-      first_drain = false;
-      g_done = g;
-      if (__any_sync(0xffffffffu, *abort_flag != 0)) break;
     }
-    (void)g_done;
   }
   tc_fence_before();
   __syncthreads();
@@ -572,8 +789,8 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                  "r"(TMEM_COLS));
   }
-  // the partner may still multicast into this CTA's stages or arrive on its
-  // barriers until it has left its loops (every wait there is bounded)
+  // the partners may still multicast into this CTA's stages or arrive on its
+  // barriers until they have left their loops (every wait there is bounded)
   if (MC) cluster_sync_all();
 }
 
@@ -732,28 +949,94 @@ int make_map(itg_handle* h, CUtensorMap* map, void* base, int64_t inner, int64_t
 
 int ws_reserve(itg_handle* h, size_t bytes);
 
-template <int BN, bool MC>
+// CTAs of one variant that fit on the GPU at once (one per SM at this shared
+// memory size; clusters must fit within a GPC), queried once per variant.
+template <int BN, int CS>
+int resident_clusters(itg_handle* h, int& out) {
+  static int cached = 0;
+  if (cached > 0) {
+    out = cached;
+    return ITG_OK;
+  }
+  int n = 0;
+  if (CS > 1) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(CS * h->num_sms));
+    cfg.blockDim = dim3(NUM_THREADS);
+    cfg.dynamicSmemBytes = Smem<BN>::TOTAL;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (cudaOccupancyMaxActiveClusters(&n, k_split_gemm<BN, CS>, &cfg) != cudaSuccess || n <= 0) {
+      (void)cudaGetLastError();
+      n = h->num_sms / CS;
+    }
+  } else {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split_gemm<BN, CS>, NUM_THREADS,
+                                                      Smem<BN>::TOTAL) != cudaSuccess ||
+        per_sm <= 0) {
+      (void)cudaGetLastError();
+      per_sm = 1;
+    }
+    n = per_sm * h->num_sms;
+  }
+  cached = n > 0 ? n : 1;
+  out = cached;
+  return ITG_OK;
+}
+
+// streamk: one persistent cluster per resident slot sharing the work evenly
+// (Part); otherwise one cluster per cluster tile.
+template <int BN, int CS>
 int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
-        double alpha, double beta) {
+        double alpha, double beta, bool streamk) {
+  constexpr bool MC = CS > 1;
   constexpr int S = S_SLICES;
   const int64_t Mpad = (p.M + BM - 1) / BM * BM;
   const int64_t Npad = (p.N + BN - 1) / BN * BN;
   const int64_t Kpad = (p.K + BK - 1) / BK * BK;
   if (Mpad * S > (int64_t)INT32_MAX || Npad * S > (int64_t)INT32_MAX || Kpad > (int64_t)INT32_MAX)
     return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: problem too large");
-  // MC pairs M tiles: an odd count gets one zero-filled partner tile
-  const int64_t tiles_m = (Mpad / BM + (MC ? 1 : 0)) / (MC ? 2 : 1) * (MC ? 2 : 1);
+  // clusters group CS M tiles: the count is padded with zero-filled partner tiles
+  const int64_t tiles_m = (Mpad / BM + CS - 1) / CS * CS;
   const int64_t tiles = tiles_m * (Npad / BN);
   // F: fixed-point fraction bits of the int64 accumulator (keeps |acc| < 2^62).
   int lk = 0;
   while (((int64_t)1 << lk) < p.K) ++lk;
   const int F = 62 - 15 - lk;
   if (F < 8) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: contraction depth too large");
+  if (tiles > (int64_t)INT32_MAX / 32) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: too many tiles");
+  // the kernels need the attribute before the occupancy query
+  static bool attr = false;
+  if (!attr) {
+    ITG_CUDA(h, cudaFuncSetAttribute(k_split_gemm<BN, CS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     Smem<BN>::TOTAL));
+    attr = true;
+  }
+  const int64_t nct = tiles / CS;  // cluster tiles
+  int64_t G = nct;
+  if (streamk) {
+    int res = 0;
+    const int rst = resident_clusters<BN, CS>(h, res);
+    if (rst != ITG_OK) return rst;
+    G = res;
+  }
+  const int64_t grid = G * CS;
+  const int64_t q = nct / G, r = nct % G;
+  const bool shares = r != 0;  // the tail tiles are split between clusters
+  const size_t tile_bytes = sizeof(long long) * (size_t)BN * BM;
   size_t off = 0;
   auto take = [&](size_t b) { size_t o = off; off += itg_align256(b); return o; };
   const size_t oEA = take(sizeof(int) * Mpad), oEB = take(sizeof(int) * Npad);
   const size_t oSA = take((size_t)2 * S * Mpad * Kpad), oSB = take((size_t)2 * S * Npad * Kpad);
-  const size_t oAcc = take(Smem<BN>::TACC ? 0 : sizeof(long long) * (size_t)tiles * BN * BM);
+  const size_t oAcc = take(Smem<BN>::TACC ? 0 : tile_bytes * (size_t)grid);
+  const size_t oTacc = take(shares ? tile_bytes * (size_t)grid : 0);
+  const size_t oCnt = take(shares ? sizeof(int) * (size_t)grid : 0);
   const size_t oErr = take(sizeof(int));
   ITG_TRY(ws_reserve(h, off));
   char* ws = (char*)h->split_ws;
@@ -762,8 +1045,14 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   __nv_bfloat16* sA = (__nv_bfloat16*)(ws + oSA);
   __nv_bfloat16* sB = (__nv_bfloat16*)(ws + oSB);
   long long* acc = (long long*)(ws + oAcc);
+  long long* tacc = (long long*)(ws + oTacc);
+  int* cnt = (int*)(ws + oCnt);
   int* err = (int*)(ws + oErr);
   ITG_CUDA(h, cudaMemsetAsync(err, 0, sizeof(int), h->stream));
+  if (shares) {
+    ITG_CUDA(h, cudaMemsetAsync(tacc, 0, tile_bytes * (size_t)grid, h->stream));
+    ITG_CUDA(h, cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)grid, h->stream));
+  }
   // exponents
   {
     ProfScope prof(h, ITG_KERNEL_SPLIT_PREP);
@@ -803,7 +1092,7 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   }
   CUtensorMap mA, mB;
   ITG_TRY(make_map(h, &mA, sA, Kpad, Mpad * S, BM));
-  ITG_TRY(make_map(h, &mB, sB, Kpad, Npad * S, MC ? BN / 2 : BN));
+  ITG_TRY(make_map(h, &mB, sB, Kpad, Npad * S, BN / CS));
   GemmArgs a;
   a.M = p.M;
   a.N = p.N;
@@ -823,32 +1112,30 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   a.alpha = alpha;
   a.beta = beta;
   a.acc = acc;
+  a.tacc = tacc;
+  a.cnt = cnt;
+  a.W = (int64_t)(S * (S + 1) / 2) * r;
+  a.G = (int)G;
+  a.q = (int)q;
   a.err = err;
-  static bool attr = false;
-  if (!attr) {
-    ITG_CUDA(h, cudaFuncSetAttribute(k_split_gemm<BN, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     Smem<BN>::TOTAL));
-    attr = true;
-  }
-  if (tiles > (int64_t)INT32_MAX) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: too many tiles");
   {
     ProfScope prof(h, ITG_KERNEL_GEMM_SPLIT);
     if (MC) {
       cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3((unsigned)tiles);
+      cfg.gridDim = dim3((unsigned)grid);
       cfg.blockDim = dim3(NUM_THREADS);
       cfg.dynamicSmemBytes = Smem<BN>::TOTAL;
       cfg.stream = h->stream;
       cudaLaunchAttribute at[1];
       at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = 2;
+      at[0].val.clusterDim.x = CS;
       at[0].val.clusterDim.y = 1;
       at[0].val.clusterDim.z = 1;
       cfg.attrs = at;
       cfg.numAttrs = 1;
-      ITG_CUDA(h, cudaLaunchKernelEx(&cfg, k_split_gemm<BN, MC>, mA, mB, a));
+      ITG_CUDA(h, cudaLaunchKernelEx(&cfg, k_split_gemm<BN, CS>, mA, mB, a));
     } else {
-      k_split_gemm<BN, MC><<<(unsigned)tiles, NUM_THREADS, Smem<BN>::TOTAL, h->stream>>>(mA, mB, a);
+      k_split_gemm<BN, CS><<<(unsigned)grid, NUM_THREADS, Smem<BN>::TOTAL, h->stream>>>(mA, mB, a);
     }
   }
   ITG_CHECK_LAUNCH(h);
@@ -877,14 +1164,18 @@ int ws_reserve(itg_handle* h, size_t bytes) {
 
 }  // namespace split
 
-// bn: tcgen05 tile variant: 128, 256, or ITG_SPLIT_BN_256_PAIR (256 wide, 2-CTA
-// cluster sharing the B tile); 0: 128 when N <= 128, else 256.
+// bn: tcgen05 tile variant: 128, 256, ITG_SPLIT_BN_256_PAIR / _QUAD (256 wide,
+// 2- / 4-CTA cluster sharing the B tile), optionally | ITG_SPLIT_STREAMK
+// (persistent clusters sharing the work evenly); 0: 128 when N <= 128, else 256.
 int itg_split_gemm(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
                    double alpha, double beta, int bn) {
   if (bn == 0) bn = p.N <= 128 ? 128 : 256;
-  if (bn == 128) return split::run<128, false>(h, p, A, B, C, alpha, beta);
-  if (bn == ITG_SPLIT_BN_256_PAIR) return split::run<256, true>(h, p, A, B, C, alpha, beta);
-  return split::run<256, false>(h, p, A, B, C, alpha, beta);
+  const bool sk = (bn & ITG_SPLIT_STREAMK) != 0;
+  bn &= ~ITG_SPLIT_STREAMK;
+  if (bn == 128) return split::run<128, 1>(h, p, A, B, C, alpha, beta, sk);
+  if (bn == ITG_SPLIT_BN_256_PAIR) return split::run<256, 2>(h, p, A, B, C, alpha, beta, sk);
+  if (bn == ITG_SPLIT_BN_256_QUAD) return split::run<256, 4>(h, p, A, B, C, alpha, beta, sk);
+  return split::run<256, 1>(h, p, A, B, C, alpha, beta, sk);
 }
 
 extern "C" double itg_split_error_bound(int64_t K) {

@@ -2,8 +2,9 @@
 
 The reference caches one cuTENSOR algorithm per (mode, dim) key after timing
 them all on first use (src/cudense.jl:284-326).  Here the variants are tile
-shapes of the FP64 gather-GEMM (128x128, 128x64, 64x64), tile widths of the
-split tcgen05 GEMM (256, 128) and the tile of grouped launches.  Every variant
+shapes of the FP64 gather-GEMM (128x128, 128x64, 64x64), tile widths, CTA
+clusters and stream-K scheduling of the split tcgen05 GEMM, and the tile of
+grouped launches.  Every variant
 must give bit-identical results, so tuning never changes an answer.
 """
 import ctypes as C
@@ -40,6 +41,8 @@ CASES = [
     ((40, 30, 50), (1, 2, 3), (50, 7, 30), (3, 4, 2), (7, 40), (4, 1)),
     ((300, 5, 260), (1, 2, 3), (260, 2, 2, 33), (3, 4, 5, 6), (33, 300, 2, 5, 2), (6, 1, 4, 2, 5)),
     ((129, 257), (1, 2), (257, 65), (2, 3), (129, 65), (1, 3)),
+    # more output tiles than SMs: the stream-K variants share tiles between CTAs
+    ((2560, 64), (1, 2), (64, 2048), (2, 3), (2560, 2048), (1, 3)),
 ]
 
 
@@ -65,12 +68,15 @@ def test_every_tile_variant_is_bit_identical(gpu, case):
     ref = O.contract(A, mA, B, mB, mC)
     got = O.unflat(outs[0], dC)
     assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref)
-    # split: both tcgen05 tile widths give identical bits too
+    # split: every tcgen05 variant gives identical bits too
     so = []
-    for bn in (256, 128, 257):  # 257: 256-wide tiles on a 2-CTA cluster sharing B
+    # 257 / 258: 256-wide tiles on a 2- / 4-CTA cluster sharing B; 0x1000: stream-K
+    for bn in (256, 128, 257, 258, 0x1000 | 256, 0x1000 | 128, 0x1000 | 257, 0x1000 | 258):
         h.call("itg_autotune_force", *_shape_args(dA, mA, dB, mB, dC, mC), -1, bn)
         so.append(_contract(h, a, dA, mA, b, dB, mB, dC, mC, prec=1).cpu().numpy())
-    assert np.array_equal(so[0], so[1]) and np.array_equal(so[0], so[2])
+    assert all(np.array_equal(so[0], x) for x in so[1:])
+    refs = O.unflat(so[0], dC)
+    assert np.linalg.norm(refs - ref) <= 1e-12 * np.linalg.norm(ref)
     h.call("itg_autotune_clear")
 
 

@@ -7,7 +7,8 @@
 * Gaussian inputs: relative Frobenius error below the stated bound
   itg_split_error_bound(K) * |A|_F |B|_F / |C|_F, and in practice below 1e-12;
 * ragged shapes (M, N, K not multiples of the tiles), both operand layouts, the
-  N <= 128 tile, K long enough for many exact groups and all levels;
+  N <= 128 tile, K long enough for many exact groups and all levels, and for a
+  level whose int32 group sums must be flushed part-way (more than 127 groups);
 * the H_eff chain with ITG_PREC_SPLIT, and a DMRG run whose energy matches the
   FP64 run within 1e-9.
 """
@@ -45,6 +46,7 @@ CASES = [
     ((300, 7, 5), (1, 2, 3), (7, 5, 257), (2, 3, 4), (4, 1)),    # C transposed, ragged
     ((1000, 40), (2, 1), (1000, 90), (2, 3), (1, 3)),            # long K: many groups, N <= 128
     ((96, 5, 96), (1, 2, 3), (96, 2, 2, 96), (1, 4, 5, 6), (3, 6, 2, 4, 5)),  # H_eff step 1
+    ((60000, 130), (2, 1), (60000, 260), (2, 3), (1, 3)),        # K = 60000: a level of > 127 groups
 ]
 
 
