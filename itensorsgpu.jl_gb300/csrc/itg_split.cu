@@ -16,21 +16,23 @@
 // Each a_p b_q product is an integer GEMM run by tcgen05.mma (kind::f16, bf16
 // in, FP32 accumulate in TMEM).  Products of one level L are accumulated in a
 // TMEM buffer only while the sum of |a||b| bounds stays <= 2^24, so every FP32
-// partial sum is an exact integer.  The buffer is then drained by the
-// epilogue warps into an exact int64 fixed-point accumulator (2^F scaling),
-// while the MMA warp fills the other TMEM buffer.  The final drain converts the
-// int64 accumulator to FP64 with integer instructions (round to nearest) and
-// scatters C through the contraction plan's offset tables.  No FP64 arithmetic
-// runs in the inner loops (GB300's FP64 rate is a small fraction of its
-// tensor rate).
+// partial sum (a "group") is an exact integer.  The epilogue warps read the
+// buffer into int32 registers, summing the groups of one level exactly, and
+// hand it back to the MMA warp, which meanwhile fills the other TMEM buffer;
+// at each level end the int32 sums are shifted into an exact int64
+// fixed-point accumulator (2^F scaling).  After the last level the int64
+// accumulator is converted to FP64 with integer instructions (round to
+// nearest) and C is scattered through the contraction plan's offset tables.
+// No FP64 arithmetic runs in the inner loops (GB300's FP64 rate is a small
+// fraction of its tensor rate).
 //
-// Kernel roles (one CTA per 128 x BN output tile, 10 warps):
+// Kernel roles (10 warps per CTA; a CTA computes one 128 x BN output tile,
+// or, persistent, a sequence of tiles and parts of tiles, see Part):
 //   warp 0    TMA producer: A/B slice tiles (64 bf16 of K per stage, 128B
 //             swizzle) into a 4-stage shared-memory ring, mbarrier complete_tx
 //   warp 1    TMEM allocator and single-thread tcgen05.mma issuer
 //   warps 2-9 TMEM drain / epilogue: warp w reads TMEM lanes 32*(w%4)..+31 and
-//             owns half of the tile's columns; each 32-column chunk issues all
-//             of its accumulator loads before using them
+//             owns half of the tile's columns
 // Every mbarrier wait is bounded (globaltimer, ~4 s); on timeout the kernel
 // records ITG_ERR_TIMEOUT, stops issuing work, waits (bounded) for its own
 // copies and MMAs, frees TMEM and returns.
