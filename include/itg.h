@@ -127,13 +127,14 @@ ITG_API int itg_autotune_info(itg_handle* h, int64_t* entries, int64_t* tunings)
 /* Empty the process-wide cache and every cached choice of this handle's plans. */
 ITG_API int itg_autotune_clear(itg_handle* h);
 /* The variant a contraction of this shape would use now (without tuning):
- * *tile = ITG_TILE_* for FP64, *split_bn = 128 or 256 for split. */
+ * *tile = ITG_TILE_* for FP64, *split_bn = ITG_SPLIT_BN_* (possibly
+ * | ITG_SPLIT_STREAMK) for split. */
 ITG_API int itg_autotune_query(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA,
                                int rankB, const int64_t* dimsB, const int32_t* modesB, int rankC,
                                const int64_t* dimsC, const int32_t* modesC, int* tile, int* split_bn);
-/* Pin the variants of one shape (tile: ITG_TILE_*, split_bn: ITG_SPLIT_BN_*; a
- * negative / zero value leaves that choice alone); stored in the process-wide
- * cache like a tuned choice. */
+/* Pin the variants of one shape (tile: ITG_TILE_*, split_bn: ITG_SPLIT_BN_*,
+ * optionally | ITG_SPLIT_STREAMK; a negative / zero value leaves that choice
+ * alone); stored in the process-wide cache like a tuned choice. */
 ITG_API int itg_autotune_force(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA,
                                int rankB, const int64_t* dimsB, const int32_t* modesB, int rankC,
                                const int64_t* dimsC, const int32_t* modesC, int tile, int split_bn);
@@ -215,6 +216,13 @@ ITG_API int itg_zscal(itg_handle* h, int64_t n, const double* alpha, double* x);
 /* Bound on |C_split - C_exact|_F / (|A|_F |B|_F) for ITG_PREC_SPLIT with the
  * library's slice count at contraction depth K (host-only arithmetic). */
 ITG_API double itg_split_error_bound(int64_t K);
+/* Work partition of the split GEMM's stream-K schedule (host-only arithmetic,
+ * the code the kernel runs): the tile segments of cluster g when
+ * cluster_tiles cluster tiles are shared by `clusters` persistent clusters.
+ * Per segment 5 ints in seg: cluster tile, first level, end level (exclusive),
+ * number of clusters contributing to that tile, the first of them.  *nseg =
+ * the segment count; ITG_ERR_SHAPE when it exceeds cap. */
+ITG_API int itg_split_partition(int64_t cluster_tiles, int clusters, int g, int32_t* seg, int cap, int* nseg);
 
 /* ----------------------------------------------------------- permutation */
 /* B = alpha * A, with B's modes a permutation of A's.

@@ -338,10 +338,10 @@ struct GemmArgs {
 struct Part {
   int64_t W;  // tail units
   int G, S, T, q;
-  __device__ int base() const { return q * G; }  // first tail tile
-  __device__ int64_t lo(int g) const { return (int64_t)g * W / G; }
+  __host__ __device__ int base() const { return q * G; }  // first tail tile
+  __host__ __device__ int64_t lo(int g) const { return (int64_t)g * W / G; }
   // first tail unit whose start offset is >= x
-  __device__ void unit_at(int64_t x, int& ct, int& L) const {
+  __host__ __device__ void unit_at(int64_t x, int& ct, int& L) const {
     ct = (int)(x / T);
     const int r = (int)(x - (int64_t)T * ct);
     ct += base();
@@ -353,13 +353,13 @@ struct Part {
     }
   }
   // cluster owning the tail unit that starts at offset s: the largest g with lo(g) <= s
-  __device__ int owner(int64_t s) const {
+  __host__ __device__ int owner(int64_t s) const {
     const int64_t g = ((s + 1) * G + W - 1) / W - 1;
     return g < 0 ? 0 : (g >= G ? G - 1 : (int)g);
   }
   // Segment idx of cluster g (tile ct, levels [L0, Le)); (tb, lb) and (te, le)
   // are unit_at(lo(g)) and unit_at(lo(g + 1)).  False past the last one.
-  __device__ bool seg(int g, int idx, int tb, int lb, int te, int le, int& ct, int& L0, int& Le) const {
+  __host__ __device__ bool seg(int g, int idx, int tb, int lb, int te, int le, int& ct, int& L0, int& Le) const {
     if (idx < q) {
       ct = g + idx * G;
       L0 = 0;
@@ -374,7 +374,7 @@ struct Part {
     return true;
   }
   // clusters contributing to tile ct (the distinct owners of its units)
-  __device__ int contributors(int ct, int& first) const {
+  __host__ __device__ int contributors(int ct, int& first) const {
     if (ct < base()) {
       first = 0;
       return 1;
@@ -1178,6 +1178,36 @@ int itg_split_gemm(itg_handle* h, const ContractPlan& p, const double* A, const 
   if (bn == ITG_SPLIT_BN_256_PAIR) return split::run<256, 2>(h, p, A, B, C, alpha, beta, sk);
   if (bn == ITG_SPLIT_BN_256_QUAD) return split::run<256, 4>(h, p, A, B, C, alpha, beta, sk);
   return split::run<256, 1>(h, p, A, B, C, alpha, beta, sk);
+}
+
+extern "C" int itg_split_partition(int64_t cluster_tiles, int clusters, int g, int32_t* seg, int cap,
+                                   int* nseg) {
+  if (cluster_tiles < 1 || clusters < 1 || g < 0 || g >= clusters || cap < 0 || !nseg || (cap > 0 && !seg) ||
+      cluster_tiles > (int64_t)INT32_MAX / 32)
+    return ITG_ERR_INVALID;
+  split::Part part;
+  part.S = split::S_SLICES;
+  part.T = part.S * (part.S + 1) / 2;
+  part.G = clusters;
+  part.q = (int)(cluster_tiles / clusters);
+  part.W = (int64_t)part.T * (cluster_tiles % clusters);
+  int tb, lb, te, le;
+  part.unit_at(part.lo(g), tb, lb);
+  part.unit_at(part.lo(g + 1), te, le);
+  int n = 0, ct, L0, Le;
+  for (int si = 0; part.seg(g, si, tb, lb, te, le, ct, L0, Le); ++si, ++n) {
+    if (n >= cap) continue;
+    int first = 0;
+    const int c = part.contributors(ct, first);
+    int32_t* o = seg + 5 * n;
+    o[0] = ct;
+    o[1] = L0;
+    o[2] = Le;
+    o[3] = c;
+    o[4] = first;
+  }
+  *nseg = n;
+  return n > cap ? ITG_ERR_SHAPE : ITG_OK;
 }
 
 extern "C" double itg_split_error_bound(int64_t K) {

@@ -72,6 +72,7 @@ SIGNATURES = {
                                C.c_double,
                                _P, C.c_int, _I64P, _I32P, C.c_int]),
     "itg_split_error_bound": (C.c_double, [C.c_int64]),
+    "itg_split_partition": (C.c_int, [C.c_int64, C.c_int, C.c_int, _I32P, C.c_int, C.POINTER(C.c_int)]),
     "itg_contract_z": (C.c_int, [_P, C.c_int, C.c_int, _DP,
                                  _P, C.c_int, _I64P, _I32P,
                                  _P, C.c_int, _I64P, _I32P,
