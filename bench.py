@@ -68,6 +68,13 @@ def _n(shape):
     return n
 
 
+def fp64_peak_live(h):
+    """FP64 FMA rate of this GPU measured now through the library (TFLOP/s)."""
+    r = C.c_double()
+    h.call("itg_fp64_peak", C.byref(r))
+    return r.value
+
+
 def measured_peaks():
     p = REPO / "MEASURED_PEAKS.json"
     if p.exists():
@@ -248,10 +255,7 @@ def run_gpu(args):
         return float(t_local.item()), clk.summary(), prof, out
 
     peaks, src = measured_peaks()
-    fp64_peak = None
-    pf = REPO / "profiles" / "fp64_peak.json"
-    if pf.exists():
-        fp64_peak = json.loads(pf.read_text()).get("fp64_tflops")
+    fp64_peak = fp64_peak_live(h)
     flop_step = flops(chi)
     gemm_flop_step = 80 * chi ** 3  # the two chi^3 contractions, FP64-equivalent
     traffic = {}
@@ -274,7 +278,7 @@ def run_gpu(args):
             roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                     "frac": (achieved / peaks["bf16_tflops"]) if achieved else None,
                     "traffic": traffic.get("k_split_gemm"),
-                    "traffic_source": ("ncu capture, profiles/k_split_gemm_heff2_chi1024.md"
+                    "traffic_source": ("ncu capture, profiles/heff2_chi1024_traffic.json"
                                        if traffic.get("k_split_gemm") else None),
                     "peak_source": f"MEASURED_PEAKS.json bf16_tflops (burst, {src})",
                     "kernel": "k_split_gemm", "launches": kn, "kernel_ms_per_launch": kms / max(kn, 1),
@@ -289,9 +293,9 @@ def run_gpu(args):
             roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                     "frac": (achieved / fp64_peak) if (achieved and fp64_peak) else None,
                     "traffic": traffic.get("k_gemm_gather_f64"),
-                    "traffic_source": ("ncu capture, profiles/k_gemm_gather_f64_heff2_chi1024.md"
+                    "traffic_source": ("ncu capture, profiles/heff2_chi1024_traffic.json"
                                        if traffic.get("k_gemm_gather_f64") else None),
-                    "peak_source": "profiles/fp64_peak.json (project DFMA probe, measured)",
+                    "peak_source": "itg_fp64_peak: DFMA rate measured live in this run",
                     "kernel": "k_gemm_gather_f64", "launches": kn, "kernel_ms_per_launch": kms / max(kn, 1),
                     "kernel_flop_per_launch": 40 * chi ** 3, "gemm_share_of_step": kms / ms}
         results[name] = {"value": value, "ms_per_step": ms / steps, "steps": steps, "clocks": clocks,
@@ -485,7 +489,7 @@ def run_contract(args):
     h = _lib.handle(0)
     p = lambda t: C.c_void_p(t.data_ptr())
     peaks, src = measured_peaks()
-    fp64_peak = json.loads((REPO / "profiles" / "fp64_peak.json").read_text())["fp64_tflops"]
+    fp64_peak = fp64_peak_live(h)
     flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device="cuda")
     out = []
     for ci, (mA, mB, mC, dims, mnk) in enumerate(_contract_cases(args.contract_cases, 1234 + 2)):
@@ -665,10 +669,7 @@ def run_ops(args):
     U = torch.empty(nn * nn, dtype=torch.float64, device="cuda")
     S = torch.empty(nn, dtype=torch.float64, device="cuda")
     V = torch.empty_like(U)
-    fp64_peak = None
-    pf = REPO / "profiles" / "fp64_peak.json"
-    if pf.exists():
-        fp64_peak = json.loads(pf.read_text()).get("fp64_tflops")
+    fp64_peak = fp64_peak_live(h)
     for name, method, prec in (("fp64_jacobi", 1, 0), ("mixed_split", 2, 1)):
         k, te, dc = C.c_int64(), C.c_double(), C.c_double()
         for rep in range(2):

@@ -75,6 +75,13 @@ ITG_API int itg_destroy(itg_handle* h);
 ITG_API int itg_set_stream(itg_handle* h, void* stream);
 ITG_API int itg_get_stream(itg_handle* h, void** stream);
 ITG_API int itg_synchronize(itg_handle* h);
+/* Device memory the handle holds now: its growable scratch arena, the
+ * split-precision workspace, the autotuning buffer (bytes) and the number of
+ * cached contraction plans (each with its device offset tables).  Any pointer
+ * may be NULL.  No reference counterpart (CUDA.jl's pool is what the
+ * reference's memory accounting goes through). */
+ITG_API int itg_workspace_info(itg_handle* h, size_t* scratch_bytes, size_t* split_bytes, size_t* tune_bytes,
+                               int64_t* plans);
 /* enable = 1: itg_davidson_heff2 captures the H_eff chain once per call into a
  * CUDA graph (on a private capture stream) and replays it for every further
  * matvec.  Off by default. */
@@ -96,6 +103,10 @@ ITG_API int itg_version(void);
 enum { ITG_KERNEL_GEMM_F64 = 0, ITG_KERNEL_GEMM_SPLIT = 1, ITG_KERNEL_SPLIT_PREP = 2 };
 ITG_API int itg_profile(itg_handle* h, int enable);
 ITG_API int itg_profile_read(itg_handle* h, int kernel, double* total_ms, int64_t* launches);
+/* Measured FP64 FMA throughput of the handle's GPU in TFLOP/s (independent
+ * DFMA chains on every SM, best of three timed launches after a warm-up; the
+ * roofline denominator of the plain FP64 contraction).  Synchronises. */
+ITG_API int itg_fp64_peak(itg_handle* h, double* tflops);
 
 /* Autotuning of kernel variants per contraction shape.  Replaces the
  * reference's per-(mode, dim) algorithm cache (src/cudense.jl:284-326, cache
@@ -113,14 +124,12 @@ ITG_API int itg_profile_read(itg_handle* h, int kernel, double* total_ms, int64_
  * enable: 1 (default unless ITG_AUTOTUNE=0 in the environment) or 0
  * (heuristic choice only). */
 enum { ITG_TILE_128x128 = 0, ITG_TILE_128x64 = 1, ITG_TILE_64x64 = 2 };
-/* Split-precision tile variants (split_bn below): 128 and 256 columns, and
- * 256 columns computed by a 2-CTA (PAIR) or 4-CTA (QUAD) cluster whose CTAs
- * share one B tile through TMA multicast.  Any of them | ITG_SPLIT_STREAMK:
- * one persistent CTA (cluster) per resident slot, the launch's work divided
- * evenly between them, a tile shared by consecutive ones at level boundaries
- * and summed with exact integer atomics (same bits as without). */
-enum { ITG_SPLIT_BN_128 = 128, ITG_SPLIT_BN_256 = 256, ITG_SPLIT_BN_256_PAIR = 257, ITG_SPLIT_BN_256_QUAD = 258,
-       ITG_SPLIT_STREAMK = 0x1000 };
+/* Split-precision tile variants (split_bn below): 128 and 256 columns per
+ * CTA.  Either | ITG_SPLIT_STREAMK: one persistent CTA per resident slot, the
+ * launch's work divided evenly between them, a tile shared by consecutive
+ * ones at level boundaries and summed with exact integer atomics (same bits
+ * as without). */
+enum { ITG_SPLIT_BN_128 = 128, ITG_SPLIT_BN_256 = 256, ITG_SPLIT_STREAMK = 0x1000 };
 ITG_API int itg_set_autotune(itg_handle* h, int enable);
 /* entries: size of the process-wide cache; tunings: tuning runs by this handle. */
 ITG_API int itg_autotune_info(itg_handle* h, int64_t* entries, int64_t* tunings);
@@ -416,8 +425,11 @@ ITG_API int itg_heff2_diag(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d,
  * more return ITG_ERR_UNSUPPORTED (itg_heff2_apply has no such limit; with
  * d = 2, w = 5 the limit is about chiL * chiR <= 100000).  FP64 arithmetic
  * only.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.  All
- * calls share the array, so calls that overlap on the GPU race. */
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  The
+ * plans' offset tables are written into the array by a kernel, so a call makes
+ * no host-to-device copy.  Sizes are checked factor by factor against the
+ * array before any product is formed.  All calls share the array, so calls
+ * that overlap on the GPU race. */
 ITG_API int itg_heff2_apply_noalloc(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d,
                                     int64_t wL, int64_t wM, int64_t wR,
                                     const double* L, const double* W1, const double* W2,

@@ -301,7 +301,7 @@ namespace itg {
 int plan_tables_host(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA,
                      int rankB, const int64_t* dimsB, const int32_t* modesB, int rankC,
                      const int64_t* dimsC, const int32_t* modesC, ContractPlan& pl,
-                     std::vector<int64_t>& tab) {
+                     std::vector<int64_t>& tab, PlanTableDesc* desc) {
   auto strides = [](int r, const int64_t* d, int64_t* s) {
     int64_t x = 1;
     for (int i = 0; i < r; ++i) { s[i] = x; x *= d[i]; }
@@ -392,6 +392,21 @@ int plan_tables_host(itg_handle* h, int rankA, const int64_t* dimsA, const int32
       }
     }
   };
+  if (desc) {
+    const std::vector<ModeInfo>* sec[3] = {&freeA, &freeB, &contr};
+    const int w1[3] = {0, 1, 0}, w2[3] = {2, 2, 1};
+    const int64_t cnt[3] = {p->M, p->N, p->K};
+    auto st = [](const ModeInfo& m, int w) { return w == 0 ? m.strA : (w == 1 ? m.strB : m.strC); };
+    for (int g = 0; g < 3; ++g) {
+      desc->nmodes[g] = (int)sec[g]->size();
+      desc->count[g] = cnt[g];
+      for (int i = 0; i < desc->nmodes[g]; ++i) {
+        desc->dim[g][i] = (*sec[g])[i].dim;
+        desc->s1[g][i] = st((*sec[g])[i], w1[g]);
+        desc->s2[g][i] = st((*sec[g])[i], w2[g]);
+      }
+    }
+  }
   int64_t* t = tab.data();
   fill(freeA, p->M, 0, 2, t, t + p->M);
   fill(freeB, p->N, 1, 2, t + 2 * p->M, t + 2 * p->M + p->N);
@@ -411,7 +426,7 @@ int build_plan(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* mo
   auto p = std::make_shared<ContractPlan>();
   std::vector<int64_t> tab;
   ITG_TRY(itg::plan_tables_host(h, rankA, dimsA, modesA, rankB, dimsB, modesB, rankC, dimsC, modesC,
-                                *p, tab));
+                                *p, tab, nullptr));
   if (!tab.empty()) {
     cudaError_t e = cudaMalloc((void**)&p->tables, tab.size() * sizeof(int64_t));
     if (e != cudaSuccess)
@@ -607,10 +622,9 @@ int choose_split(itg_handle* h, const ContractPlan& p, const double* A, const do
     bn = p.split_bn;
     return ITG_OK;
   }
-  // heuristic: 128-wide tiles for narrow outputs; otherwise the 2-CTA cluster
-  // sharing its B tile when there are M tiles to pair
+  // heuristic: 128-wide tiles for narrow outputs, else 256-wide
   const bool narrow = p.N <= 128;
-  bn = narrow ? ITG_SPLIT_BN_128 : (p.M > 128 ? ITG_SPLIT_BN_256_PAIR : ITG_SPLIT_BN_256);
+  bn = narrow ? ITG_SPLIT_BN_128 : ITG_SPLIT_BN_256;
   if (p.key.empty() || narrow) {
     if (!p.key.empty()) p.split_bn = bn;
     return ITG_OK;
@@ -629,13 +643,11 @@ int choose_split(itg_handle* h, const ContractPlan& p, const double* A, const do
   float best = 1e30f;
   int best_bn = bn;
   int st = ITG_OK;
-  // one tile per cluster, or stream-K (persistent clusters, the last partial
-  // wave split at level boundaries): each wins on some shapes
-  const int cands[] = {ITG_SPLIT_BN_256_PAIR, ITG_SPLIT_BN_256_PAIR | ITG_SPLIT_STREAMK,
-                       ITG_SPLIT_BN_256_QUAD | ITG_SPLIT_STREAMK, ITG_SPLIT_BN_256 | ITG_SPLIT_STREAMK,
-                       ITG_SPLIT_BN_128};
+  // one tile per CTA, or stream-K (persistent CTAs, the last partial wave
+  // split at level boundaries): each wins on some shapes
+  const int cands[] = {ITG_SPLIT_BN_256, ITG_SPLIT_BN_256 | ITG_SPLIT_STREAMK, ITG_SPLIT_BN_128,
+                       ITG_SPLIT_BN_128 | ITG_SPLIT_STREAMK};
   for (int cand : cands) {
-    if ((cand & ~ITG_SPLIT_STREAMK) == ITG_SPLIT_BN_256_QUAD && p.M <= 3 * 128) continue;  // mostly zero-filled partners
     float ms = 0.f;
     st = time_variant(h, [&]() { return itg_split_gemm(h, p, A, B, out, alpha, 0.0, cand); }, ms);
     if (st != ITG_OK) break;
@@ -958,7 +970,7 @@ extern "C" int itg_autotune_query(itg_handle* h, int rankA, const int64_t* dimsA
   else *tile = tune::heuristic_tile(h, p.M, p.N);
   if (p.split_bn) *split_bn = p.split_bn;
   else if (tune::lookup("split|" + p.key, v)) *split_bn = v;
-  else *split_bn = p.N <= 128 ? ITG_SPLIT_BN_128 : (p.M > 128 ? ITG_SPLIT_BN_256_PAIR : ITG_SPLIT_BN_256);
+  else *split_bn = p.N <= 128 ? ITG_SPLIT_BN_128 : ITG_SPLIT_BN_256;
   return ITG_OK;
 }
 
@@ -968,8 +980,7 @@ extern "C" int itg_autotune_force(itg_handle* h, int rankA, const int64_t* dimsA
   if (!h) return ITG_ERR_INVALID;
   if (tile > ITG_TILE_64x64 ||
       (split_bn > 0 && (split_bn & ~ITG_SPLIT_STREAMK) != ITG_SPLIT_BN_128 &&
-       (split_bn & ~ITG_SPLIT_STREAMK) != ITG_SPLIT_BN_256 && (split_bn & ~ITG_SPLIT_STREAMK) != ITG_SPLIT_BN_256_PAIR &&
-       (split_bn & ~ITG_SPLIT_STREAMK) != ITG_SPLIT_BN_256_QUAD))
+       (split_bn & ~ITG_SPLIT_STREAMK) != ITG_SPLIT_BN_256))
     return itg_fail(h, ITG_ERR_INVALID, "unknown variant (tile %d, split_bn %d)", tile, split_bn);
   if (rankA < 0 || rankB < 0 || rankC < 0 || rankA > ITG_MAX_RANK || rankB > ITG_MAX_RANK || rankC > ITG_MAX_RANK)
     return itg_fail(h, ITG_ERR_UNSUPPORTED, "rank outside 0..%d", ITG_MAX_RANK);

@@ -178,6 +178,64 @@ extern "C" const char* itg_last_error(itg_handle* h) {
   return h->last_error.c_str();
 }
 
+extern "C" int itg_workspace_info(itg_handle* h, size_t* scratch_bytes, size_t* split_bytes,
+                                  size_t* tune_bytes, int64_t* plans) {
+  if (!h) return ITG_ERR_INVALID;
+  if (scratch_bytes) *scratch_bytes = h->scratch_bytes;
+  if (split_bytes) *split_bytes = h->split_ws_bytes;
+  if (tune_bytes) *tune_bytes = h->tune_buf_bytes;
+  if (plans) *plans = (int64_t)h->plans.size();
+  return ITG_OK;
+}
+
+// FP64 FMA throughput of this GPU: 8 independent DFMA chains per thread,
+// 8 CTAs of 256 threads per SM, a fixed trip count; the result sums the
+// chains so nothing is dead code.  The roofline denominator of the plain FP64
+// contraction (k_gemm_gather_f64 runs on the same DFMA pipe).
+__global__ void k_dfma_rate(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3 + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+extern "C" int itg_fp64_peak(itg_handle* h, double* tflops) {
+  if (!h || !tflops) return ITG_ERR_INVALID;
+  const int threads = 256, blocks = h->num_sms * 8, iters = 4096;
+  ITG_TRY(itg_scratch_reserve(h, sizeof(double) * (size_t)threads * blocks));
+  double* out = (double*)h->scratch;
+  cudaEvent_t e0, e1;
+  ITG_CUDA(h, cudaEventCreate(&e0));
+  ITG_CUDA(h, cudaEventCreate(&e1));
+  float best = 0.f;
+  int st = ITG_OK;
+  for (int rep = 0; rep < 4 && st == ITG_OK; ++rep) {  // the first run warms up
+    cudaEventRecord(e0, h->stream);
+    k_dfma_rate<<<blocks, threads, 0, h->stream>>>(out, iters, 1.0000001, 1e-7);
+    cudaEventRecord(e1, h->stream);
+    if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+      st = itg_fail(h, ITG_ERR_CUDA, "FP64 rate kernel failed");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ITG_TRY(st);
+  const double flop = 2.0 * 8 * iters * (double)threads * blocks;
+  *tflops = best > 0.f ? flop / (best * 1e-3) / 1e12 : 0.0;
+  return ITG_OK;
+}
+
 int itg_scratch_reserve(itg_handle* h, size_t bytes) {
   if (bytes <= h->scratch_bytes) return ITG_OK;
   size_t want = itg_align256(bytes + bytes / 4);

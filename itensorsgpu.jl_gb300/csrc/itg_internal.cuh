@@ -42,6 +42,19 @@ struct ContractPlan {
   }
 };
 
+// The six offset tables of a ContractPlan as mixed-radix sums: section g
+// (0: M, 1: N, 2: K) has count[g] entries; entry l, written as digits of
+// dim[g][0..nmodes[g]) (first mode fastest), gives sum digit * s1 to the
+// section's first table and sum digit * s2 to its second.  Lets a kernel
+// build the tables on the device (itg_noalloc.cu).
+struct PlanTableDesc {
+  int nmodes[3];
+  int64_t count[3];
+  int64_t dim[3][ITG_MAX_RANK];
+  int64_t s1[3][ITG_MAX_RANK];
+  int64_t s2[3][ITG_MAX_RANK];
+};
+
 struct itg_handle {
   int device = 0;
   int num_sms = 0;

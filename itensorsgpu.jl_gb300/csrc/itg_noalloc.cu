@@ -12,11 +12,16 @@
 // Limits and rules (also in include/itg.h):
 //  * capacity ITG_NOALLOC_SCRATCH_DOUBLES doubles (32 MiB) per device, held by
 //    every GPU that loads libitg.so until the process exits; a problem that does
-//    not fit returns ITG_ERR_UNSUPPORTED with the required and available sizes;
+//    not fit returns ITG_ERR_UNSUPPORTED with the required and available sizes
+//    (the sizes are checked factor by factor before any product is formed, so
+//    no dimensions can wrap around the check);
 //  * FP64 arithmetic only (the split path needs a larger workspace);
 //  * the first call on a device resolves the array's device address with
 //    cudaGetSymbolAddress (once per device, under a mutex); make that first call
 //    before any stream capture;
+//  * the contraction plans' offset tables are written into the array by a
+//    kernel from a small by-value descriptor, so a call issues no host-to-device
+//    copy;
 //  * every call reuses the same array, so calls that overlap on the GPU (two
 //    streams, two host threads) race; the array keeps the last call's contents,
 //    and nothing in it needs to start at zero because every intermediate is
@@ -34,7 +39,7 @@ namespace itg {
 int plan_tables_host(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* modesA,
                      int rankB, const int64_t* dimsB, const int32_t* modesB, int rankC,
                      const int64_t* dimsC, const int32_t* modesC, ContractPlan& pl,
-                     std::vector<int64_t>& tab);
+                     std::vector<int64_t>& tab, PlanTableDesc* desc);
 int run_plan(itg_handle* h, const ContractPlan& p, double alpha, const double* A, const double* B,
              double beta, double* C, int precision);
 int heff_form_weff(itg_handle* h, int64_t d, int64_t wL, int64_t wM, int64_t wR, const double* W1,
@@ -67,6 +72,35 @@ int scratch_address(itg_handle* h, double** out) {
   return ITG_OK;
 }
 
+// The six offset tables of a plan (layout of ContractPlan::tables: offAm offCm
+// | offBn offCn | offAk offBk) from their mixed-radix description.
+__global__ void k_plan_tables(const PlanTableDesc d, int64_t* __restrict__ t) {
+  const int64_t M = d.count[0], N = d.count[1], K = d.count[2];
+  const int64_t total = M + N + K;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int g = i < M ? 0 : (i < M + N ? 1 : 2);
+    const int64_t l = g == 0 ? i : (g == 1 ? i - M : i - M - N);
+    int64_t* o1 = g == 0 ? t : (g == 1 ? t + 2 * M : t + 2 * M + 2 * N);
+    int64_t* o2 = o1 + d.count[g];
+    int64_t r = l, a = 0, b = 0;
+    for (int m = 0; m < d.nmodes[g]; ++m) {
+      const int64_t q = r / d.dim[g][m], digit = r - q * d.dim[g][m];
+      a += digit * d.s1[g][m];
+      b += digit * d.s2[g][m];
+      r = q;
+    }
+    o1[l] = a;
+    o2[l] = b;
+  }
+}
+
+// a * b when it stays <= cap (a, b >= 1), else -1; never overflows.
+int64_t mul_capped(int64_t a, int64_t b, int64_t cap) {
+  if (a < 1 || b < 1 || a > cap / b) return -1;
+  return a * b;
+}
+
 // A ContractPlan whose tables live in the static array: never freed.
 struct BorrowedPlan : ContractPlan {
   ~BorrowedPlan() { tables = nullptr; }
@@ -84,9 +118,35 @@ extern "C" int itg_heff2_apply_noalloc(itg_handle* h, int64_t chiL, int64_t chiR
   if (psi == out) return itg_fail(h, ITG_ERR_INVALID, "out must not alias psi");
   if (chiL <= 0 || chiR <= 0 || d <= 0 || wL <= 0 || wM <= 0 || wR <= 0)
     return itg_fail(h, ITG_ERR_SHAPE, "heff2_noalloc: non-positive dimension");
-  const int64_t nc = wL * d * d, nj = d * d * wR;
+  // Sizes, each checked against the capacity before it is formed: T1 and T3
+  // hold chiL * chiR * nc and chiL * chiR * nj doubles, so once those fit every
+  // other buffer (the merged MPO block and the plans' tables, whose lengths are
+  // sums of factors of T1 and T3) is bounded by a small multiple of the cap.
+  const int64_t CAP = ITG_NOALLOC_SCRATCH_DOUBLES;
+  const int64_t dd = mul_capped(d, d, CAP);
+  const int64_t nc = dd < 0 ? -1 : mul_capped(wL, dd, CAP), nj = dd < 0 ? -1 : mul_capped(dd, wR, CAP);
+  const int64_t chi2 = mul_capped(chiL, chiR, CAP);
+  const int64_t nT1 = (chi2 < 0 || nc < 0) ? -1 : mul_capped(chi2, nc, CAP);
+  const int64_t nT3 = (chi2 < 0 || nj < 0) ? -1 : mul_capped(chi2, nj, CAP);
+  if (nT1 < 0 || nT3 < 0)
+    return itg_fail(h, ITG_ERR_UNSUPPORTED,
+                    "heff2_noalloc: the intermediates exceed the fixed no-allocation array of %lld doubles "
+                    "(use itg_heff2_apply)",
+                    (long long)CAP);
   if (nc * nj * 8 > 48 * 1024)
     return itg_fail(h, ITG_ERR_UNSUPPORTED, "heff2_noalloc: MPO block too large");
+  // table lengths of the two chi^3 steps: 2 (M + N + K) each
+  const int64_t nTab1 = 2 * (wL * chiL + dd * chiR + chiL);
+  const int64_t nTab3 = 2 * (chiL * dd + chiR + chiR * wR);
+  // layout in doubles: T1 | T3 | Weff | tables of step 1 | tables of step 3
+  const int64_t oT1 = 0, oT3 = oT1 + align32(nT1), oW = oT3 + align32(nT3);
+  const int64_t oTab1 = oW + align32(nc * nj), oTab3 = oTab1 + align32(nTab1);
+  const int64_t need = oTab3 + align32(nTab3);
+  if (need > CAP)
+    return itg_fail(h, ITG_ERR_UNSUPPORTED,
+                    "heff2_noalloc: needs %lld doubles of scratch, the fixed no-allocation array "
+                    "holds %lld (use itg_heff2_apply)",
+                    (long long)need, (long long)CAP);
   const int64_t dL[3] = {chiL, wL, chiL};
   const int32_t mL[3] = {1, 2, 3};
   const int64_t dP[4] = {chiL, d, d, chiR};
@@ -101,18 +161,11 @@ extern "C" int itg_heff2_apply_noalloc(itg_handle* h, int64_t chiL, int64_t chiR
   const int32_t mO[4] = {3, 7, 9, 11};
   BorrowedPlan p1, p3;
   std::vector<int64_t> tab1, tab3;
-  ITG_TRY(itg::plan_tables_host(h, 3, dL, mL, 4, dP, mP, 5, dT1, mT1, p1, tab1));
-  ITG_TRY(itg::plan_tables_host(h, 5, dT3, mT3, 3, dR, mR, 4, dO, mO, p3, tab3));
-  // layout in doubles: T1 | T3 | Weff | tables of step 1 | tables of step 3
-  const int64_t nT1 = chiL * chiR * nc, nT3 = chiL * chiR * nj;
-  const int64_t oT1 = 0, oT3 = oT1 + align32(nT1), oW = oT3 + align32(nT3);
-  const int64_t oTab1 = oW + align32(nc * nj), oTab3 = oTab1 + align32((int64_t)tab1.size());
-  const int64_t need = oTab3 + align32((int64_t)tab3.size());
-  if (need > ITG_NOALLOC_SCRATCH_DOUBLES)
-    return itg_fail(h, ITG_ERR_UNSUPPORTED,
-                    "heff2_noalloc: needs %lld doubles of scratch, the fixed no-allocation array "
-                    "holds %lld (use itg_heff2_apply)",
-                    (long long)need, (long long)ITG_NOALLOC_SCRATCH_DOUBLES);
+  PlanTableDesc desc1, desc3;
+  ITG_TRY(itg::plan_tables_host(h, 3, dL, mL, 4, dP, mP, 5, dT1, mT1, p1, tab1, &desc1));
+  ITG_TRY(itg::plan_tables_host(h, 5, dT3, mT3, 3, dR, mR, 4, dO, mO, p3, tab3, &desc3));
+  if ((int64_t)tab1.size() != nTab1 || (int64_t)tab3.size() != nTab3)
+    return itg_fail(h, ITG_ERR_INVALID, "heff2_noalloc: unexpected plan table size");
   double* base = nullptr;
   ITG_TRY(scratch_address(h, &base));
   double* T1 = base + oT1;
@@ -120,13 +173,12 @@ extern "C" int itg_heff2_apply_noalloc(itg_handle* h, int64_t chiL, int64_t chiR
   double* Weff = base + oW;
   p1.tables = (int64_t*)(base + oTab1);
   p3.tables = (int64_t*)(base + oTab3);
-  ITG_CUDA(h, cudaMemcpyAsync(p1.tables, tab1.data(), tab1.size() * sizeof(int64_t),
-                              cudaMemcpyHostToDevice, h->stream));
-  ITG_CUDA(h, cudaMemcpyAsync(p3.tables, tab3.data(), tab3.size() * sizeof(int64_t),
-                              cudaMemcpyHostToDevice, h->stream));
+  k_plan_tables<<<itg_blocks_for(nTab1 / 2, 256, h->num_sms * 4), 256, 0, h->stream>>>(desc1, p1.tables);
+  k_plan_tables<<<itg_blocks_for(nTab3 / 2, 256, h->num_sms * 4), 256, 0, h->stream>>>(desc3, p3.tables);
+  ITG_CHECK_LAUNCH(h);
   ITG_TRY(itg::heff_form_weff(h, d, wL, wM, wR, W1, W2, Weff));
   ITG_TRY(itg::run_plan(h, p1, 1.0, L, psi, 0.0, T1, ITG_PREC_FP64));
-  ITG_TRY(itg::heff_mid(h, chiL * chiR, (int)nc, (int)nj, T1, Weff, T3));
+  ITG_TRY(itg::heff_mid(h, chi2, (int)nc, (int)nj, T1, Weff, T3));
   ITG_TRY(itg::run_plan(h, p3, 1.0, T3, R, 0.0, out, ITG_PREC_FP64));
   return ITG_OK;
 }

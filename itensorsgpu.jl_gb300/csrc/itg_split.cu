@@ -111,25 +111,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
 }
-// Multicast variant: the tile lands at the same shared-memory offset in every
-// CTA of ctaMask, and complete_tx is signalled on the mbarrier at the same
-// offset in each of them.
-__device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
-                                               uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
-      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
-      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
-      : "memory");
-}
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
@@ -140,14 +121,6 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
-}
-// Commit arriving on the mbarrier at the same offset in every CTA of ctaMask.
-__device__ __forceinline__ void tc_commit_mc(uint64_t* bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-          smem_u32(bar)),
-      "h"(mask)
-      : "memory");
 }
 __device__ __forceinline__ void tc_mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
                                             uint32_t idesc, uint32_t accumulate) {
@@ -316,25 +289,24 @@ struct GemmArgs {
   double* C;
   double alpha, beta;
   long long* acc;    // one private int64 tile accumulator per CTA
-  long long* tacc;   // shared accumulators of tiles split between clusters (one per CTA)
+  long long* tacc;   // shared accumulators of tiles split between CTAs (one per CTA)
   int* cnt;          // contributions received by each shared accumulator
-  int64_t W;         // tail work units: T * (cluster tiles mod G)
-  int G;             // clusters in the grid
-  int q;             // whole tiles per cluster before the tail
+  int64_t W;         // tail work units: T * (tiles mod G)
+  int G;             // CTAs in the grid
+  int q;             // whole tiles per CTA before the tail
   int* err;
 };
 
-// Work partition over G clusters.  With q, r = divmod(cluster tiles, G),
-// cluster g first computes the whole tiles g, g + G, ..., g + (q - 1) G (in
-// waves, so the tiles in flight at any time are neighbours and share operand
-// panels in L2), then its share of the last r tiles: their units
-// (cluster tile ct, level L) in tile-major order, unit (ct, L) costing L + 1
-// (its k-blocks number (L + 1) * nkb) and starting at offset
-// T * (ct - q G) + L (L + 1) / 2, T = S (S + 1) / 2.  Cluster g owns the tail
-// units whose start offset lies in [lo(g), lo(g + 1)), lo(g) = floor(g W / G),
-// W = T r, so a tail tile may be shared by consecutive clusters, always at a
-// level boundary.  With G equal to the number of cluster tiles every cluster
-// computes exactly one whole tile.
+// Work partition over G persistent CTAs.  With q, r = divmod(tiles, G), CTA
+// g first computes the whole tiles g, g + G, ..., g + (q - 1) G (in waves, so
+// the tiles in flight at any time are neighbours and share operand panels in
+// L2), then its share of the last r tiles: their units (tile ct, level L) in
+// tile-major order, unit (ct, L) costing L + 1 (its k-blocks number
+// (L + 1) * nkb) and starting at offset T * (ct - q G) + L (L + 1) / 2,
+// T = S (S + 1) / 2.  CTA g owns the tail units whose start offset lies in
+// [lo(g), lo(g + 1)), lo(g) = floor(g W / G), W = T r, so a tail tile may be
+// shared by consecutive CTAs, always at a level boundary.  With G equal to
+// the number of tiles every CTA computes exactly one whole tile.
 struct Part {
   int64_t W;  // tail units
   int G, S, T, q;
@@ -352,12 +324,12 @@ struct Part {
       L = 0;
     }
   }
-  // cluster owning the tail unit that starts at offset s: the largest g with lo(g) <= s
+  // CTA owning the tail unit that starts at offset s: the largest g with lo(g) <= s
   __host__ __device__ int owner(int64_t s) const {
     const int64_t g = ((s + 1) * G + W - 1) / W - 1;
     return g < 0 ? 0 : (g >= G ? G - 1 : (int)g);
   }
-  // Segment idx of cluster g (tile ct, levels [L0, Le)); (tb, lb) and (te, le)
+  // Segment idx of CTA g (tile ct, levels [L0, Le)); (tb, lb) and (te, le)
   // are unit_at(lo(g)) and unit_at(lo(g + 1)).  False past the last one.
   __host__ __device__ bool seg(int g, int idx, int tb, int lb, int te, int le, int& ct, int& L0, int& Le) const {
     if (idx < q) {
@@ -373,7 +345,7 @@ struct Part {
     Le = ct == te ? le : S;
     return true;
   }
-  // clusters contributing to tile ct (the distinct owners of its units)
+  // CTAs contributing to tile ct (the distinct owners of its units)
   __host__ __device__ int contributors(int ct, int& first) const {
     if (ct < base()) {
       first = 0;
@@ -455,26 +427,17 @@ __device__ __forceinline__ void load_acc16(uint32_t lane_base, const long long* 
   }
 }
 
-// CS: cluster of CS CTAs (1, 2 or 4) along M sharing one B tile.  Each CTA
-// loads 1/CS of the B tile with a TMA multicast into every CTA's stage, so a
-// stage's B bytes come in equal parts from all CTAs of the cluster and a stage
-// is refilled only when the MMAs of all of them have released it (empty
-// barriers count CS commits, each sent to every CTA).  Cuts the L2 -> SM
-// traffic of B by CS.  All CTAs of a cluster walk the same units (Part).
-//
-// A CTA walks its cluster's units tile segment by tile segment; the pipeline
+// A CTA walks its units (Part) tile segment by tile segment; the pipeline
 // state (stage ring, TMEM buffers) carries over from one segment to the next.
-// A tile owned by one cluster is converted to FP64 straight from the CTA's
+// A tile owned by one CTA is converted to FP64 straight from the CTA's
 // private accumulator.  A shared tile: every contributor adds its private
 // accumulator into the tile's shared one with 64-bit integer atomics (exact,
 // so the result does not depend on their order), then counts itself in; the
 // last one to arrive converts.  Nobody waits for anybody else.
-template <int BN, int CS>
+template <int BN>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
              GemmArgs args) {
-  constexpr bool MC = CS > 1;
-  constexpr uint16_t CMASK = (uint16_t)((1u << CS) - 1u);
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int NST = Smem<BN>::NSTAGE;
@@ -491,8 +454,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
   volatile int* decision = (volatile int*)(bars + 2 * NST + 7);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t rank = MC ? cluster_ctarank() : 0u;
-  const int gcl = (int)(blockIdx.x / CS);  // this CTA's cluster
+  const int gcl = (int)blockIdx.x;  // this CTA's share of the work
   Part part;
   part.W = args.W;
   part.G = args.G;
@@ -507,7 +469,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], CS);
+      mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
@@ -526,7 +488,6 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (MC) cluster_sync_all();  // the partners' barriers exist before any multicast reaches them
   const uint32_t tmem_base = *tmem_slot;
 
   if (warp == 0) {
@@ -538,7 +499,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
       for (int si = 0; ok && part.seg(gcl, si, tb, lb, te, le, ct, L0, Le); ++si) {
         const int m_grp = ct / args.tiles_n;
         const int n_tile = ct - m_grp * args.tiles_n;
-        const int m0 = (CS * m_grp + (int)rank) * BM, n0 = n_tile * BN;
+        const int m0 = m_grp * BM, n0 = n_tile * BN;
         Sched sc;
         sc.begin(args.S, args.nkb);
         sc.seek(L0);
@@ -558,13 +519,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
           uint8_t* sb = sa + Smem<BN>::A_BYTES;
           mbar_arrive_expect_tx(&full[s], Smem<BN>::STAGE_BYTES);
           tma_load_2d(sa, &mapA, sc.kb * BK, sc.p * args.Mpad + m0, &full[s]);
-          if (MC) {
-            // this CTA's part of the B tile, into every CTA (rows rank*BN/CS .. +BN/CS)
-            tma_load_2d_mc(sb + rank * (Smem<BN>::B_BYTES / CS), &mapB, sc.kb * BK,
-                           sc.q() * args.Npad + n0 + (int)rank * (BN / CS), &full[s], CMASK);
-          } else {
-            tma_load_2d(sb, &mapB, sc.kb * BK, sc.q() * args.Npad + n0, &full[s]);
-          }
+          tma_load_2d(sb, &mapB, sc.kb * BK, sc.q() * args.Npad + n0, &full[s]);
           sc.advance();
           ++it;
         }
@@ -605,8 +560,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
             const uint32_t accum = (first && kk == 0) ? 0u : 1u;
             tc_mma_bf16(tmem_d, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), idesc, accum);
           }
-          if (MC) tc_commit_mc(&empty[s], CMASK);
-          else tc_commit(&empty[s]);
+          tc_commit(&empty[s]);
           if (sc.advance()) {
             tc_commit(&acc_full[b]);
             ++lg;
@@ -726,7 +680,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
       int first_owner;
       const int contributors = part.contributors(ct, first_owner);
       const bool shared_tile = contributors > 1;
-      const int slot = first_owner * CS + (int)rank;
+      const int slot = first_owner;
       long long* tile_acc = args.tacc + (size_t)slot * BN * BM;
       if (shared_tile && complete) {
 #pragma unroll 1
@@ -756,7 +710,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
         if (shared_tile) __threadfence();
         const int m_grp = ct / args.tiles_n;
         const int n0 = (ct - m_grp * args.tiles_n) * BN;
-        const int64_t m = (int64_t)(CS * m_grp + (int)rank) * BM + row;
+        const int64_t m = (int64_t)m_grp * BM + row;
         const int64_t cm = m < args.M ? args.offCm[m] : 0;
         const int em = m < args.M ? args.eA[m] - 1022 : 0;
 #pragma unroll 1
@@ -791,9 +745,6 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                  "r"(TMEM_COLS));
   }
-  // the partners may still multicast into this CTA's stages or arrive on its
-  // barriers until they have left their loops (every wait there is bounded)
-  if (MC) cluster_sync_all();
 }
 
 // ----------------------------------------------------------- slicing
@@ -952,60 +903,39 @@ int make_map(itg_handle* h, CUtensorMap* map, void* base, int64_t inner, int64_t
 int ws_reserve(itg_handle* h, size_t bytes);
 
 // CTAs of one variant that fit on the GPU at once (one per SM at this shared
-// memory size; clusters must fit within a GPC), queried once per variant.
-template <int BN, int CS>
-int resident_clusters(itg_handle* h, int& out) {
+// memory size), queried once per variant.
+template <int BN>
+int resident_ctas(itg_handle* h, int& out) {
   static int cached = 0;
   if (cached > 0) {
     out = cached;
     return ITG_OK;
   }
-  int n = 0;
-  if (CS > 1) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(CS * h->num_sms));
-    cfg.blockDim = dim3(NUM_THREADS);
-    cfg.dynamicSmemBytes = Smem<BN>::TOTAL;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = CS;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    if (cudaOccupancyMaxActiveClusters(&n, k_split_gemm<BN, CS>, &cfg) != cudaSuccess || n <= 0) {
-      (void)cudaGetLastError();
-      n = h->num_sms / CS;
-    }
-  } else {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split_gemm<BN, CS>, NUM_THREADS,
-                                                      Smem<BN>::TOTAL) != cudaSuccess ||
-        per_sm <= 0) {
-      (void)cudaGetLastError();
-      per_sm = 1;
-    }
-    n = per_sm * h->num_sms;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_split_gemm<BN>, NUM_THREADS, Smem<BN>::TOTAL) !=
+          cudaSuccess ||
+      per_sm <= 0) {
+    (void)cudaGetLastError();
+    per_sm = 1;
   }
+  const int n = per_sm * h->num_sms;
   cached = n > 0 ? n : 1;
   out = cached;
   return ITG_OK;
 }
 
-// streamk: one persistent cluster per resident slot sharing the work evenly
-// (Part); otherwise one cluster per cluster tile.
-template <int BN, int CS>
+// streamk: one persistent CTA per resident slot sharing the work evenly
+// (Part); otherwise one CTA per tile.
+template <int BN>
 int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
         double alpha, double beta, bool streamk) {
-  constexpr bool MC = CS > 1;
   constexpr int S = S_SLICES;
   const int64_t Mpad = (p.M + BM - 1) / BM * BM;
   const int64_t Npad = (p.N + BN - 1) / BN * BN;
   const int64_t Kpad = (p.K + BK - 1) / BK * BK;
   if (Mpad * S > (int64_t)INT32_MAX || Npad * S > (int64_t)INT32_MAX || Kpad > (int64_t)INT32_MAX)
     return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: problem too large");
-  // clusters group CS M tiles: the count is padded with zero-filled partner tiles
-  const int64_t tiles_m = (Mpad / BM + CS - 1) / CS * CS;
+  const int64_t tiles_m = Mpad / BM;
   const int64_t tiles = tiles_m * (Npad / BN);
   // F: fixed-point fraction bits of the int64 accumulator (keeps |acc| < 2^62).
   int lk = 0;
@@ -1016,21 +946,21 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   // the kernels need the attribute before the occupancy query
   static bool attr = false;
   if (!attr) {
-    ITG_CUDA(h, cudaFuncSetAttribute(k_split_gemm<BN, CS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    ITG_CUDA(h, cudaFuncSetAttribute(k_split_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      Smem<BN>::TOTAL));
     attr = true;
   }
-  const int64_t nct = tiles / CS;  // cluster tiles
+  const int64_t nct = tiles;
   int64_t G = nct;
   if (streamk) {
     int res = 0;
-    const int rst = resident_clusters<BN, CS>(h, res);
+    const int rst = resident_ctas<BN>(h, res);
     if (rst != ITG_OK) return rst;
     G = res;
   }
-  const int64_t grid = G * CS;
+  const int64_t grid = G;
   const int64_t q = nct / G, r = nct % G;
-  const bool shares = r != 0;  // the tail tiles are split between clusters
+  const bool shares = r != 0;  // the tail tiles are split between CTAs
   const size_t tile_bytes = sizeof(long long) * (size_t)BN * BM;
   size_t off = 0;
   auto take = [&](size_t b) { size_t o = off; off += itg_align256(b); return o; };
@@ -1094,7 +1024,7 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   }
   CUtensorMap mA, mB;
   ITG_TRY(make_map(h, &mA, sA, Kpad, Mpad * S, BM));
-  ITG_TRY(make_map(h, &mB, sB, Kpad, Npad * S, BN / CS));
+  ITG_TRY(make_map(h, &mB, sB, Kpad, Npad * S, BN));
   GemmArgs a;
   a.M = p.M;
   a.N = p.N;
@@ -1122,23 +1052,7 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   a.err = err;
   {
     ProfScope prof(h, ITG_KERNEL_GEMM_SPLIT);
-    if (MC) {
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3((unsigned)grid);
-      cfg.blockDim = dim3(NUM_THREADS);
-      cfg.dynamicSmemBytes = Smem<BN>::TOTAL;
-      cfg.stream = h->stream;
-      cudaLaunchAttribute at[1];
-      at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = CS;
-      at[0].val.clusterDim.y = 1;
-      at[0].val.clusterDim.z = 1;
-      cfg.attrs = at;
-      cfg.numAttrs = 1;
-      ITG_CUDA(h, cudaLaunchKernelEx(&cfg, k_split_gemm<BN, CS>, mA, mB, a));
-    } else {
-      k_split_gemm<BN, CS><<<(unsigned)grid, NUM_THREADS, Smem<BN>::TOTAL, h->stream>>>(mA, mB, a);
-    }
+    k_split_gemm<BN><<<(unsigned)grid, NUM_THREADS, Smem<BN>::TOTAL, h->stream>>>(mA, mB, a);
   }
   ITG_CHECK_LAUNCH(h);
   // surface a device-side timeout on the next synchronising call
@@ -1166,18 +1080,15 @@ int ws_reserve(itg_handle* h, size_t bytes) {
 
 }  // namespace split
 
-// bn: tcgen05 tile variant: 128, 256, ITG_SPLIT_BN_256_PAIR / _QUAD (256 wide,
-// 2- / 4-CTA cluster sharing the B tile), optionally | ITG_SPLIT_STREAMK
-// (persistent clusters sharing the work evenly); 0: 128 when N <= 128, else 256.
+// bn: tcgen05 tile variant: 128 or 256 columns, optionally | ITG_SPLIT_STREAMK
+// (persistent CTAs sharing the work evenly); 0: 128 when N <= 128, else 256.
 int itg_split_gemm(itg_handle* h, const ContractPlan& p, const double* A, const double* B, double* C,
                    double alpha, double beta, int bn) {
   if (bn == 0) bn = p.N <= 128 ? 128 : 256;
   const bool sk = (bn & ITG_SPLIT_STREAMK) != 0;
   bn &= ~ITG_SPLIT_STREAMK;
-  if (bn == 128) return split::run<128, 1>(h, p, A, B, C, alpha, beta, sk);
-  if (bn == ITG_SPLIT_BN_256_PAIR) return split::run<256, 2>(h, p, A, B, C, alpha, beta, sk);
-  if (bn == ITG_SPLIT_BN_256_QUAD) return split::run<256, 4>(h, p, A, B, C, alpha, beta, sk);
-  return split::run<256, 1>(h, p, A, B, C, alpha, beta, sk);
+  if (bn == 128) return split::run<128>(h, p, A, B, C, alpha, beta, sk);
+  return split::run<256>(h, p, A, B, C, alpha, beta, sk);
 }
 
 extern "C" int itg_split_partition(int64_t cluster_tiles, int clusters, int g, int32_t* seg, int cap,

@@ -10,7 +10,7 @@ from ._lib import (DimensionMismatch, ITGError, NotConverged, PREC_FP64, PREC_SP
 from .tensor import (Diag, Dense, ITensor, ITensor_host, Index, Spectrum, contract, cpu, cu,
                      cuITensor, dag, delta, dense, diagITensor, dim, eigen, factorize, get_precision, norm, permute,
                      prime, qr, randomCuITensor, set_precision, svd)
-from .mps import (MPO, MPS, cuMPO, cuMPS, heisenberg_mpo, j1j2_mpo, mpo_dense_matrix, op, ops,
+from .mps import (MPO, MPS, cuMPO, cuMPS, heisenberg_mpo, j1j2_mpo, op, ops,
                   productCuMPS, productMPS_host, randomCuMPS, siteinds, spin_ops, tfim_mpo, xxz_mpo)
 from .dmrg import (DMRGResult, Sweeps, cutoff_, dmrg, expect_energy, inner, maxdim_, mindim_,
                    noise_, sweepnext)

@@ -54,12 +54,15 @@ SIGNATURES = {
     "itg_set_stream": (C.c_int, [_P, _P]),
     "itg_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "itg_synchronize": (C.c_int, [_P]),
+    "itg_workspace_info": (C.c_int, [_P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t),
+                                     _I64P]),
     "itg_set_graphs": (C.c_int, [_P, C.c_int]),
     "itg_last_error": (C.c_char_p, [_P]),
     "itg_status_string": (C.c_char_p, [C.c_int]),
     "itg_version": (C.c_int, []),
     "itg_profile": (C.c_int, [_P, C.c_int]),
     "itg_profile_read": (C.c_int, [_P, C.c_int, _DP, _I64P]),
+    "itg_fp64_peak": (C.c_int, [_P, _DP]),
     "itg_malloc": (C.c_int, [_P, C.POINTER(_P), C.c_size_t]),
     "itg_free": (C.c_int, [_P, _P]),
     "itg_memcpy_h2d": (C.c_int, [_P, _P, _P, C.c_size_t]),

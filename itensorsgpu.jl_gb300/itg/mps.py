@@ -417,20 +417,3 @@ def j1j2_mpo(sites, J1=1.0, J2=0.0) -> MPO:
         return w
 
     return _mpo_from_W(sites, W, 7, 0)
-
-
-def mpo_dense_matrix(H: MPO) -> np.ndarray:
-    """Full 2^N x 2^N matrix of a small host MPO (tests only need N <= 12)."""
-    H = cpu(H)
-    M = None
-    for t in H.tensors:
-        W = t.array()  # (wl, s', s, wr)
-        if M is None:
-            M = W[0]  # (s', s, wr)
-            M = M.reshape(W.shape[1], W.shape[2], W.shape[3])
-        else:
-            # M: (S', S, w) ; W: (w, s', s, wr) -> (S' s', S s, wr)
-            M = np.einsum("abw,wcdx->acbdx", M, W)
-            a, c, b, dd, x = M.shape
-            M = M.reshape(a * c, b * dd, x)
-    return M[:, :, 0]

@@ -40,3 +40,11 @@ def gpu(itg_lib):
         pytest.fail("GPU test collected on a machine without CUDA (run with -m 'not gpu')")
     import itg
     return itg
+
+
+def mpo_dense_matrix(H):
+    """Full matrix of a small host MPO (site 0 the slowest index), through the
+    oracle's contraction of its W tensors."""
+    import itg
+    from oracle import itg_oracle as O
+    return O.mpo_matrix([t.array() for t in itg.cpu(H).tensors])

@@ -14,6 +14,7 @@ import numpy as np
 import pytest
 
 from oracle import itg_oracle as O
+from conftest import mpo_dense_matrix
 
 REPO = Path(__file__).resolve().parent.parent
 HEADER = REPO / "include" / "itg.h"
@@ -67,7 +68,7 @@ def test_product_heisenberg_mpo_matches_oracle(N, d):
     import itg
     sites = itg.siteinds("S=1/2" if d == 2 else "S=1", N)
     H = itg.heisenberg_mpo(sites)
-    M = itg.mpo_dense_matrix(H)
+    M = mpo_dense_matrix(H)
     Mo = O.mpo_matrix(O.heisenberg_mpo(N, d=d))
     assert np.allclose(M, Mo, atol=1e-14)
     assert max(t.dims[3] for t in H.tensors[:-1]) == 5
@@ -76,10 +77,10 @@ def test_product_heisenberg_mpo_matches_oracle(N, d):
 def test_product_tfim_and_j1j2_mpos_match_oracle():
     import itg
     sites = itg.siteinds("S=1/2", 6)
-    assert np.allclose(itg.mpo_dense_matrix(itg.tfim_mpo(sites, h=0.5)),
+    assert np.allclose(mpo_dense_matrix(itg.tfim_mpo(sites, h=0.5)),
                        O.mpo_matrix(O.tfim_mpo(6, h=0.5)), atol=1e-14)
     Hj = itg.j1j2_mpo(sites, J1=1.0, J2=0.3)
-    assert np.allclose(itg.mpo_dense_matrix(Hj), O.mpo_matrix(O.heisenberg_mpo(6, J2=0.3)), atol=1e-14)
+    assert np.allclose(mpo_dense_matrix(Hj), O.mpo_matrix(O.heisenberg_mpo(6, J2=0.3)), atol=1e-14)
     assert max(t.dims[3] for t in Hj.tensors[:-1]) == 8
 
 
@@ -89,7 +90,7 @@ def test_xxz_per_bond_couplings():
     J = rng.uniform(0.5, 1.5, 5)
     D = rng.uniform(0.5, 1.5, 5)
     sites = itg.siteinds("S=1/2", 6)
-    M = itg.mpo_dense_matrix(itg.xxz_mpo(sites, J=J, Delta=D))
+    M = mpo_dense_matrix(itg.xxz_mpo(sites, J=J, Delta=D))
     assert np.allclose(M, O.mpo_matrix(O.heisenberg_mpo(6, J=J, Delta=D)), atol=1e-14)
 
 

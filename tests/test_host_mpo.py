@@ -2,6 +2,7 @@
 path runs on equal the Hamiltonians built directly from spin operators."""
 import numpy as np
 import pytest
+from conftest import mpo_dense_matrix
 
 
 def _ops(d):
@@ -40,7 +41,7 @@ def _heis_like(N, d, J, D):
 def _dense(H):
     # site 0 is the slowest index of the dense matrix, as in the Kronecker products
     import itg
-    return itg.mpo_dense_matrix(H)
+    return mpo_dense_matrix(H)
 
 
 @pytest.mark.parametrize("d", [2, 3])

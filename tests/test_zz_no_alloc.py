@@ -5,9 +5,12 @@ or they cannot accept the synchronisation a cudaMalloc may cause).
 Checks, through the C ABI, that two calls in a row give the same result as the
 allocating entry point itg_heff2_apply (relative Frobenius difference <= 1e-12,
 the FP64 contraction tolerance of the other tests), that a stale result from
-the shared scratch array cannot leak into the next call, and that a problem
-larger than the fixed scratch array is refused with a clear error.  This file
-is collected last so that a failure here does not hide any other test.
+the shared scratch array cannot leak into the next call, that a first call on a
+fresh handle with autotuning on leaves every library workspace of the handle
+unallocated, and that a problem larger than the fixed scratch array (also one
+whose sizes would overflow 64-bit products) is refused with a clear error.
+This file is collected last so that a failure here does not hide any other
+test.
 """
 import ctypes as C
 
@@ -67,3 +70,51 @@ def test_noalloc_rejects_oversized_problem(gpu):
                C.c_int64(w), C.c_int64(w), p, p, p, p, p, C.c_void_p(out.data_ptr()))
     assert ei.value.status == _lib.ITG_ERR_UNSUPPORTED
     assert "no-allocation" in str(ei.value)
+
+
+def _workspace(h):
+    sc, sp, tu, pl = C.c_size_t(), C.c_size_t(), C.c_size_t(), C.c_int64()
+    h.call("itg_workspace_info", C.byref(sc), C.byref(sp), C.byref(tu), C.byref(pl))
+    return sc.value, sp.value, tu.value, pl.value
+
+
+def test_noalloc_first_call_on_fresh_handle_allocates_nothing(gpu, monkeypatch):
+    import torch
+    from itg import _lib
+    monkeypatch.setenv("ITG_AUTOTUNE", "1")
+    dims = (64, 48, 2, 5)
+    chiL, chiR, d, w = dims
+    h = _lib.Handle(0)  # fresh handle: no workspace yet
+    try:
+        h.call("itg_set_autotune", 1)
+        assert _workspace(h) == (0, 0, 0, 0)
+        ins = _inputs(chiL, chiR, d, w, 7)
+        got = torch.full((chiL * d * d * chiR,), float("nan"), dtype=torch.float64, device="cuda")
+        _apply(h, "itg_heff2_apply_noalloc", dims, ins, got)
+        torch.cuda.synchronize()
+        assert _workspace(h) == (0, 0, 0, 0)
+        # the allocating entry point on another handle gives the same numbers
+        ref = torch.empty_like(got)
+        _apply(_lib.handle(0), "itg_heff2_apply", dims, ins, ref)
+        torch.cuda.synchronize()
+        err = (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item()
+        assert err <= RTOL, err
+    finally:
+        h.close()
+
+
+def test_noalloc_rejects_sizes_whose_products_overflow(gpu):
+    import torch
+    from itg import _lib
+    h = _lib.handle(0)
+    small = torch.zeros(8, dtype=torch.float64, device="cuda")
+    p = C.c_void_p(small.data_ptr())
+    out = torch.zeros(8, dtype=torch.float64, device="cuda")
+    big = 1 << 40  # chiL * chiR * 20 wraps a signed 64-bit product
+    for chiL, chiR, d in ((big, big, 2), (1, 1, 1 << 33), (big, 1, 2)):
+        with pytest.raises(_lib.ITGError) as ei:
+            h.call("itg_heff2_apply_noalloc", C.c_int64(chiL), C.c_int64(chiR), C.c_int64(d), C.c_int64(5),
+                   C.c_int64(5), C.c_int64(5), p, p, p, p, p, C.c_void_p(out.data_ptr()))
+        assert ei.value.status == _lib.ITG_ERR_UNSUPPORTED
+        assert "no-allocation" in str(ei.value)
+    assert torch.count_nonzero(out).item() == 0
