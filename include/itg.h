@@ -225,6 +225,24 @@ ITG_API int itg_zscal(itg_handle* h, int64_t n, const double* alpha, double* x);
 /* Bound on |C_split - C_exact|_F / (|A|_F |B|_F) for ITG_PREC_SPLIT with the
  * library's slice count at contraction depth K (host-only arithmetic). */
 ITG_API double itg_split_error_bound(int64_t K);
+/* Limit of every bounded device-side wait (the split GEMM's mbarrier waits,
+ * the cooperative Jacobi's grid barrier), in nanoseconds of %globaltimer;
+ * 4 s by default, accepted range [1 us, 60 s].  A wait that runs out makes the
+ * kernel record ITG_ERR_TIMEOUT, stop, wait (bounded) for its own copies in
+ * flight, release what it holds and return; the calling entry point, or the
+ * next synchronising one, reports ITG_ERR_TIMEOUT and the handle stays usable.
+ * The reference's only failure handling on this path is the skip-and-warn
+ * around its cuTENSOR calls (src/tensor/cudense.jl:321-323). */
+ITG_API int itg_set_wait_limit_ns(itg_handle* h, uint64_t ns);
+/* Runs one bounded wait that is designed to run out, through the same device
+ * code as the library's kernels, and returns its status (ITG_ERR_TIMEOUT when
+ * the wait ran out as designed):
+ *   which = 0: the cooperative Jacobi's grid barrier, on 2 blocks, counting
+ *              one participant that never arrives;
+ *   which = 1: the split GEMM's mbarrier wait, on a barrier nobody arrives on.
+ * Takes the handle's wait limit; synchronises.  Failure-path check for
+ * callers and tests; nothing faults, traps or hangs. */
+ITG_API int itg_wait_selftest(itg_handle* h, int which);
 /* Work partition of the split GEMM's stream-K schedule (host-only arithmetic,
  * the code the kernel runs): the tile segments of cluster g when
  * cluster_tiles cluster tiles are shared by `clusters` persistent clusters.

@@ -78,6 +78,9 @@ struct itg_handle {
   std::unordered_map<std::string, std::shared_ptr<ContractPlan>> plans;
   // Device status word for bounded waits (ITG_ERR_TIMEOUT reporting).
   int* dev_status = nullptr;
+  // Limit of every bounded device-side wait, in %globaltimer nanoseconds
+  // (itg_set_wait_limit_ns).
+  uint64_t wait_ns = 4000000000ull;
   // Descriptor array of grouped launches (separate from scratch: grouped calls
   // run inside callers that hold scratch regions).
   void* group_desc = nullptr;

@@ -16,8 +16,9 @@
 // Columns move between SMs from step to step, so every load of W and V goes
 // through L2 (ld.global.cg) and stores bypass L1 (st.global.cg); the barrier
 // fences before arriving and after leaving.  The barrier wait is bounded by
-// %globaltimer (4 s): a block that times out raises a status word that makes
-// every other waiting block leave too, and the host reports ITG_ERR_TIMEOUT.
+// %globaltimer (the handle's wait limit, 4 s by default): a block that times
+// out raises a status word that makes every other waiting block leave too,
+// and the host reports ITG_ERR_TIMEOUT.
 #include "itg_internal.cuh"
 
 #include <cmath>
@@ -26,7 +27,6 @@ namespace {
 
 constexpr int JP_THREADS = 256;
 constexpr int JP_WARPS = JP_THREADS / 32;
-constexpr unsigned long long JP_WAIT_NS = 4000000000ull;
 
 __device__ __forceinline__ unsigned long long jp_timer() {
   unsigned long long t;
@@ -48,7 +48,8 @@ __device__ __forceinline__ T jp_warp_sum(T v) {
 // Grid-wide barrier over `nblocks` co-resident blocks (count / generation
 // words in global memory).  Returns false for every thread of the block when
 // the wait timed out or another block reported a timeout.
-__device__ bool jp_grid_sync(unsigned* count, unsigned* gen, int* status, unsigned nblocks) {
+__device__ bool jp_grid_sync(unsigned* count, unsigned* gen, int* status, unsigned nblocks,
+                             unsigned long long wait_ns) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -67,7 +68,7 @@ __device__ bool jp_grid_sync(unsigned* count, unsigned* gen, int* status, unsign
           good = 0;
           break;
         }
-        if (jp_timer() - t0 > JP_WAIT_NS) {
+        if (jp_timer() - t0 > wait_ns) {
           atomicExch(status, 1);
           good = 0;
           break;
@@ -118,7 +119,7 @@ template <class T, int RC>
 __global__ void __launch_bounds__(JP_THREADS)
 k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, T tol_conv, T amin, T amin_conv,
                  int max_sweeps,
-                 int* aux) {
+                 int* aux, unsigned long long wait_ns) {
   __shared__ T sh[3][JP_WARPS];
   unsigned* count = (unsigned*)aux;
   unsigned* gen = (unsigned*)aux + 1;
@@ -193,7 +194,7 @@ k_jacobi_persist(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T tol, 
         if (t == 0 && a > amin_conv && b > amin_conv && fabs(g) > tol_conv * sqrt(a) * sqrt(b))
           __stcg(rot + sweep, 1);
       }
-      if (!jp_grid_sync(count, gen, status, gridDim.x)) {
+      if (!jp_grid_sync(count, gen, status, gridDim.x, wait_ns)) {
         done = -1;
         break;
       }
@@ -364,9 +365,32 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
   if (t == 0 && major) *rotated = 1;
 }
 
+// Self-test of the grid barrier's timeout path: every block arrives at a
+// barrier that counts one participant more than the grid has, so the count
+// is never met; each block waits until the limit, the first to give up raises
+// the status word and all of them leave.  No block spins past the limit.
+__global__ void k_grid_barrier_selftest(int* aux, unsigned long long wait_ns) {
+  const bool ok = jp_grid_sync((unsigned*)aux, (unsigned*)aux + 1, aux + 2, gridDim.x + 1, wait_ns);
+  if (threadIdx.x == 0 && !ok) atomicAdd(aux + 3, 1);
+}
+
 }  // namespace
 
 namespace itg {
+
+int grid_barrier_selftest(itg_handle* h, int* status, int* blocks_out) {
+  ITG_TRY(itg_scratch_reserve(h, 8 * sizeof(int)));
+  int* aux = (int*)h->scratch;
+  ITG_CUDA(h, cudaMemsetAsync(aux, 0, 8 * sizeof(int), h->stream));
+  k_grid_barrier_selftest<<<2, 32, 0, h->stream>>>(aux, (unsigned long long)h->wait_ns);
+  ITG_CHECK_LAUNCH(h);
+  int* hp = (int*)h->pinned;
+  ITG_CUDA(h, cudaMemcpyAsync(hp, aux, 4 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  *status = hp[2];
+  *blocks_out = hp[3];
+  return ITG_OK;
+}
 
 int jacobi_aux_ints(int max_sweeps) { return 8 + max_sweeps; }
 
@@ -386,8 +410,10 @@ int launch_persist(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, T
   int64_t grid = (int64_t)h->num_sms * per_sm;
   if ((int64_t)np / 2 < grid) grid = np / 2;
   if (grid < 1) grid = 1;
-  void* args[] = {(void*)&W,   (void*)&m,          (void*)&n,  (void*)&V,
-                  (void*)&tol, (void*)&tol_conv, (void*)&amin, (void*)&amin_conv, (void*)&max_sweeps, (void*)&aux};
+  unsigned long long wait_ns = h->wait_ns;
+  void* args[] = {(void*)&W,          (void*)&m,          (void*)&n,    (void*)&V,
+                  (void*)&tol,        (void*)&tol_conv,   (void*)&amin, (void*)&amin_conv,
+                  (void*)&max_sweeps, (void*)&aux,        (void*)&wait_ns};
   ITG_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_jacobi_persist<T, RC>, dim3((unsigned)grid),
                                           dim3(JP_THREADS), args, 0, h->stream));
   return ITG_OK;

@@ -33,9 +33,10 @@
 //   warp 1    TMEM allocator and single-thread tcgen05.mma issuer
 //   warps 2-9 TMEM drain / epilogue: warp w reads TMEM lanes 32*(w%4)..+31 and
 //             owns half of the tile's columns
-// Every mbarrier wait is bounded (globaltimer, ~4 s); on timeout the kernel
-// records ITG_ERR_TIMEOUT, stops issuing work, waits (bounded) for its own
-// copies and MMAs, frees TMEM and returns.
+// Every mbarrier wait is bounded (%globaltimer; the handle's wait limit,
+// itg_set_wait_limit_ns, 4 s by default); on timeout the kernel records
+// ITG_ERR_TIMEOUT, stops issuing work, waits (bounded, regardless of the
+// abort) for its own copies and MMAs still in flight, frees TMEM and returns.
 #include "itg_internal.cuh"
 
 #include <cuda.h>
@@ -55,7 +56,6 @@ constexpr int BK = 64;         // K per pipeline stage (128 bytes of bf16)
 constexpr int STAGES = 4;
 constexpr int NUM_EPI_WARPS = 8;  // two per TMEM lane quarter, each owning half the columns
 constexpr int NUM_THREADS = 64 + 32 * NUM_EPI_WARPS;
-constexpr uint64_t WAIT_NS = 4000000000ull;  // bounded waits: 4 s
 
 // ------------------------------------------------------------ PTX wrappers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -86,21 +86,33 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait; returns false (and records the timeout) when it runs out.
+// Bounded wait (wait_ns of %globaltimer); returns false when it runs out,
+// recording ITG_ERR_TIMEOUT and raising the CTA's abort flag, or when another
+// role of the CTA raised the flag first.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
-                                          volatile int* abort_flag) {
+                                          volatile int* abort_flag, uint64_t wait_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
   for (uint32_t it = 0;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 63) == 63) {
       if (*abort_flag) return false;
-      if (globaltimer() - t0 > WAIT_NS) {
+      if (globaltimer() - t0 > wait_ns) {
         atomicExch(err, ITG_ERR_TIMEOUT);
         *abort_flag = 1;
         return false;
       }
     }
+  }
+}
+// Bounded wait that ignores the abort flag: on the way out, for this CTA's own
+// TMA copies and MMAs still in flight (they complete by themselves; the bound
+// only guards against a wait that can never end).
+__device__ __forceinline__ bool mbar_drain(uint64_t* bar, uint32_t parity, uint64_t wait_ns) {
+  const uint64_t t0 = globaltimer();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 63) == 63 && globaltimer() - t0 > wait_ns) return false;
   }
 }
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
@@ -294,6 +306,7 @@ struct GemmArgs {
   int64_t W;         // tail work units: T * (tiles mod G)
   int G;             // CTAs in the grid
   int q;             // whole tiles per CTA before the tail
+  uint64_t wait_ns;  // limit of every mbarrier wait (%globaltimer ns)
   int* err;
 };
 
@@ -510,7 +523,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
           }
           const int s = it % NST;
           if (it >= NST) {
-            if (!mbar_wait(&empty[s], ((it / NST) - 1) & 1, args.err, abort_flag)) {
+            if (!mbar_wait(&empty[s], ((it / NST) - 1) & 1, args.err, abort_flag, args.wait_ns)) {
               ok = false;
               break;
             }
@@ -525,8 +538,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
         }
       }
       // make sure no copy is still landing in shared memory when we leave
-      for (int j = std::max(0, it - NST); j < it; ++j)
-        mbar_wait(&full[j % NST], (j / NST) & 1, args.err, abort_flag);
+      for (int j = std::max(0, it - NST); j < it; ++j) mbar_drain(&full[j % NST], (j / NST) & 1, args.wait_ns);
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------- MMA issuer
@@ -543,12 +555,12 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
           const int b = lg & 1;
           const bool first = sc.first_in_group;
           if (first && lg >= 2) {
-            ok = mbar_wait(&acc_empty[b], ((lg >> 1) - 1) & 1, args.err, abort_flag);
+            ok = mbar_wait(&acc_empty[b], ((lg >> 1) - 1) & 1, args.err, abort_flag, args.wait_ns);
             tc_fence_after();
             if (!ok) break;
           }
           const int s = it % NST;
-          ok = mbar_wait(&full[s], (it / NST) & 1, args.err, abort_flag);
+          ok = mbar_wait(&full[s], (it / NST) & 1, args.err, abort_flag, args.wait_ns);
           if (!ok) break;
           tc_fence_after();
           const uint32_t sa = smem_u32(stage_mem + s * Smem<BN>::STAGE_BYTES);
@@ -570,7 +582,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
       }
       // all MMAs issued by this thread complete before TMEM is released
       tc_commit(done_bar);
-      mbar_wait(done_bar, 0, args.err, abort_flag);
+      mbar_drain(done_bar, 0, args.wait_ns);
     }
   } else {
     // ------------------------------------------------------ drain/epilogue
@@ -604,7 +616,7 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
         const int b = lg & 1;
         // every lane polls; the outcome is made warp-uniform because the TMEM
         // loads below are .sync.aligned
-        const bool ok_lane = mbar_wait(&acc_full[b], (lg >> 1) & 1, args.err, abort_flag);
+        const bool ok_lane = mbar_wait(&acc_full[b], (lg >> 1) & 1, args.err, abort_flag, args.wait_ns);
         if (!__all_sync(0xffffffffu, ok_lane)) break;
         tc_fence_after();
 #pragma unroll
@@ -745,6 +757,26 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                  "r"(TMEM_COLS));
   }
+}
+
+// Self-test of the mbarrier timeout path shared by every role of
+// k_split_gemm: one thread waits, through mbar_wait, for phase 0 of a
+// barrier that expects one arrival nobody makes; the wait runs out after the
+// limit, records ITG_ERR_TIMEOUT in *err and raises the abort flag.
+__global__ void k_mbar_selftest(int* err, uint64_t wait_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const bool ok = mbar_wait(&bar, 0, err, (volatile int*)&abort_flag, wait_ns);
+    if (ok) atomicExch(err, ITG_OK);
+  }
+  __syncthreads();
 }
 
 // ----------------------------------------------------------- slicing
@@ -1049,6 +1081,7 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   a.W = (int64_t)(S * (S + 1) / 2) * r;
   a.G = (int)G;
   a.q = (int)q;
+  a.wait_ns = h->wait_ns;
   a.err = err;
   {
     ProfScope prof(h, ITG_KERNEL_GEMM_SPLIT);
@@ -1089,6 +1122,44 @@ int itg_split_gemm(itg_handle* h, const ContractPlan& p, const double* A, const 
   bn &= ~ITG_SPLIT_STREAMK;
   if (bn == 128) return split::run<128>(h, p, A, B, C, alpha, beta, sk);
   return split::run<256>(h, p, A, B, C, alpha, beta, sk);
+}
+
+namespace itg {
+int grid_barrier_selftest(itg_handle* h, int* status, int* blocks_out);  // itg_jacobi.cu
+}
+
+extern "C" int itg_set_wait_limit_ns(itg_handle* h, uint64_t ns) {
+  if (!h) return ITG_ERR_INVALID;
+  if (ns < 1000ull || ns > 60000000000ull)
+    return itg_fail(h, ITG_ERR_INVALID, "wait limit %llu ns outside [1 us, 60 s]", (unsigned long long)ns);
+  h->wait_ns = ns;
+  return ITG_OK;
+}
+
+extern "C" int itg_wait_selftest(itg_handle* h, int which) {
+  if (!h) return ITG_ERR_INVALID;
+  if (which == 0) {
+    int status = 0, blocks = 0;
+    ITG_TRY(itg::grid_barrier_selftest(h, &status, &blocks));
+    if (status != 0)
+      return itg_fail(h, ITG_ERR_TIMEOUT, "grid barrier wait ran out after %llu ns (%d of 2 blocks gave up)",
+                      (unsigned long long)h->wait_ns, blocks);
+    return itg_fail(h, ITG_ERR_INVALID, "grid barrier self-test: the wait did not run out");
+  }
+  if (which == 1) {
+    ITG_TRY(itg_scratch_reserve(h, 256));
+    int* err = (int*)h->scratch;
+    ITG_CUDA(h, cudaMemsetAsync(err, 0xFF, sizeof(int), h->stream));  // -1: not reported
+    split::k_mbar_selftest<<<1, 32, 0, h->stream>>>(err, h->wait_ns);
+    ITG_CHECK_LAUNCH(h);
+    int* hp = (int*)h->pinned;
+    ITG_CUDA(h, cudaMemcpyAsync(hp, err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hp[0] == ITG_ERR_TIMEOUT)
+      return itg_fail(h, ITG_ERR_TIMEOUT, "mbarrier wait ran out after %llu ns", (unsigned long long)h->wait_ns);
+    return itg_fail(h, ITG_ERR_INVALID, "mbarrier self-test: the wait did not run out (%d)", hp[0]);
+  }
+  return itg_fail(h, ITG_ERR_INVALID, "unknown self-test %d", which);
 }
 
 extern "C" int itg_split_partition(int64_t cluster_tiles, int clusters, int g, int32_t* seg, int cap,

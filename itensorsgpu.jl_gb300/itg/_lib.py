@@ -75,6 +75,8 @@ SIGNATURES = {
                                C.c_double,
                                _P, C.c_int, _I64P, _I32P, C.c_int]),
     "itg_split_error_bound": (C.c_double, [C.c_int64]),
+    "itg_set_wait_limit_ns": (C.c_int, [_P, C.c_uint64]),
+    "itg_wait_selftest": (C.c_int, [_P, C.c_int]),
     "itg_split_partition": (C.c_int, [C.c_int64, C.c_int, C.c_int, _I32P, C.c_int, C.POINTER(C.c_int)]),
     "itg_contract_z": (C.c_int, [_P, C.c_int, C.c_int, _DP,
                                  _P, C.c_int, _I64P, _I32P,

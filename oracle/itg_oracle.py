@@ -88,6 +88,75 @@ def contract(A: np.ndarray, la, B: np.ndarray, lb, lc) -> np.ndarray:
     return np.einsum(spec, A, B, optimize=True)
 
 
+def _exact_slices(X: np.ndarray, axis: int, nslices: int = 4, bits: int = 14):
+    """Row (axis=1: rows of an M x K matrix) or column (axis=0) scaled integer
+    slices of X: X = 2^e * sum_p s_p 2^(-bits (p + 1)) up to 2^(-bits nslices - 1)
+    relative to the row maximum.  Balanced digits (round to nearest), so
+    |s_0| <= 2^bits, |s_p| <= 2^(bits - 1) and the truncation residue has no
+    bias; every s_p is an integer held exactly in FP64.  Returns (slices, e)."""
+    mx = np.max(np.abs(X), axis=axis, keepdims=True)
+    _, e = np.frexp(np.where(mx > 0, mx, 1.0))       # mx < 2^e
+    r = np.ldexp(X, -e)                                # |r| < 1, exact (power-of-two scaling)
+    out = []
+    for _ in range(nslices):
+        r = np.ldexp(r, bits)
+        s = np.rint(r)
+        out.append(s)
+        r = r - s                                      # exact: |r - s| <= 1/2
+    return out, e
+
+
+def matmul_exact(A: np.ndarray, B: np.ndarray) -> np.ndarray:
+    """A @ B for FP64 matrices with an error near one rounding of each output.
+
+    Compensated checker for deep contractions (large K), where an FP64 BLAS
+    product carries up to K * 2^-53 of rounding relative to |A| |B|.  Each row
+    of A and column of B is split into balanced integer slices of 14 bits (4
+    slices, truncation below 2^-57 of the row / column maximum); every slice
+    product is a sum of integers below 2^(28 + log2 K), and each level's sum of
+    at most four of them stays below 2^53 for K < 2^22, so BLAS computes them
+    exactly in any summation order.  The levels p + q <= 3 are combined with
+    Neumaier's compensated summation; the dropped levels are below 2^-54 of
+    |A| |B| and, the digits being balanced, add up without bias."""
+    K = A.shape[1]
+    if K >= (1 << 22):
+        raise ValueError("matmul_exact: K too large for exact slice products")
+    sa, ea = _exact_slices(A, axis=1)
+    sb, eb = _exact_slices(B, axis=0)
+    terms = []
+    for L in range(4):
+        acc = None
+        for p in range(L + 1):
+            t = sa[p] @ sb[L - p]                      # exact integers
+            acc = t if acc is None else acc + t        # exact: < 2^(30 + log2 K) <= 2^53
+        terms.append(np.ldexp(acc, -14 * (L + 2)))
+    s = terms[0].copy()
+    c = np.zeros_like(s)
+    for t in terms[1:]:
+        u = s + t
+        c += np.where(np.abs(s) >= np.abs(t), (s - u) + t, (t - u) + s)
+        s = u
+    return np.ldexp(s + c, ea + eb)
+
+
+def contract_exact(A: np.ndarray, la, B: np.ndarray, lb, lc) -> np.ndarray:
+    """contract() through matmul_exact: the same labels and output order, the
+    contracted labels folded into one GEMM depth."""
+    la, lb, lc = list(la), list(lb), list(lc)
+    con = [x for x in la if x in lb and x not in lc]
+    fa = [x for x in la if x in lc]
+    fb = [x for x in lb if x in lc]
+    dims = {x: A.shape[i] for i, x in enumerate(la)}
+    dims.update({x: B.shape[i] for i, x in enumerate(lb)})
+    M = int(np.prod([dims[x] for x in fa], dtype=np.int64))
+    N = int(np.prod([dims[x] for x in fb], dtype=np.int64))
+    K = int(np.prod([dims[x] for x in con], dtype=np.int64))
+    A2 = np.transpose(A, [la.index(x) for x in fa + con]).reshape(M, K)
+    B2 = np.transpose(B, [lb.index(x) for x in con + fb]).reshape(K, N)
+    C2 = matmul_exact(A2, B2).reshape([dims[x] for x in fa + fb])
+    return np.transpose(C2, [(fa + fb).index(x) for x in lc])
+
+
 def permute(A: np.ndarray, la, lb) -> np.ndarray:
     return np.transpose(A, [list(la).index(x) for x in lb])
 
