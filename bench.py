@@ -193,7 +193,7 @@ def run_gpu(args):
     import torch
     import torch.distributed as dist
     from itg import _lib
-    from itg._lib import (KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_SPLIT_PREP, PREC_FP64,
+    from itg._lib import (KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_HEFF_MID, KERNEL_SPLIT_PREP, PREC_FP64,
                           PREC_SPLIT)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -251,7 +251,7 @@ def run_gpu(args):
         t_local = torch.tensor([ms], dtype=torch.float64, device=dev)
         if world > 1:
             dist.all_reduce(t_local, op=dist.ReduceOp.MAX)
-        prof = {k: read_prof(k) for k in (KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_SPLIT_PREP)}
+        prof = {k: read_prof(k) for k in (KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_SPLIT_PREP, KERNEL_HEFF_MID)}
         return float(t_local.item()), clk.summary(), prof, out
 
     peaks, src = measured_peaks()
@@ -286,6 +286,7 @@ def run_gpu(args):
                     "flop_note": "bf16 tensor flop executed: 28 digit products x 2MNK per chi^3 contraction",
                     "fp64_equiv_tflops": gemm_flop_step * steps / (kms / 1e3) / 1e12 if kms > 0 else None,
                     "prep_ms_per_step": prep_ms / steps,
+                    "mid_ms_per_step": prof[KERNEL_HEFF_MID][0] / steps,
                     "gemm_share_of_step": kms / ms}
         else:
             kms, kn = prof[KERNEL_GEMM_F64]

@@ -99,8 +99,9 @@ ITG_API int itg_version(void);
  * and launch count of one kernel class:
  *   ITG_KERNEL_GEMM_F64   the FP64 gather-GEMM (k_gemm_gather_f64)
  *   ITG_KERNEL_GEMM_SPLIT the tcgen05 split-precision GEMM (k_split_gemm)
- *   ITG_KERNEL_SPLIT_PREP the split operand preparation (exponents + digits) */
-enum { ITG_KERNEL_GEMM_F64 = 0, ITG_KERNEL_GEMM_SPLIT = 1, ITG_KERNEL_SPLIT_PREP = 2 };
+ *   ITG_KERNEL_SPLIT_PREP the split operand preparation (exponents + digits)
+ *   ITG_KERNEL_HEFF_MID   the middle (merged-MPO) step of the H_eff matvec */
+enum { ITG_KERNEL_GEMM_F64 = 0, ITG_KERNEL_GEMM_SPLIT = 1, ITG_KERNEL_SPLIT_PREP = 2, ITG_KERNEL_HEFF_MID = 3 };
 ITG_API int itg_profile(itg_handle* h, int enable);
 ITG_API int itg_profile_read(itg_handle* h, int kernel, double* total_ms, int64_t* launches);
 /* Measured FP64 FMA throughput of the handle's GPU in TFLOP/s (independent

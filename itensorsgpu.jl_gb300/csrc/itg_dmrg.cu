@@ -23,6 +23,7 @@ int get_plan(itg_handle* h, int rankA, const int64_t* dimsA, const int32_t* mode
              const int32_t* modesC, std::shared_ptr<ContractPlan>& plan);
 int run_plan(itg_handle* h, const ContractPlan& p, double alpha, const double* A, const double* B,
              double beta, double* C, int precision);
+int heff_mid_split(itg_handle* h, int64_t R, int nc, int nj, const double* T1, const double* Weff, double* T3);
 }  // namespace itg
 
 namespace {
@@ -163,9 +164,18 @@ int heff_apply(itg_handle* h, const HeffDims& D, const double* L, const double* 
   ITG_TRY(itg::run_plan(h, *p1, 1.0, L, psi, 0.0, w.T1, precision));
   const int64_t Rrows = D.chiL * D.chiR;
   const int nc = (int)D.nc(), nj = (int)D.nj();
-  k_heff_mid<<<itg_blocks_for(Rrows, 256, h->num_sms * 8), 256, sizeof(double) * nc * nj, h->stream>>>(
-      w.T1, w.Weff, w.T3, Rrows, nc, nj);
-  ITG_CHECK_LAUNCH(h);
+  // split precision: the middle step on the tensor cores by the same exact
+  // digit products (nc, nj <= 32); otherwise FP64 FMA
+  int mid = ITG_ERR_UNSUPPORTED;
+  if (precision == ITG_PREC_SPLIT) mid = itg::heff_mid_split(h, Rrows, nc, nj, w.T1, w.Weff, w.T3);
+  if (mid == ITG_ERR_UNSUPPORTED) {
+    ProfScope prof(h, ITG_KERNEL_HEFF_MID);
+    k_heff_mid<<<itg_blocks_for(Rrows, 256, h->num_sms * 8), 256, sizeof(double) * nc * nj, h->stream>>>(
+        w.T1, w.Weff, w.T3, Rrows, nc, nj);
+    ITG_CHECK_LAUNCH(h);
+  } else {
+    ITG_TRY(mid);
+  }
   ITG_TRY(itg::run_plan(h, *p3, 1.0, w.T3, R, 0.0, out, precision));
   return ITG_OK;
 }

@@ -44,6 +44,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 
 
@@ -857,6 +858,211 @@ __device__ __forceinline__ void make_digits(double x, int efield_r, int (&d)[S])
   }
 }
 
+// ------------------------------------------------- H_eff middle step
+// T3[r, j] = sum_c T1[r, c] Weff[c, j] for R rows r, c < nc <= 32, j < nj <= 32
+// (the merged-MPO step of the two-site H_eff chain: K = nc = wL d^2, N = nj =
+// d^2 wR), by the same exact digit products as k_split_gemm.  A CTA takes 128
+// rows: every thread loads its row of T1 (coalesced across the CTA per c),
+// forms the row exponent and the 7 balanced digits of each element, and
+// writes them K-major with the 128-byte swizzle into shared memory, two
+// slices per 128-byte row (slice p at k offset 32 (p % 2) of tile p / 2); the
+// digits of Weff's columns go the same way into the B tiles.  One thread
+// issues the 28 digit products (two K = 16 steps each) into seven TMEM level
+// accumulators of NJP columns; one group per level suffices because
+// sum_{p+q=L} nc 2^(7+7) <= 7 * 32 * 2^14 < 2^24 keeps every FP32 partial
+// sum an exact integer.  Each thread then reads its row's level sums, forms
+// the int64 fixed-point value and converts it to FP64 with integer
+// instructions: the same bits as k_split_gemm for this product.
+constexpr int MID_ROWS = 128;
+constexpr int MID_THREADS = 128;
+constexpr int MID_KSLICE = 32;  // padded K per slice (nc <= 32)
+constexpr int MID_A_TILE = MID_ROWS * 128;   // bytes: 128 rows x 128 B (two slices)
+constexpr int MID_NTILE = (S_SLICES + 1) / 2;  // 4 tiles hold the 7 slices
+
+template <int NJP>
+struct MidSmem {
+  static constexpr int B_TILE = NJP * 128;
+  static constexpr int A_OFF = 0;
+  static constexpr int B_OFF = MID_NTILE * MID_A_TILE;
+  static constexpr int TOTAL = 1024 /*align slack*/ + B_OFF + MID_NTILE * B_TILE + 256;
+  static constexpr uint32_t TMEM_COLS = (S_SLICES * NJP <= 128) ? 128u : 256u;
+};
+
+// byte offset of element (row i, k) of a K-major 128-byte-swizzled tile
+__device__ __forceinline__ uint32_t sw128_off(int i, int k) {
+  return (uint32_t)(i * 128 + ((((k >> 3) ^ (i & 7))) << 4) + ((k & 7) << 1));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(int lo, int hi) {
+  const uint32_t a = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)lo));
+  const uint32_t b = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)hi));
+  return a | (b << 16);
+}
+
+// Writes the digits of 8 consecutive k (c0 .. c0 + 7 of slice p) of row i.
+__device__ __forceinline__ void store_digit_chunk(uint8_t* tile, int i, int p, int c0, const int (&dg)[8]) {
+  const int k = (p & 1) * MID_KSLICE + c0;
+  uint4 v;
+  v.x = pack_bf16x2(dg[0], dg[1]);
+  v.y = pack_bf16x2(dg[2], dg[3]);
+  v.z = pack_bf16x2(dg[4], dg[5]);
+  v.w = pack_bf16x2(dg[6], dg[7]);
+  *(uint4*)(tile + sw128_off(i, k)) = v;
+}
+
+template <int NJP>
+__global__ void __launch_bounds__(MID_THREADS)
+k_heff_mid_split(const double* __restrict__ T1, const double* __restrict__ Weff, double* __restrict__ T3,
+                 int64_t R, int nc, int nj, uint64_t wait_ns, int* err) {
+  constexpr int S = S_SLICES;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* sA = base + MidSmem<NJP>::A_OFF;
+  uint8_t* sB = base + MidSmem<NJP>::B_OFF;
+  uint8_t* tail = sB + MID_NTILE * MidSmem<NJP>::B_TILE;
+  uint64_t* done = (uint64_t*)tail;
+  uint32_t* tmem_slot = (uint32_t*)(tail + 8);
+  int* fB = (int*)(tail + 16);              // [NJP] column exponent fields of Weff
+  volatile int* abort_flag = (volatile int*)(tail + 16 + 4 * 32);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int64_t r = (int64_t)blockIdx.x * MID_ROWS + t;
+
+  if (t == 0) {
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(MidSmem<NJP>::TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  // ---- B: digits of Weff's columns (row j of the B tiles, k = c)
+  {
+    const int j = t >> 2, cg = t & 3;  // NJP * 4 <= 128 threads
+    if (j < NJP) {
+      int ef = 0;
+      if (j < nj) {
+        unsigned long long mx = 0;
+        for (int c = 0; c < nc; ++c) {
+          const unsigned long long b = (unsigned long long)__double_as_longlong(Weff[c + (int64_t)nc * j]) &
+                                       0x7FFFFFFFFFFFFFFFull;
+          mx = b > mx ? b : mx;
+        }
+        ef = (int)((mx >> 52) & 0x7FF);
+      }
+      if (cg == 0) fB[j] = ef;
+      int dg[S][8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int c = cg * 8 + e;
+        int d[S];
+        make_digits<S>((j < nj && c < nc) ? Weff[c + (int64_t)nc * j] : 0.0, ef, d);
+#pragma unroll
+        for (int p = 0; p < S; ++p) dg[p][e] = d[p];
+      }
+#pragma unroll
+      for (int p = 0; p < S; ++p) store_digit_chunk(sB + (p >> 1) * MidSmem<NJP>::B_TILE, j, p, cg * 8, dg[p]);
+      if (S & 1) {  // the unused upper half of the last tile: zeros
+        const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        store_digit_chunk(sB + (S >> 1) * MidSmem<NJP>::B_TILE, j, S, cg * 8, zero);
+      }
+    }
+  }
+  // ---- A: this thread's row of T1
+  double x[MID_KSLICE];
+  unsigned long long mx = 0;
+#pragma unroll
+  for (int c = 0; c < MID_KSLICE; ++c) {
+    x[c] = (c < nc && r < R) ? T1[r + R * c] : 0.0;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x[c]) & 0x7FFFFFFFFFFFFFFFull;
+    mx = b > mx ? b : mx;
+  }
+  const int eA = (int)((mx >> 52) & 0x7FF);
+#pragma unroll
+  for (int cg = 0; cg < MID_KSLICE / 8; ++cg) {
+    int dg[S][8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      int d[S];
+      make_digits<S>(x[cg * 8 + e], eA, d);
+#pragma unroll
+      for (int p = 0; p < S; ++p) dg[p][e] = d[p];
+    }
+#pragma unroll
+    for (int p = 0; p < S; ++p) store_digit_chunk(sA + (p >> 1) * MID_A_TILE, t, p, cg * 8, dg[p]);
+    if (S & 1) {
+      const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      store_digit_chunk(sA + (S >> 1) * MID_A_TILE, t, S, cg * 8, zero);
+    }
+  }
+  // generic-proxy smem writes -> visible to the tensor core (async proxy)
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+  const int ksteps = nc > 16 ? 2 : 1;
+  if (t == 0) {
+    constexpr uint32_t idesc = idesc_bf16(MID_ROWS, NJP);
+    for (int L = 0; L < S; ++L) {
+      for (int p = 0; p <= L; ++p) {
+        const int q = L - p;
+        const uint64_t ad = sdesc_sw128(smem_u32(sA + (p >> 1) * MID_A_TILE));
+        const uint64_t bd = sdesc_sw128(smem_u32(sB + (q >> 1) * MidSmem<NJP>::B_TILE));
+        for (int s = 0; s < ksteps; ++s) {
+          const uint64_t ka = (uint64_t)(2 * (2 * (p & 1) + s)), kb = (uint64_t)(2 * (2 * (q & 1) + s));
+          tc_mma_bf16(tmem_base + (uint32_t)(L * NJP), ad + ka, bd + kb, idesc, (p > 0 || s > 0) ? 1u : 0u);
+        }
+      }
+    }
+    tc_commit(done);
+  }
+  // every thread waits (bounded) for the products, then drains its row
+  const bool ok = mbar_wait(done, 0, err, abort_flag, wait_ns);
+  tc_fence_after();
+  if (__all_sync(0xffffffffu, ok)) {
+    int lk = 0;
+    while ((1 << lk) < nc) ++lk;
+    const int F = 62 - 15 - lk;
+    long long acc[NJP];
+#pragma unroll
+    for (int j = 0; j < NJP; ++j) acc[j] = 0;
+    const uint32_t lane_base = tmem_base + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+    for (int L = 0; L < S; ++L) {
+      uint32_t v[16];
+#pragma unroll
+      for (int h = 0; h < NJP / 16; ++h) {
+        tc_ld_32x32b_x16(lane_base + (uint32_t)(L * NJP + 16 * h), v);
+        const int sh = F - 7 * L;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          long long tv = (long long)__float2int_rn(__uint_as_float(v[j]));
+          tv = sh >= 0 ? (long long)((unsigned long long)tv << sh) : (tv >> (-sh));
+          acc[16 * h + j] += tv;
+        }
+      }
+    }
+    if (r < R) {
+      const int em = eA - 1022;
+#pragma unroll
+      for (int j = 0; j < NJP; ++j)
+        if (j < nj) T3[r + R * j] = i64_to_double_scaled(acc[j], em + fB[j] - 1022 - 14 - F);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) {
+    // after a timeout the products may still be in flight: wait (bounded) before freeing TMEM
+    if (!__all_sync(0xffffffffu, ok)) mbar_drain(done, 0, wait_ns);
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "r"(MidSmem<NJP>::TMEM_COLS));
+  }
+}
+
 // out[p][r][k] (bf16, k contiguous, padded to Rpad x Kpad) for the gathered X.
 template <bool KMAJ, int S>
 __global__ void __launch_bounds__(256)
@@ -1093,6 +1299,38 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   return ITG_OK;
 }
 
+// The H_eff middle step on the tensor cores (k_heff_mid_split); rows R =
+// chiL chiR, T1 / T3 column-major with R rows.  ITG_ERR_UNSUPPORTED when nc or
+// nj exceeds 32 (the caller then runs the FP64 kernel).
+int heff_mid_split(itg_handle* h, int64_t R, int nc, int nj, const double* T1, const double* Weff, double* T3) {
+  if (nc < 1 || nj < 1 || nc > MID_KSLICE || nj > 32) return ITG_ERR_UNSUPPORTED;
+  const int64_t grid = (R + MID_ROWS - 1) / MID_ROWS;
+  if (grid > (int64_t)INT32_MAX) return itg_fail(h, ITG_ERR_UNSUPPORTED, "heff mid: too many rows");
+  ITG_TRY(ws_reserve(h, 256));
+  int* err = (int*)h->split_ws;
+  ITG_CUDA(h, cudaMemsetAsync(err, 0, sizeof(int), h->stream));
+  auto launch = [&](auto njp_tag) -> int {
+    constexpr int NJP = decltype(njp_tag)::value;
+    static bool attr = false;
+    if (!attr) {
+      ITG_CUDA(h, cudaFuncSetAttribute(k_heff_mid_split<NJP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       MidSmem<NJP>::TOTAL));
+      attr = true;
+    }
+    k_heff_mid_split<NJP><<<(unsigned)grid, MID_THREADS, MidSmem<NJP>::TOTAL, h->stream>>>(T1, Weff, T3, R, nc, nj,
+                                                                                            h->wait_ns, err);
+    ITG_CHECK_LAUNCH(h);
+    return ITG_OK;
+  };
+  {
+    ProfScope prof(h, ITG_KERNEL_HEFF_MID);
+    if (nj <= 16) ITG_TRY(launch(std::integral_constant<int, 16>()));
+    else ITG_TRY(launch(std::integral_constant<int, 32>()));
+  }
+  ITG_CUDA(h, cudaMemcpyAsync(h->dev_status, err, sizeof(int), cudaMemcpyDeviceToDevice, h->stream));
+  return ITG_OK;
+}
+
 int ws_reserve(itg_handle* h, size_t bytes) {
   if (bytes <= h->split_ws_bytes) return ITG_OK;
   size_t want = itg_align256(bytes + bytes / 8);
@@ -1112,6 +1350,12 @@ int ws_reserve(itg_handle* h, size_t bytes) {
 }
 
 }  // namespace split
+
+namespace itg {
+int heff_mid_split(itg_handle* h, int64_t R, int nc, int nj, const double* T1, const double* Weff, double* T3) {
+  return split::heff_mid_split(h, R, nc, nj, T1, Weff, T3);
+}
+}  // namespace itg
 
 // bn: tcgen05 tile variant: 128 or 256 columns, optionally | ITG_SPLIT_STREAMK
 // (persistent CTAs sharing the work evenly); 0: 128 when N <= 128, else 256.

@@ -24,7 +24,7 @@ ITG_ERR_TIMEOUT, ITG_ERR_NOTCONVERGED, ITG_ERR_UNSUPPORTED = 5, 6, 7
 ITG_F64 = 0
 ITG_C64 = 1
 PREC_FP64, PREC_SPLIT = 0, 1
-KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_SPLIT_PREP = 0, 1, 2
+KERNEL_GEMM_F64, KERNEL_GEMM_SPLIT, KERNEL_SPLIT_PREP, KERNEL_HEFF_MID = 0, 1, 2, 3
 SVD_AUTO, SVD_JACOBI, SVD_MIXED = 0, 1, 2
 
 

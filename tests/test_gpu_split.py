@@ -118,6 +118,32 @@ def test_split_heff_matches_oracle(gpu):
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12
 
 
+@pytest.mark.parametrize("chiL,chiR,d,w", [(7, 9, 2, 5), (40, 33, 2, 4), (130, 130, 2, 5), (50, 70, 2, 3),
+                                            (33, 17, 3, 4)])
+def test_split_heff_middle_step_shapes(gpu, chiL, chiR, d, w):
+    """The split matvec's middle step runs on the tensor cores for nc = w d^2 and
+    nj = d^2 w up to 32 (one or two K = 16 steps, 16- or 32-column TMEM level
+    accumulators, a ragged last row block) and on FP64 FMA above (d = 3, w = 4:
+    nc = 36); both within 1e-12 of the oracle."""
+    from itg import _lib
+    import torch
+    rng = np.random.default_rng(chiL * 7 + chiR)
+    L = rng.standard_normal((chiL, w, chiL))
+    R = rng.standard_normal((chiR, w, chiR))
+    W1 = rng.standard_normal((w, d, d, w))
+    W2 = rng.standard_normal((w, d, d, w))
+    psi = rng.standard_normal((chiL, d, d, chiR))
+    h = _lib.handle(0)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    Ld, W1d, W2d, Rd, pd = map(_dev, (L, W1, W2, R, psi))
+    out = torch.full_like(pd, float("nan"))
+    h.call("itg_heff2_apply", C.c_int64(chiL), C.c_int64(chiR), C.c_int64(d), C.c_int64(w), C.c_int64(w),
+           C.c_int64(w), p(Ld), p(W1d), p(W2d), p(Rd), p(pd), p(out), 1)
+    ref = O.heff_apply(L, W1, W2, R, psi)
+    got = O.unflat(out.cpu().numpy(), psi.shape)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12
+
+
 def test_split_dmrg_energy_matches_fp64(gpu):
     N = 16
     sites = gpu.siteinds("S=1/2", N)
