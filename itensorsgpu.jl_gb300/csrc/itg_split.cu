@@ -858,25 +858,63 @@ __device__ __forceinline__ void make_digits(double x, int efield_r, int (&d)[S])
   }
 }
 
+// make_digits for S = 7 with 32-bit integer work: the same balanced digits,
+// returned as magnitudes-with-sign-applied-later: d (as make_digits gives for
+// |x|) and neg.  Y (at most 49 bits) splits into 28 + 21 bits whose 7-bit
+// fields are the unbalanced digits u_p; the balanced ones follow by one carry
+// pass from the least significant digit (v = u_p + carry, v >= 64 -> v - 128
+// with carry 1), which is what make_digits' repeated (Y - d) >> 7 computes.
+__device__ __forceinline__ void make_digits7_abs(double x, int efield_r, int (&d)[7], bool& neg) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  neg = (bits >> 63) != 0;
+  const int E = (int)((bits >> 52) & 0x7FF);
+  unsigned long long M = bits & ((1ull << 52) - 1);
+  if (E) M |= 1ull << 52;
+  const int Ee = E ? E : 1;
+  const int sh = Ee - 1075 - (efield_r - 1022) + 49;
+  unsigned long long Y;
+  if (M == 0 || E == 2047) {
+    Y = 0;
+  } else if (sh >= 0) {
+    Y = M << sh;
+  } else if (sh <= -60) {
+    Y = 0;
+  } else {
+    Y = (M >> (-sh)) + ((M >> (-sh - 1)) & 1ull);
+  }
+  const uint32_t lo = (uint32_t)Y & 0x0FFFFFFFu, hi = (uint32_t)(Y >> 28);
+  const uint32_t u[7] = {hi >> 14, (hi >> 7) & 127u, hi & 127u, lo >> 21, (lo >> 14) & 127u, (lo >> 7) & 127u,
+                         lo & 127u};
+  int c = 0;
+#pragma unroll
+  for (int p = 6; p >= 1; --p) {
+    const int v = (int)u[p] + c;
+    c = v >= 64;
+    d[p] = c ? v - 128 : v;
+  }
+  d[0] = (int)u[0] + c;
+}
+
 // ------------------------------------------------- H_eff middle step
 // T3[r, j] = sum_c T1[r, c] Weff[c, j] for R rows r, c < nc <= 32, j < nj <= 32
 // (the merged-MPO step of the two-site H_eff chain: K = nc = wL d^2, N = nj =
-// d^2 wR), by the same exact digit products as k_split_gemm.  A CTA takes 128
-// rows: every thread loads its row of T1 (coalesced across the CTA per c),
-// forms the row exponent and the 7 balanced digits of each element, and
-// writes them K-major with the 128-byte swizzle into shared memory, two
-// slices per 128-byte row (slice p at k offset 32 (p % 2) of tile p / 2); the
-// digits of Weff's columns go the same way into the B tiles.  One thread
-// issues the 28 digit products (two K = 16 steps each) into seven TMEM level
-// accumulators of NJP columns; one group per level suffices because
-// sum_{p+q=L} nc 2^(7+7) <= 7 * 32 * 2^14 < 2^24 keeps every FP32 partial
-// sum an exact integer.  Each thread then reads its row's level sums, forms
-// the int64 fixed-point value and converts it to FP64 with integer
-// instructions: the same bits as k_split_gemm for this product.
+// d^2 wR), by the same exact digit products as k_split_gemm.  Persistent CTAs
+// of 128 threads walk blocks of 128 rows.  Per block every thread loads its
+// row of T1 (coalesced across the CTA per c), forms the row exponent and the
+// 7 balanced digits of each element, and writes them K-major with the
+// 128-byte swizzle into shared memory, two slices per 128-byte row (slice p
+// at k offset 32 (p % 2) of tile p / 2); Weff's column digits are written the
+// same way once per CTA.  One thread issues the 28 digit products (one or two
+// K = 16 steps each) into seven TMEM level accumulators of NJP columns; one
+// group per level suffices because sum_{p+q=L} nc 2^(7+7) <= 7 * 32 * 2^14 <
+// 2^22 keeps every FP32 partial sum an exact integer.  Each thread then reads
+// its row's level sums, forms the int64 fixed-point value and converts it to
+// FP64 with integer instructions: the same bits as k_split_gemm computes for
+// this product (same digits, same fixed point, same rounding).
 constexpr int MID_ROWS = 128;
 constexpr int MID_THREADS = 128;
 constexpr int MID_KSLICE = 32;  // padded K per slice (nc <= 32)
-constexpr int MID_A_TILE = MID_ROWS * 128;   // bytes: 128 rows x 128 B (two slices)
+constexpr int MID_A_TILE = MID_ROWS * 128;     // bytes: 128 rows x 128 B (two slices)
 constexpr int MID_NTILE = (S_SLICES + 1) / 2;  // 4 tiles hold the 7 slices
 
 template <int NJP>
@@ -893,21 +931,46 @@ __device__ __forceinline__ uint32_t sw128_off(int i, int k) {
   return (uint32_t)(i * 128 + ((((k >> 3) ^ (i & 7))) << 4) + ((k & 7) << 1));
 }
 
+// bf16 bits of two small integers (|d| <= 2^8, exact in bf16) packed low | high:
+// float(d) = (0x4B400000 + d as float bits) - 1.5 * 2^23 exactly, and the bf16
+// of a float with at most 8 significant bits is its upper half.
 __device__ __forceinline__ uint32_t pack_bf16x2(int lo, int hi) {
-  const uint32_t a = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)lo));
-  const uint32_t b = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)hi));
-  return a | (b << 16);
+  const float fl = __int_as_float(0x4B400000 + lo) - 12582912.0f;
+  const float fh = __int_as_float(0x4B400000 + hi) - 12582912.0f;
+  return __byte_perm((uint32_t)__float_as_int(fl), (uint32_t)__float_as_int(fh), 0x7632);
 }
 
-// Writes the digits of 8 consecutive k (c0 .. c0 + 7 of slice p) of row i.
-__device__ __forceinline__ void store_digit_chunk(uint8_t* tile, int i, int p, int c0, const int (&dg)[8]) {
+// Writes the digits of 8 consecutive k (c0 .. c0 + 7 of slice p) of row i;
+// sgn[q] holds the sign bits (0x8000 per half) of elements 2q, 2q + 1.
+__device__ __forceinline__ void store_digit_chunk(uint8_t* tile, int i, int p, int c0, const int (&dg)[8],
+                                                  const uint32_t (&sgn)[4]) {
   const int k = (p & 1) * MID_KSLICE + c0;
   uint4 v;
-  v.x = pack_bf16x2(dg[0], dg[1]);
-  v.y = pack_bf16x2(dg[2], dg[3]);
-  v.z = pack_bf16x2(dg[4], dg[5]);
-  v.w = pack_bf16x2(dg[6], dg[7]);
+  v.x = pack_bf16x2(dg[0], dg[1]) ^ sgn[0];
+  v.y = pack_bf16x2(dg[2], dg[3]) ^ sgn[1];
+  v.z = pack_bf16x2(dg[4], dg[5]) ^ sgn[2];
+  v.w = pack_bf16x2(dg[6], dg[7]) ^ sgn[3];
   *(uint4*)(tile + sw128_off(i, k)) = v;
+}
+
+// The 7 digits of 8 elements (x[c0 .. c0 + 7], row exponent field ef) into the
+// 7 slices' chunks of row i.  A negative element's digits are the negated
+// digits of its magnitude (bf16 sign bit), as make_digits forms them.
+__device__ __forceinline__ void digits8(uint8_t* tiles, int tile_bytes, int i, int c0, const double* x, int ef) {
+  constexpr int S = S_SLICES;
+  int dg[S][8];
+  uint32_t sgn[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    int d[S];
+    bool neg;
+    make_digits7_abs(x[e], ef, d, neg);
+    if (neg) sgn[e >> 1] |= (e & 1) ? 0x80000000u : 0x00008000u;
+#pragma unroll
+    for (int p = 0; p < S; ++p) dg[p][e] = d[p];
+  }
+#pragma unroll
+  for (int p = 0; p < S; ++p) store_digit_chunk(tiles + (p >> 1) * tile_bytes, i, p, c0, dg[p], sgn);
 }
 
 template <int NJP>
@@ -922,10 +985,10 @@ k_heff_mid_split(const double* __restrict__ T1, const double* __restrict__ Weff,
   uint8_t* tail = sB + MID_NTILE * MidSmem<NJP>::B_TILE;
   uint64_t* done = (uint64_t*)tail;
   uint32_t* tmem_slot = (uint32_t*)(tail + 8);
-  int* fB = (int*)(tail + 16);              // [NJP] column exponent fields of Weff
+  int* fB = (int*)(tail + 16);  // [NJP] column exponent fields of Weff
   volatile int* abort_flag = (volatile int*)(tail + 16 + 4 * 32);
-  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int64_t r = (int64_t)blockIdx.x * MID_ROWS + t;
+  const int t = threadIdx.x, warp = t >> 5;
+  const int ngrp = (nc + 7) >> 3;  // 8-element groups of c holding data
 
   if (t == 0) {
     mbar_init(done, 1);
@@ -937,7 +1000,15 @@ k_heff_mid_split(const double* __restrict__ T1, const double* __restrict__ Weff,
                  "r"(MidSmem<NJP>::TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  // ---- B: digits of Weff's columns (row j of the B tiles, k = c)
+  // A chunks no block writes (k groups past nc): zero once
+  {
+    const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const uint32_t nosign[4] = {0u, 0u, 0u, 0u};
+    for (int cg = ngrp; cg < MID_KSLICE / 8; ++cg)
+#pragma unroll
+      for (int p = 0; p < S; ++p) store_digit_chunk(sA + (p >> 1) * MID_A_TILE, t, p, cg * 8, zero, nosign);
+  }
+  // B: digits of Weff's columns (row j of the B tiles, k = c), once per CTA
   {
     const int j = t >> 2, cg = t & 3;  // NJP * 4 <= 128 threads
     if (j < NJP) {
@@ -952,95 +1023,87 @@ k_heff_mid_split(const double* __restrict__ T1, const double* __restrict__ Weff,
         ef = (int)((mx >> 52) & 0x7FF);
       }
       if (cg == 0) fB[j] = ef;
-      int dg[S][8];
+      double w[8];
 #pragma unroll
       for (int e = 0; e < 8; ++e) {
         const int c = cg * 8 + e;
-        int d[S];
-        make_digits<S>((j < nj && c < nc) ? Weff[c + (int64_t)nc * j] : 0.0, ef, d);
-#pragma unroll
-        for (int p = 0; p < S; ++p) dg[p][e] = d[p];
+        w[e] = (j < nj && c < nc) ? Weff[c + (int64_t)nc * j] : 0.0;
       }
-#pragma unroll
-      for (int p = 0; p < S; ++p) store_digit_chunk(sB + (p >> 1) * MidSmem<NJP>::B_TILE, j, p, cg * 8, dg[p]);
-      if (S & 1) {  // the unused upper half of the last tile: zeros
-        const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        store_digit_chunk(sB + (S >> 1) * MidSmem<NJP>::B_TILE, j, S, cg * 8, zero);
-      }
+      digits8(sB, MidSmem<NJP>::B_TILE, j, cg * 8, w, ef);
     }
   }
-  // ---- A: this thread's row of T1
-  double x[MID_KSLICE];
-  unsigned long long mx = 0;
-#pragma unroll
-  for (int c = 0; c < MID_KSLICE; ++c) {
-    x[c] = (c < nc && r < R) ? T1[r + R * c] : 0.0;
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x[c]) & 0x7FFFFFFFFFFFFFFFull;
-    mx = b > mx ? b : mx;
-  }
-  const int eA = (int)((mx >> 52) & 0x7FF);
-#pragma unroll
-  for (int cg = 0; cg < MID_KSLICE / 8; ++cg) {
-    int dg[S][8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      int d[S];
-      make_digits<S>(x[cg * 8 + e], eA, d);
-#pragma unroll
-      for (int p = 0; p < S; ++p) dg[p][e] = d[p];
-    }
-#pragma unroll
-    for (int p = 0; p < S; ++p) store_digit_chunk(sA + (p >> 1) * MID_A_TILE, t, p, cg * 8, dg[p]);
-    if (S & 1) {
-      const int zero[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      store_digit_chunk(sA + (S >> 1) * MID_A_TILE, t, S, cg * 8, zero);
-    }
-  }
-  // generic-proxy smem writes -> visible to the tensor core (async proxy)
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
+  const uint32_t lane_base = tmem_base + ((uint32_t)(warp * 32) << 16);
   const int ksteps = nc > 16 ? 2 : 1;
-  if (t == 0) {
-    constexpr uint32_t idesc = idesc_bf16(MID_ROWS, NJP);
-    for (int L = 0; L < S; ++L) {
-      for (int p = 0; p <= L; ++p) {
-        const int q = L - p;
-        const uint64_t ad = sdesc_sw128(smem_u32(sA + (p >> 1) * MID_A_TILE));
-        const uint64_t bd = sdesc_sw128(smem_u32(sB + (q >> 1) * MidSmem<NJP>::B_TILE));
-        for (int s = 0; s < ksteps; ++s) {
-          const uint64_t ka = (uint64_t)(2 * (2 * (p & 1) + s)), kb = (uint64_t)(2 * (2 * (q & 1) + s));
-          tc_mma_bf16(tmem_base + (uint32_t)(L * NJP), ad + ka, bd + kb, idesc, (p > 0 || s > 0) ? 1u : 0u);
+  int lk = 0;
+  while ((1 << lk) < nc) ++lk;
+  const int F = 62 - 15 - lk;
+  const int64_t nblk = (R + MID_ROWS - 1) / MID_ROWS;
+  bool ok = true;
+  uint32_t phase = 0;
+  for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x, phase ^= 1u) {
+    const int64_t r = blk * MID_ROWS + t;
+    // ---- A: this thread's row of T1 (all loads first)
+    double x[MID_KSLICE];
+#pragma unroll
+    for (int c = 0; c < MID_KSLICE; ++c) x[c] = (c < nc && r < R) ? __ldcs(T1 + r + R * c) : 0.0;
+    unsigned long long mx = 0;
+#pragma unroll
+    for (int c = 0; c < MID_KSLICE; ++c) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(x[c]) & 0x7FFFFFFFFFFFFFFFull;
+      mx = b > mx ? b : mx;
+    }
+    const int eA = (int)((mx >> 52) & 0x7FF);
+#pragma unroll
+    for (int cg = 0; cg < MID_KSLICE / 8; ++cg)
+      if (cg < ngrp) digits8(sA, MID_A_TILE, t, cg * 8, x + cg * 8, eA);
+    // generic-proxy smem writes -> visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (t == 0) {
+      constexpr uint32_t idesc = idesc_bf16(MID_ROWS, NJP);
+      for (int L = 0; L < S; ++L) {
+        for (int p = 0; p <= L; ++p) {
+          const int q = L - p;
+          const uint64_t ad = sdesc_sw128(smem_u32(sA + (p >> 1) * MID_A_TILE));
+          const uint64_t bd = sdesc_sw128(smem_u32(sB + (q >> 1) * MidSmem<NJP>::B_TILE));
+          for (int s = 0; s < ksteps; ++s) {
+            const uint64_t ka = (uint64_t)(2 * (2 * (p & 1) + s)), kb = (uint64_t)(2 * (2 * (q & 1) + s));
+            tc_mma_bf16(tmem_base + (uint32_t)(L * NJP), ad + ka, bd + kb, idesc, (p > 0 || s > 0) ? 1u : 0u);
+          }
         }
       }
+      tc_commit(done);
     }
-    tc_commit(done);
-  }
-  // every thread waits (bounded) for the products, then drains its row
-  const bool ok = mbar_wait(done, 0, err, abort_flag, wait_ns);
-  tc_fence_after();
-  if (__all_sync(0xffffffffu, ok)) {
-    int lk = 0;
-    while ((1 << lk) < nc) ++lk;
-    const int F = 62 - 15 - lk;
+    // every thread waits (bounded) for the products, then drains its row
+    ok = mbar_wait(done, phase, err, abort_flag, wait_ns);
+    tc_fence_after();
+    // CTA-uniform decision: every thread reaches this barrier whatever its wait returned
+    if (__syncthreads_or(!ok)) {
+      ok = false;
+      break;
+    }
+    // int64 fixed point: acc = sum_L s_L 2^(F - 7L) (F >= 42 here, so every
+    // shift is a left shift), by Horner over the levels and one final shift
     long long acc[NJP];
 #pragma unroll
-    for (int j = 0; j < NJP; ++j) acc[j] = 0;
-    const uint32_t lane_base = tmem_base + ((uint32_t)(warp * 32) << 16);
-#pragma unroll
     for (int L = 0; L < S; ++L) {
-      uint32_t v[16];
 #pragma unroll
       for (int h = 0; h < NJP / 16; ++h) {
-        tc_ld_32x32b_x16(lane_base + (uint32_t)(L * NJP + 16 * h), v);
-        const int sh = F - 7 * L;
+        if (16 * h < nj) {
+          uint32_t v[16];
+          tc_ld_32x32b_x16(lane_base + (uint32_t)(L * NJP + 16 * h), v);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          long long tv = (long long)__float2int_rn(__uint_as_float(v[j]));
-          tv = sh >= 0 ? (long long)((unsigned long long)tv << sh) : (tv >> (-sh));
-          acc[16 * h + j] += tv;
+          for (int j = 0; j < 16; ++j) {
+            // exact integer below 2^22 in magnitude: float -> int by the 1.5 * 2^23 shift
+            const long long tv = (long long)(__float_as_int(__uint_as_float(v[j]) + 12582912.0f) - 0x4B400000);
+            acc[16 * h + j] = L == 0 ? tv : (long long)((unsigned long long)acc[16 * h + j] << 7) + tv;
+          }
         }
       }
     }
@@ -1048,15 +1111,21 @@ k_heff_mid_split(const double* __restrict__ T1, const double* __restrict__ Weff,
       const int em = eA - 1022;
 #pragma unroll
       for (int j = 0; j < NJP; ++j)
-        if (j < nj) T3[r + R * j] = i64_to_double_scaled(acc[j], em + fB[j] - 1022 - 14 - F);
+        if (j < nj)
+          __stcs(T3 + r + R * j, i64_to_double_scaled((long long)((unsigned long long)acc[j] << (F - 42)),
+                                                      em + fB[j] - 1022 - 14 - F));
     }
+    // the TMEM accumulators and the A tiles are reused by the next block
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   if (warp == 0) {
     // after a timeout the products may still be in flight: wait (bounded) before freeing TMEM
-    if (!__all_sync(0xffffffffu, ok)) mbar_drain(done, 0, wait_ns);
+    if (!ok) mbar_drain(done, phase, wait_ns);
     __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                  "r"(MidSmem<NJP>::TMEM_COLS));
@@ -1315,10 +1384,21 @@ int heff_mid_split(itg_handle* h, int64_t R, int nc, int nj, const double* T1, c
     if (!attr) {
       ITG_CUDA(h, cudaFuncSetAttribute(k_heff_mid_split<NJP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        MidSmem<NJP>::TOTAL));
+      ITG_CUDA(h, cudaFuncSetAttribute(k_heff_mid_split<NJP>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared));
       attr = true;
     }
-    k_heff_mid_split<NJP><<<(unsigned)grid, MID_THREADS, MidSmem<NJP>::TOTAL, h->stream>>>(T1, Weff, T3, R, nc, nj,
-                                                                                            h->wait_ns, err);
+    // CTAs per SM: by shared memory (the carveout is set to its maximum) and by
+    // TMEM (512 columns per SM)
+    int smem_sm = 0;
+    ITG_CUDA(h, cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, h->device));
+    int per_sm = smem_sm / (MidSmem<NJP>::TOTAL + 1024);
+    const int tmem_cap = (int)(512u / MidSmem<NJP>::TMEM_COLS);
+    if (per_sm > tmem_cap) per_sm = tmem_cap;
+    if (per_sm < 1) per_sm = 1;
+    const int64_t g = std::min<int64_t>(grid, (int64_t)per_sm * h->num_sms);
+    k_heff_mid_split<NJP><<<(unsigned)g, MID_THREADS, MidSmem<NJP>::TOTAL, h->stream>>>(T1, Weff, T3, R, nc, nj,
+                                                                                         h->wait_ns, err);
     ITG_CHECK_LAUNCH(h);
     return ITG_OK;
   };
