@@ -133,6 +133,8 @@ extern "C" int itg_destroy(itg_handle* h) {
   cudaSetDevice(h->device);
   cudaStreamSynchronize(h->stream);
   itg_release_plans(h);
+  for (auto& c : h->slice_cache)
+    if (c.buf) cudaFree(c.buf);
   prof_clear(h);
   for (auto e : h->prof_pool) cudaEventDestroy(e);
   if (h->scratch) cudaFree(h->scratch);

@@ -161,7 +161,13 @@ int heff_apply(itg_handle* h, const HeffDims& D, const double* L, const double* 
   std::shared_ptr<ContractPlan> p1, p3;
   ITG_TRY(itg::get_plan(h, 3, dL, mL, 4, dP, mP, 5, dT1, mT1, p1));
   ITG_TRY(itg::get_plan(h, 5, dT3, mT3, 3, dR, mR, 4, dO, mO, p3));
-  ITG_TRY(itg::run_plan(h, *p1, 1.0, L, psi, 0.0, w.T1, precision));
+  // inside one Davidson solve L and R are constant: the split path keeps their
+  // digit slices (step 1's A operand, step 3's B operand) after the first matvec
+  const bool keep = h->heff_keep_env_slices && precision == ITG_PREC_SPLIT;
+  h->slice_keep[0] = keep;
+  const int st1 = itg::run_plan(h, *p1, 1.0, L, psi, 0.0, w.T1, precision);
+  h->slice_keep[0] = false;
+  ITG_TRY(st1);
   const int64_t Rrows = D.chiL * D.chiR;
   const int nc = (int)D.nc(), nj = (int)D.nj();
   // split precision: the middle step on the tensor cores by the same exact
@@ -176,7 +182,10 @@ int heff_apply(itg_handle* h, const HeffDims& D, const double* L, const double* 
   } else {
     ITG_TRY(mid);
   }
-  ITG_TRY(itg::run_plan(h, *p3, 1.0, w.T3, R, 0.0, out, precision));
+  h->slice_keep[1] = keep;
+  const int st3 = itg::run_plan(h, *p3, 1.0, w.T3, R, 0.0, out, precision);
+  h->slice_keep[1] = false;
+  ITG_TRY(st3);
   return ITG_OK;
 }
 
@@ -417,6 +426,17 @@ static int davidson_impl(itg_handle* h, int64_t chiL, int64_t chiR, int64_t d, i
   if (!h || !L || !W1 || !W2 || !R || !psi || !energy) return ITG_ERR_INVALID;
   HeffDims D{chiL, chiR, d, wL, wM, wR};
   ITG_TRY(heff_validate(h, D));
+  // L and R do not change during the solve: let the split matvecs keep their
+  // digit slices; forget them when the solve ends, however it ends
+  struct EnvSliceScope {
+    itg_handle* h;
+    explicit EnvSliceScope(itg_handle* hh) : h(hh) { h->heff_keep_env_slices = true; }
+    ~EnvSliceScope() {
+      h->heff_keep_env_slices = false;
+      h->slice_cache[0].valid = false;
+      h->slice_cache[1].valid = false;
+    }
+  } env_scope(h);
   const int kmax = krylovdim < 2 ? 2 : (krylovdim > 32 ? 32 : krylovdim);
   if (maxiter < 1) maxiter = 1;
   const int64_t n = D.n();

@@ -55,6 +55,19 @@ struct PlanTableDesc {
   int64_t s2[3][ITG_MAX_RANK];
 };
 
+// Operand slices of a split-precision contraction kept for reuse: the bf16
+// digit slices and row exponents of one operand (src) under one plan and
+// padding.  Used only while an entry point knows that operand is constant
+// (the environments L and R during one Davidson solve).
+struct SliceCache {
+  const double* src = nullptr;
+  const void* plan = nullptr;
+  int64_t rows_pad = 0, kpad = 0;
+  bool valid = false;
+  void* buf = nullptr;
+  size_t bytes = 0;
+};
+
 struct itg_handle {
   int device = 0;
   int num_sms = 0;
@@ -101,6 +114,11 @@ struct itg_handle {
   size_t cplx_buf_bytes = 0;
   int64_t* tab_buf = nullptr; // offset tables of the blocked QR's submatrix products
   int64_t tab_buf_elems = 0;
+  // Split operand slice reuse: [0] the A operand, [1] the B operand of the
+  // next split contraction when slice_keep[i] is set (see SliceCache).
+  SliceCache slice_cache[2];
+  bool slice_keep[2] = {false, false};
+  bool heff_keep_env_slices = false;  // set by Davidson for the duration of one solve
   int last_sweeps = 0;        // Jacobi sweeps of the last SVD / eigh call
   bool last_mixed = false;    // the last SVD finished on the mixed method
   int64_t svd_fallbacks = 0;  // mixed SVDs redone with FP64 Jacobi

@@ -823,47 +823,13 @@ __global__ void k_row_expfield_mmajor(const double* __restrict__ X, const int64_
   if (e) atomicMax(&efield[r], e);
 }
 
-// Balanced base-2^7 digits of X[r,k] * 2^-e_r rounded to 7S fractional bits.
-template <int S>
-__device__ __forceinline__ void make_digits(double x, int efield_r, int (&d)[S]) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-  const bool neg = bits >> 63;
-  const int E = (int)((bits >> 52) & 0x7FF);
-  unsigned long long M = bits & ((1ull << 52) - 1);
-  if (E) M |= 1ull << 52;
-  const int Ee = E ? E : 1;
-  const int er = efield_r - 1022;
-  const int sh = Ee - 1075 - er + 7 * S;
-  unsigned long long Y;
-  if (M == 0 || E == 2047) {
-    Y = 0;
-  } else if (sh >= 0) {
-    Y = M << sh;
-  } else if (sh <= -60) {
-    Y = 0;
-  } else {
-    Y = (M >> (-sh)) + ((M >> (-sh - 1)) & 1ull);
-  }
-#pragma unroll
-  for (int p = S - 1; p >= 1; --p) {
-    int lo = (int)(Y & 127ull);
-    if (lo >= 64) lo -= 128;
-    d[p] = lo;
-    Y = (Y - (unsigned long long)(long long)lo) >> 7;
-  }
-  d[0] = (int)Y;
-  if (neg) {
-#pragma unroll
-    for (int p = 0; p < S; ++p) d[p] = -d[p];
-  }
-}
-
-// make_digits for S = 7 with 32-bit integer work: the same balanced digits,
-// returned as magnitudes-with-sign-applied-later: d (as make_digits gives for
-// |x|) and neg.  Y (at most 49 bits) splits into 28 + 21 bits whose 7-bit
-// fields are the unbalanced digits u_p; the balanced ones follow by one carry
-// pass from the least significant digit (v = u_p + carry, v >= 64 -> v - 128
-// with carry 1), which is what make_digits' repeated (Y - d) >> 7 computes.
+// Balanced base-2^7 digits of |X[r,k]| * 2^-e_r rounded to 49 fractional bits
+// (S = 7 digits), and the sign of X[r,k]; the digits of X are the digits of
+// |X| negated.  Y = |X| 2^(49 - e_r) (at most 2^49) splits into 28 + 21 bits
+// whose 7-bit fields are the unbalanced digits u_p; one carry pass from the
+// least significant digit makes them balanced (v = u_p + carry; v >= 64 ->
+// digit v - 128, carry 1), so |d_0| <= 128 and |d_p| <= 64 for p >= 1, all
+// exact in bf16.
 __device__ __forceinline__ void make_digits7_abs(double x, int efield_r, int (&d)[7], bool& neg) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   neg = (bits >> 63) != 0;
@@ -955,7 +921,8 @@ __device__ __forceinline__ void store_digit_chunk(uint8_t* tile, int i, int p, i
 
 // The 7 digits of 8 elements (x[c0 .. c0 + 7], row exponent field ef) into the
 // 7 slices' chunks of row i.  A negative element's digits are the negated
-// digits of its magnitude (bf16 sign bit), as make_digits forms them.
+// digits of its magnitude (bf16 sign bit; a zero digit may so become -0,
+// which changes no product or sum).
 __device__ __forceinline__ void digits8(uint8_t* tiles, int tile_bytes, int i, int c0, const double* x, int ef) {
   constexpr int S = S_SLICES;
   int dg[S][8];
@@ -1163,18 +1130,32 @@ k_make_slices(const double* __restrict__ X, const int64_t* __restrict__ offR,
     }
   }
   __syncthreads();
-  const int kk = t & 63;
-  const size_t plane = (size_t)Rpad * Kpad;
+  // each thread: 8 consecutive k of one row -> one 16-byte store per slice
+  static_assert(S == S_SLICES, "digit routine is written for 7 slices");
+  const int rr = t >> 3, kc = t & 7;
+  const int64_t r = r0 + rr;
+  const int ef = (r < R) ? efield[r] : 0;
+  int dg[S][8];
+  uint32_t sgn[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int rr = (t >> 6) + 4 * i;
-    const int64_t r = r0 + rr;
+  for (int e = 0; e < 8; ++e) {
     int d[S];
-    const int ef = (r < R) ? efield[r] : 0;
-    make_digits<S>(tile[rr][kk], ef, d);
-    const size_t o = (size_t)r * Kpad + k0 + kk;
+    bool neg;
+    make_digits7_abs(tile[rr][kc * 8 + e], ef, d, neg);
+    if (neg) sgn[e >> 1] |= (e & 1) ? 0x80000000u : 0x00008000u;
 #pragma unroll
-    for (int p = 0; p < S; ++p) out[(size_t)p * plane + o] = __float2bfloat16_rn((float)d[p]);
+    for (int p = 0; p < S; ++p) dg[p][e] = d[p];
+  }
+  const size_t plane = (size_t)Rpad * Kpad;
+  const size_t o = (size_t)r * Kpad + k0 + kc * 8;
+#pragma unroll
+  for (int p = 0; p < S; ++p) {
+    uint4 v;
+    v.x = pack_bf16x2(dg[p][0], dg[p][1]) ^ sgn[0];
+    v.y = pack_bf16x2(dg[p][2], dg[p][3]) ^ sgn[1];
+    v.z = pack_bf16x2(dg[p][4], dg[p][5]) ^ sgn[2];
+    v.w = pack_bf16x2(dg[p][6], dg[p][7]) ^ sgn[3];
+    *(uint4*)(out + (size_t)p * plane + o) = v;
   }
 }
 
@@ -1269,10 +1250,44 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   const int64_t q = nct / G, r = nct % G;
   const bool shares = r != 0;  // the tail tiles are split between CTAs
   const size_t tile_bytes = sizeof(long long) * (size_t)BN * BM;
+  // operands whose slices are kept (SliceCache): reuse on a match, else fill
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  ITG_CUDA(h, cudaStreamIsCapturing(h->stream, &cap));
+  SliceCache* cache[2] = {nullptr, nullptr};
+  bool hit[2] = {false, false};
+  const double* srcs[2] = {A, B};
+  const int64_t rpads[2] = {Mpad, Npad};
+  for (int i = 0; i < 2; ++i) {
+    if (!h->slice_keep[i]) continue;
+    SliceCache& c = h->slice_cache[i];
+    hit[i] = c.valid && c.src == srcs[i] && c.plan == (const void*)&p && c.rows_pad == rpads[i] && c.kpad == Kpad;
+    if (hit[i]) {
+      cache[i] = &c;
+      continue;
+    }
+    if (cap != cudaStreamCaptureStatusNone) continue;  // no allocation inside a capture: plain path
+    const size_t need = itg_align256(sizeof(int) * rpads[i]) + (size_t)2 * S * rpads[i] * Kpad;
+    if (c.bytes < need) {
+      ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+      if (c.buf) cudaFree(c.buf);
+      c.buf = nullptr;
+      c.bytes = 0;
+      c.valid = false;
+      if (cudaMalloc(&c.buf, need) != cudaSuccess) {
+        (void)cudaGetLastError();
+        c.buf = nullptr;
+        continue;  // no room to keep them: plain path
+      }
+      c.bytes = need;
+    }
+    c.valid = false;
+    cache[i] = &c;
+  }
   size_t off = 0;
   auto take = [&](size_t b) { size_t o = off; off += itg_align256(b); return o; };
-  const size_t oEA = take(sizeof(int) * Mpad), oEB = take(sizeof(int) * Npad);
-  const size_t oSA = take((size_t)2 * S * Mpad * Kpad), oSB = take((size_t)2 * S * Npad * Kpad);
+  const size_t oEA = take(cache[0] ? 0 : sizeof(int) * Mpad), oEB = take(cache[1] ? 0 : sizeof(int) * Npad);
+  const size_t oSA = take(cache[0] ? 0 : (size_t)2 * S * Mpad * Kpad);
+  const size_t oSB = take(cache[1] ? 0 : (size_t)2 * S * Npad * Kpad);
   const size_t oAcc = take(Smem<BN>::TACC ? 0 : tile_bytes * (size_t)grid);
   const size_t oTacc = take(shares ? tile_bytes * (size_t)grid : 0);
   const size_t oCnt = take(shares ? sizeof(int) * (size_t)grid : 0);
@@ -1283,6 +1298,14 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   int* eB = (int*)(ws + oEB);
   __nv_bfloat16* sA = (__nv_bfloat16*)(ws + oSA);
   __nv_bfloat16* sB = (__nv_bfloat16*)(ws + oSB);
+  if (cache[0]) {
+    eA = (int*)cache[0]->buf;
+    sA = (__nv_bfloat16*)((char*)cache[0]->buf + itg_align256(sizeof(int) * Mpad));
+  }
+  if (cache[1]) {
+    eB = (int*)cache[1]->buf;
+    sB = (__nv_bfloat16*)((char*)cache[1]->buf + itg_align256(sizeof(int) * Npad));
+  }
   long long* acc = (long long*)(ws + oAcc);
   long long* tacc = (long long*)(ws + oTacc);
   int* cnt = (int*)(ws + oCnt);
@@ -1310,8 +1333,8 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
       }
       return ITG_OK;
     };
-    ITG_TRY(expo(p.a_kmaj, A, p.offAm(), p.offAk(), p.M, eA));
-    ITG_TRY(expo(p.b_kmaj, B, p.offBn(), p.offBk(), p.N, eB));
+    if (!hit[0]) ITG_TRY(expo(p.a_kmaj, A, p.offAm(), p.offAk(), p.M, eA));
+    if (!hit[1]) ITG_TRY(expo(p.b_kmaj, B, p.offBn(), p.offBk(), p.N, eB));
     ITG_CHECK_LAUNCH(h);
   }
   // slices
@@ -1319,15 +1342,27 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
     ProfScope prof(h, ITG_KERNEL_SPLIT_PREP);
     dim3 gA((unsigned)(Kpad / 64), (unsigned)(Mpad / 32)), gB((unsigned)(Kpad / 64), (unsigned)(Npad / 32));
     if (gA.y > 65535 || gB.y > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: too many rows");
-    if (p.a_kmaj)
-      k_make_slices<true, S><<<gA, 256, 0, h->stream>>>(A, p.offAm(), p.offAk(), p.M, p.K, Mpad, Kpad, eA, sA);
-    else
-      k_make_slices<false, S><<<gA, 256, 0, h->stream>>>(A, p.offAm(), p.offAk(), p.M, p.K, Mpad, Kpad, eA, sA);
-    if (p.b_kmaj)
-      k_make_slices<true, S><<<gB, 256, 0, h->stream>>>(B, p.offBn(), p.offBk(), p.N, p.K, Npad, Kpad, eB, sB);
-    else
-      k_make_slices<false, S><<<gB, 256, 0, h->stream>>>(B, p.offBn(), p.offBk(), p.N, p.K, Npad, Kpad, eB, sB);
+    if (!hit[0]) {
+      if (p.a_kmaj)
+        k_make_slices<true, S><<<gA, 256, 0, h->stream>>>(A, p.offAm(), p.offAk(), p.M, p.K, Mpad, Kpad, eA, sA);
+      else
+        k_make_slices<false, S><<<gA, 256, 0, h->stream>>>(A, p.offAm(), p.offAk(), p.M, p.K, Mpad, Kpad, eA, sA);
+    }
+    if (!hit[1]) {
+      if (p.b_kmaj)
+        k_make_slices<true, S><<<gB, 256, 0, h->stream>>>(B, p.offBn(), p.offBk(), p.N, p.K, Npad, Kpad, eB, sB);
+      else
+        k_make_slices<false, S><<<gB, 256, 0, h->stream>>>(B, p.offBn(), p.offBk(), p.N, p.K, Npad, Kpad, eB, sB);
+    }
     ITG_CHECK_LAUNCH(h);
+  }
+  for (int i = 0; i < 2; ++i) {
+    if (!cache[i] || hit[i]) continue;
+    cache[i]->src = srcs[i];
+    cache[i]->plan = (const void*)&p;
+    cache[i]->rows_pad = rpads[i];
+    cache[i]->kpad = Kpad;
+    cache[i]->valid = true;
   }
   CUtensorMap mA, mB;
   ITG_TRY(make_map(h, &mA, sA, Kpad, Mpad * S, BM));
