@@ -722,7 +722,7 @@ def run_svd(args):
     Cm = torch.empty(n * n, dtype=torch.float64, device="cuda")
     k = C.c_int64()
     prec = 1 if args.svd_method == 2 else 0
-    h.call("itg_set_svd_options", int(args.svd_qr), 0)
+    h.call("itg_set_svd_options", int(args.svd_qr), int(args.svd_jacobi_mode))
 
     converged = [True]
 
@@ -930,6 +930,8 @@ def main():
     ap.add_argument("--svd-method", type=int, default=2, choices=[1, 2])
     ap.add_argument("--svd-qr", type=int, default=1, choices=[0, 1], help="Householder QR preconditioning")
     ap.add_argument("--svd-reps", type=int, default=1, help="timed factorisations (after one warm-up if > 1)")
+    ap.add_argument("--svd-jacobi-mode", type=int, default=0, choices=[0, 1, 2],
+                    help="itg_set_svd_options jacobi_mode")
     ap.add_argument("--sweep-n", type=int, default=24,
                     help="chain length of the sweep measurement in the default run (0: skip)")
     ap.add_argument("--batch-count", type=int, default=256)

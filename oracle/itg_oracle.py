@@ -524,11 +524,17 @@ def random_mps(dims_site, linkdim, seed):
 
 # ------------------------------------------------------------------ DMRG
 def _env_left(L, A, W):
-    return np.einsum("awc,asb,wtsx,ctd->bxd", L, A, W, A, optimize=True)
+    """L'[b, x, d] = sum L[a, w, c] A[a, s, b] W[w, t, s, x] A[c, t, d] (pairwise BLAS products)."""
+    t = np.tensordot(L, A, axes=([0], [0]))                  # (w, c, s, b)
+    t = np.tensordot(t, W, axes=([0, 2], [0, 2]))            # (c, b, t, x)
+    return np.tensordot(t, A, axes=([0, 2], [0, 1]))         # (b, x, d)
 
 
 def _env_right(R, A, W):
-    return np.einsum("asb,wtsx,bxd,ctd->awc", A, W, R, A, optimize=True)
+    """R'[a, w, c] = sum A[a, s, b] W[w, t, s, x] R[b, x, d] A[c, t, d] (pairwise BLAS products)."""
+    t = np.tensordot(A, R, axes=([2], [0]))                  # (a, s, x, d)
+    t = np.tensordot(t, W, axes=([1, 2], [2, 3]))            # (a, d, w, t)
+    return np.tensordot(t, A, axes=([1, 3], [2, 1]))         # (a, w, c)
 
 
 def _noise_split(M, phi, L, W1, W2, R, ha, noise, maxdim, mindim, cutoff, legacy):

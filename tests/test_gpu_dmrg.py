@@ -178,6 +178,28 @@ def test_dmrg_heisenberg_n20_matches_oracle_and_ed(gpu):
         assert abs(rec.energy - eo) < 1e-6
 
 
+@pytest.mark.parametrize("form", ["chosen", "plain"])
+def test_dmrg_heisenberg_n100_matches_oracle_fixture(gpu, form):
+    """The N = 100 Heisenberg workload (random MPS of link dimension 16, Philox
+    seed 1236; 10 sweeps with maxdim 16 -> 1024, cutoff 1e-12) in the chosen form
+    (split-precision contractions, mixed SVD) and the plain form (FP64
+    contractions, FP64 Jacobi SVD): final energy within 1e-10 of the oracle's
+    FP64 run of the same workload (tests/golden/config3_oracle.json, made by
+    tests/golden/make_config3_energy.py)."""
+    fix = json.loads((Path(__file__).parent / "golden" / "config3_oracle.json").read_text())
+    N = fix["N"]
+    sites = gpu.siteinds("S=1/2", N)
+    H = gpu.cuMPO(gpu.heisenberg_mpo(sites))
+    psi0 = gpu.randomCuMPS(sites, fix["linkdim"], seed=fix["seed"])
+    sw = gpu.Sweeps(fix["nsweep"], maxdim=fix["maxdims"], cutoff=[fix["cutoff"]])
+    prec, svd = ("split", 2) if form == "chosen" else ("fp64", 1)
+    res = gpu.dmrg(H, psi0, sw, precision=prec, svd_method=svd, return_result=True)
+    assert abs(res.energy - fix["energy"]) < 1e-10, (form, res.energy, fix["energy"])
+    # the sweeps follow the oracle's convergence once maxdim stops binding
+    for rec, eo in list(zip(res.sweeps, fix["sweep_energies"]))[5:]:
+        assert abs(rec.energy - eo) < 1e-9, (rec.energy, eo)
+
+
 def test_dmrg_heisenberg_n12_exact(gpu):
     """No truncation needed at N=12: the energy must reach ED at 1e-10."""
     N = 12
