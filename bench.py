@@ -14,6 +14,12 @@ Printed JSON line (one, from rank 0):
   roofline  dominant kernel (the chi^3 contraction kernel) against its bound
   cpu_baseline  the oracle's NumPy/OpenBLAS matvec on the host cores
   clocks    nvidia-smi SM clocks sampled during the timed region
+  sweep     one DMRG sweep at chi = 1024 on the N = 100 Heisenberg chain (random
+            MPS of link dimension 1024, cutoff 0), chosen vs plain form, with
+            phase times (eigensolver, factorisation, environments)
+  vs_oracle the chosen form on the N = 100 Heisenberg workload (10 sweeps,
+            maxdim 16 -> 1024, cutoff 1e-12): per-sweep |dE| against the FP64
+            oracle's run of the same workload (tests/golden/config3_oracle.json)
 
 --impl reference times the reference's CPU path for the same matvec: the
 reference (ITensorsGPU.jl, Julia) cannot run here, so this is the oracle's
@@ -337,10 +343,14 @@ def run_gpu(args):
     e2e_value = flop_step / e2e_s / 1e12
     finite = bool(torch.isfinite(chosen["out"]).all().item())
 
-    # ---- one DMRG sweep at bond dimension chi, chosen vs plain (rank 0, N=1)
+    # ---- one DMRG sweep at bond dimension chi, chosen vs plain (rank 0, N=1),
+    # and the N = 100 cutoff-1e-12 run of the chosen form against the FP64 oracle
     sweep = None
     if args.sweep_n > 0 and world == 1:
         sweep = measure_sweeps(args.sweep_n, chi, 1, 0.0)
+    conv = None
+    if args.config3 and world == 1:
+        conv = measure_vs_oracle()
     if rank != 0:
         return 0
     cpu = None
@@ -358,7 +368,9 @@ def run_gpu(args):
                        l2="flushed (256 MB write) between timed steps"),
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_s * 1e3},
-        "gpu_launches": (11 if chosen_prec == PREC_SPLIT else 4) * chosen["steps"],
+        # per split matvec: Weff, 2 x (2 exponent + 2 slice kernels + the GEMM), the
+        # tensor-core middle step; per FP64 matvec: Weff, GEMM, middle step, GEMM
+        "gpu_launches": (12 if chosen_prec == PREC_SPLIT else 4) * chosen["steps"],
         "roofline": chosen["roofline"],
         "cpu_baseline": cpu,
         "clocks": chosen["clocks"],
@@ -373,6 +385,8 @@ def run_gpu(args):
         line["split_vs_fp64_rel_frobenius"] = accuracy
     if sweep is not None:
         line["sweep"] = sweep
+    if conv is not None:
+        line["vs_oracle"] = conv
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -380,6 +394,31 @@ def run_gpu(args):
 
 
 # ------------------------------------------------------ DMRG sweep workload
+def measure_vs_oracle():
+    """The chosen form (split contractions, mixed SVD) on the N = 100 Heisenberg
+    workload the FP64 oracle ran for tests/golden/config3_oracle.json (random MPS
+    of link dimension 16, Philox seed 1236, 10 sweeps with maxdim 16 -> 1024,
+    cutoff 1e-12): per-sweep energies, |dE| against the oracle's, wall time."""
+    import torch
+    import itg
+    fix = json.loads((REPO / "tests" / "golden" / "config3_oracle.json").read_text())
+    sites = itg.siteinds("S=1/2", fix["N"])
+    H = itg.cuMPO(itg.heisenberg_mpo(sites))
+    psi0 = itg.randomCuMPS(sites, fix["linkdim"], seed=fix["seed"])
+    sw = itg.Sweeps(fix["nsweep"], maxdim=fix["maxdims"], cutoff=[fix["cutoff"]])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = itg.dmrg(H, psi0, sw, precision="split", svd_method=2, phase_timing=True, return_result=True)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    de = [abs(r.energy - eo) for r, eo in zip(res.sweeps, fix["sweep_energies"])]
+    return {"workload": "Heisenberg N=100, link 16 (seed 1236), 10 sweeps maxdim 16->1024, cutoff 1e-12",
+            "form": "chosen (split contractions, mixed SVD)", "seconds": el,
+            "energy": res.energy, "oracle_energy": fix["energy"], "abs_dE": abs(res.energy - fix["energy"]),
+            "per_sweep_abs_dE": de, "maxlinkdim": res.sweeps[-1].maxlinkdim,
+            "oracle": "NumPy FP64 restatement (oracle/itg_oracle.py), tests/golden/config3_oracle.json"}
+
+
 def measure_sweeps(N, chi, nsweep, cutoff, seed=1236, init_linkdim=None, maxdims=None):
     """One DMRG run per form from the same initial state; per-sweep times and phases.
 
@@ -932,7 +971,9 @@ def main():
     ap.add_argument("--svd-reps", type=int, default=1, help="timed factorisations (after one warm-up if > 1)")
     ap.add_argument("--svd-jacobi-mode", type=int, default=0, choices=[0, 1, 2],
                     help="itg_set_svd_options jacobi_mode")
-    ap.add_argument("--sweep-n", type=int, default=24,
+    ap.add_argument("--config3", type=int, default=1, choices=[0, 1],
+                    help="run the N=100 cutoff-1e-12 chosen-form DMRG against the FP64 oracle's energies")
+    ap.add_argument("--sweep-n", type=int, default=100,
                     help="chain length of the sweep measurement in the default run (0: skip)")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-n", type=int, default=32)
