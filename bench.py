@@ -701,11 +701,12 @@ def run_ops(args):
     del T, Out
     # SVD microbench
     nn = 2048
-    g = torch.Generator(device="cuda").manual_seed(1234 + 2)
-    Q1, _ = torch.linalg.qr(torch.randn(nn, nn, dtype=torch.float64, device="cuda", generator=g))
-    Q2, _ = torch.linalg.qr(torch.randn(nn, nn, dtype=torch.float64, device="cuda", generator=g))
-    sv = torch.exp(-torch.arange(nn, dtype=torch.float64, device="cuda") / 20.0)
-    M = ((Q1 * sv) @ Q2.T).T.contiguous().reshape(-1)
+    import numpy as np
+    rng = np.random.default_rng(1234 + 2)
+    Q1, _ = np.linalg.qr(rng.standard_normal((nn, nn)))   # Haar orthogonal (host LAPACK)
+    Q2, _ = np.linalg.qr(rng.standard_normal((nn, nn)))
+    sv = np.exp(-np.arange(nn) / 20.0)
+    M = torch.from_numpy(np.ascontiguousarray(((Q1 * sv) @ Q2.T).T).reshape(-1)).cuda()
     U = torch.empty(nn * nn, dtype=torch.float64, device="cuda")
     S = torch.empty(nn, dtype=torch.float64, device="cuda")
     V = torch.empty_like(U)
