@@ -705,8 +705,9 @@ def run_ops(args):
     rng = np.random.default_rng(1234 + 2)
     Q1, _ = np.linalg.qr(rng.standard_normal((nn, nn)))   # Haar orthogonal (host LAPACK)
     Q2, _ = np.linalg.qr(rng.standard_normal((nn, nn)))
-    sv = np.exp(-np.arange(nn) / 20.0)
-    M = torch.from_numpy(np.ascontiguousarray(((Q1 * sv) @ Q2.T).T).reshape(-1)).cuda()
+    svh = np.exp(-np.arange(nn) / 20.0)
+    M = torch.from_numpy(np.ascontiguousarray(((Q1 * svh) @ Q2.T).T).reshape(-1)).cuda()
+    sv = torch.from_numpy(svh).cuda()
     U = torch.empty(nn * nn, dtype=torch.float64, device="cuda")
     S = torch.empty(nn, dtype=torch.float64, device="cuda")
     V = torch.empty_like(U)

@@ -266,6 +266,85 @@ def _orthogonalize_left_end(h, ch: _Chain):
     h.call("itg_scal", C.c_int64(ch.A[0].numel()), C.c_double(1.0 / nrm.value), _ptr(ch.A[0]))
 
 
+def _dmrg_complex(H: MPO, psi0: MPS, sweeps: Sweeps, krylovdim: int, maxiter: int, eigsolve_tol: float,
+                  precision: int, outputlevel: int):
+    """Two-site DMRG on ComplexF64 tensors, at the ITensor level of the library.
+
+    ITensors' algorithm step by step (the projected environments as ITensors,
+    the ProjMPO product as four contractions L * phi * W1 * W2 * R, the
+    eigensolver davidson on that map, the bond split by replacebond! through
+    the complex SVD), every operation on the device through libitg.so's complex
+    entry points (itg_contract_z, itg_svd_trunc_z, itg_qr_z).  Used when the MPO
+    or the MPS has complex tensors; the real path is the fused one above.
+    """
+    from . import mpsops
+    from .solvers import davidson
+    N = len(psi0)
+    psi = psi0.copy()
+    for j in range(N):
+        if not psi[j].is_complex:
+            psi[j] = T.complex_(psi[j])
+    W = [H[j] if H[j].is_complex else T.complex_(H[j]) for j in range(N)]
+    mpsops.orthogonalize_(psi, 0)
+    prec = int(precision)
+
+    def ctr(a, b):
+        return T.contract(a, b, precision=prec)
+
+    def edge(ket_link, w_link):
+        t = T.cuITensor(np.ones((1, 1, 1), dtype=np.complex128), ket_link, w_link, ket_link.prime())
+        return t
+
+    Lenv = [None] * (N + 1)
+    Renv = [None] * (N + 1)
+    Lenv[0] = edge(psi[0].inds[0], W[0].inds[0])
+    Renv[N] = edge(psi[N - 1].inds[2], W[N - 1].inds[3])
+
+    def ext_right(R, A, Wj):   # R_{j} from R_{j+1}: sites j..N-1
+        return ctr(ctr(ctr(R, A), Wj), T.dag(T.prime(A)))
+
+    def ext_left(L, A, Wj):
+        return ctr(ctr(ctr(L, A), Wj), T.dag(T.prime(A)))
+
+    for j in range(N - 1, 1, -1):
+        Renv[j] = ext_right(Renv[j + 1], psi[j], W[j])
+    energy = 0.0
+    records = []
+    for sw in range(sweeps.nsweep):
+        t0 = time.perf_counter()
+        maxdim, mindim, cutoff = sweeps.maxdim(sw), sweeps.mindim(sw), sweeps.cutoff(sw)
+        maxerr = 0.0
+        nmv = 0
+        for b, ha in sweepnext(N):
+            phi = ctr(psi[b], psi[b + 1])
+            L, R, W1, W2 = Lenv[b], Renv[b + 2], W[b], W[b + 1]
+
+            def heff(x):
+                nonlocal nmv
+                nmv += 1
+                y = ctr(ctr(ctr(ctr(L, x), W1), W2), R)
+                y = y.replaceinds(y.inds, [i.noprime() if i.plev > 0 else i for i in y.inds])
+                return T.permute(y, *x.inds)
+
+            energy, phi = davidson(heff, phi, maxiter=max(1, krylovdim * maxiter), tol=eigsolve_tol,
+                                   restart_dim=max(2, krylovdim + 1))
+            energy = float(np.real(energy))
+            spec = mpsops.replacebond_(psi, b, phi, ortho="left" if ha == 1 else "right", maxdim=maxdim,
+                                       mindim=mindim, cutoff=cutoff)
+            maxerr = max(maxerr, float(spec.truncerr))
+            if ha == 1:
+                Lenv[b + 1] = ext_left(L, psi[b], W1)
+            else:
+                Renv[b + 1] = ext_right(R, psi[b + 1], W2)
+        T._h().call("itg_synchronize")
+        rec = SweepRecord(energy, psi.maxlinkdim(), maxerr, time.perf_counter() - t0, nmv)
+        records.append(rec)
+        if outputlevel > 0:
+            print(f"After sweep {sw + 1} energy={energy:.14f} maxlinkdim={rec.maxlinkdim} "
+                  f"maxerr={rec.maxtruncerr:.2e} time={rec.seconds:.3f}", flush=True)
+    return energy, psi, records
+
+
 def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int = 2,
          eigsolve_tol: float = 1e-14, precision: str | int = "fp64", legacy_gpu_truncate: bool = False,
          svd_method: int = 0, preconditioner=None, bond_hook=None, phase_timing: bool = False,
@@ -297,6 +376,14 @@ def dmrg(H: MPO, psi0: MPS, sweeps: Sweeps, *, krylovdim: int = 3, maxiter: int 
         raise ValueError("dmrg needs at least two sites")
     psi0 = T.cu(psi0)
     H = T.cu(H)
+    if any(t.is_complex for t in list(psi0.tensors) + list(H.tensors)):
+        if preconditioner is not None or bond_hook is not None or any(sweeps.noise(s) > 0 for s in range(sweeps.nsweep)):
+            raise ValueError("dmrg on complex tensors: no learned preconditioner, bond hook or noise term")
+        energy, psi, records = _dmrg_complex(H, psi0, sweeps, krylovdim, maxiter, eigsolve_tol, precision,
+                                             outputlevel)
+        if return_result:
+            return DMRGResult(energy, psi, records)
+        return energy, psi
     ch = _Chain(psi0.copy(), H)
     _orthogonalize_left_end(h, ch)
     one = T.empty_dev(1).fill_(1.0)

@@ -200,6 +200,45 @@ def test_dmrg_heisenberg_n100_matches_oracle_fixture(gpu, form):
         assert abs(rec.energy - eo) < 1e-9, (rec.energy, eo)
 
 
+def _rotated_heisenberg(gpu, sites, seed):
+    """U H U^dagger for the S=1/2 Heisenberg MPO and random single-site unitaries
+    u_j: complex Hermitian site operators, the spectrum of H unchanged."""
+    from itg.mps import MPO
+    rng = np.random.default_rng(seed)
+    H = gpu.heisenberg_mpo(sites)
+    out = []
+    for j, t in enumerate(H.tensors):
+        z = rng.standard_normal((2, 2)) + 1j * rng.standard_normal((2, 2))
+        u, _ = np.linalg.qr(z)
+        W = t.array()                                   # (wl, s', s, wr)
+        Wr = np.einsum("ap,wpqx,bq->wabx", u, W, u.conj())
+        out.append(gpu.ITensor_host(Wr, *t.inds))
+    return MPO(out, sites)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("split", 1e-9)])
+def test_dmrg_complex_rotated_heisenberg_matches_ed(gpu, precision, tol):
+    """A complex DMRG sweep (ComplexF64 MPO and MPS: ITensors' algorithm on the
+    library's complex contraction, SVD and QR entry points): the Heisenberg
+    chain N = 12 rotated by random single-site unitaries has complex matrix
+    elements and the spectrum of the real chain, so the ground energy must be
+    the exact-diagonalisation value."""
+    N = 12
+    sites = gpu.siteinds("S=1/2", N)
+    H = gpu.cuMPO(_rotated_heisenberg(gpu, sites, seed=21))
+    assert all(t.is_complex for t in H.tensors)
+    psi0 = gpu.randomCuMPS(sites, 4, seed=8)
+    sw = gpu.Sweeps(8, maxdim=[8, 16, 32, 64], cutoff=[1e-14])
+    res = gpu.dmrg(H, psi0, sw, krylovdim=4, maxiter=3, eigsolve_tol=1e-13, precision=precision,
+                   return_result=True)
+    e_ed = GOLD["ed"]["heisenberg_N12"]
+    assert abs(res.energy - e_ed) < tol, (res.energy, e_ed)
+    assert all(t.is_complex for t in res.psi.tensors)
+    # the state is an eigenvector: <psi|H|psi> = E with <psi|psi> = 1
+    e_exp = gpu.inner(res.psi, H, res.psi)
+    assert abs(complex(e_exp) - res.energy) < 10 * tol
+
+
 def test_dmrg_heisenberg_n12_exact(gpu):
     """No truncation needed at N=12: the energy must reach ED at 1e-10."""
     N = 12
