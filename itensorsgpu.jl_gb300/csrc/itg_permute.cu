@@ -59,39 +59,49 @@ __global__ void k_perm_rows(const double* __restrict__ A, double* __restrict__ B
 }
 
 // Tiled transpose between A's mode 0 (size n0, stride 1 in A, stride s0B in B)
-// and A's mode q (size nq, stride sqA in A, stride 1 in B).
+// and A's mode q (size nq, stride sqA in A, stride 1 in B).  blockIdx.y walks
+// the batches (the other modes), so their offsets are decomposed once per
+// batch, and blockIdx.x the 32 x 32 tiles of one batch; the index arithmetic
+// inside a batch is 32-bit.
 #define TP 32
-__global__ void k_perm_transpose(const double* __restrict__ A, double* __restrict__ B,
-                                 const double* __restrict__ Bin, double alpha, double beta,
-                                 int64_t n0, int64_t nq, int64_t sqA, int64_t s0B,
-                                 int64_t nbatch, RestDesc rest) {
+__global__ void __launch_bounds__(256)
+k_perm_transpose(const double* __restrict__ A, double* __restrict__ B, const double* __restrict__ Bin,
+                 double alpha, double beta, int64_t n0, int64_t nq, int64_t sqA, int64_t s0B, int64_t nbatch,
+                 RestDesc rest) {
   __shared__ double tile[TP][TP + 1];
-  const int64_t t0 = (n0 + TP - 1) / TP, tq = (nq + TP - 1) / TP;
-  const int64_t ntiles = t0 * tq * nbatch;
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    int64_t b = t / (t0 * tq);
-    int64_t r = t - b * t0 * tq;
-    int64_t iq = r / t0, i0 = r - iq * t0;
+  const int t0 = (int)((n0 + TP - 1) / TP), tq = (int)((nq + TP - 1) / TP);
+  const int tiles = t0 * tq;
+  for (int64_t b = blockIdx.y; b < nbatch; b += gridDim.y) {
     int64_t oa, ob;
     rest_offsets(rest, b, oa, ob);
-    const int64_t base0 = i0 * TP, baseq = iq * TP;
-    // read: threadIdx.x runs along mode 0 (contiguous in A)
-    for (int y = threadIdx.y; y < TP; y += blockDim.y) {
-      int64_t i = base0 + threadIdx.x, k = baseq + y;
-      if (i < n0 && k < nq) tile[y][threadIdx.x] = A[oa + i + k * sqA];
-    }
-    __syncthreads();
-    // write: threadIdx.x runs along mode q (contiguous in B)
-    for (int y = threadIdx.y; y < TP; y += blockDim.y) {
-      int64_t k = baseq + threadIdx.x, i = base0 + y;
-      if (i < n0 && k < nq) {
-        int64_t o = ob + k + i * s0B;
-        double v = alpha * tile[threadIdx.x][y];
-        if (Bin) v = fma(beta, Bin[o], v);
-        B[o] = v;
+    for (int r = blockIdx.x; r < tiles; r += gridDim.x) {
+      const int iq = r / t0, i0 = r - iq * t0;
+      const int64_t base0 = (int64_t)i0 * TP, baseq = (int64_t)iq * TP;
+      // read: threadIdx.x runs along mode 0 (contiguous in A); all loads first
+      double v[TP / 8];
+#pragma unroll
+      for (int j = 0; j < TP / 8; ++j) {
+        const int y = threadIdx.y + 8 * j;
+        const int64_t i = base0 + threadIdx.x, k = baseq + y;
+        v[j] = (i < n0 && k < nq) ? A[oa + i + k * sqA] : 0.0;
       }
+#pragma unroll
+      for (int j = 0; j < TP / 8; ++j) tile[threadIdx.y + 8 * j][threadIdx.x] = v[j];
+      __syncthreads();
+      // write: threadIdx.x runs along mode q (contiguous in B)
+#pragma unroll
+      for (int j = 0; j < TP / 8; ++j) {
+        const int y = threadIdx.y + 8 * j;
+        const int64_t k = baseq + threadIdx.x, i = base0 + y;
+        if (i < n0 && k < nq) {
+          const int64_t o = ob + k + i * s0B;
+          double w = alpha * tile[threadIdx.x][y];
+          if (Bin) w = fma(beta, Bin[o], w);
+          B[o] = w;
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
@@ -188,11 +198,14 @@ static int permute_axpby(itg_handle* h, double alpha, const double* A, int rank,
     }
     int64_t n0 = d.dims[0], nq = d.dims[q];
     int64_t nbatch = total / (n0 * nq);
-    int64_t ntiles = ((n0 + TP - 1) / TP) * ((nq + TP - 1) / TP) * nbatch;
-    int blocks = (int)std::min<int64_t>(ntiles, (int64_t)h->num_sms * 32);
+    const int64_t tiles = ((n0 + TP - 1) / TP) * ((nq + TP - 1) / TP);
+    if (tiles > (int64_t)INT32_MAX) return itg_fail(h, ITG_ERR_UNSUPPORTED, "permute: transpose too large");
+    const int64_t want = (int64_t)h->num_sms * 32;  // resident CTAs
+    const int64_t gx = std::min<int64_t>(tiles, want);
+    const int64_t gy = std::min<int64_t>(std::min<int64_t>(nbatch, std::max<int64_t>(1, want / gx)), 65535);
     dim3 thr(TP, 8);
-    k_perm_transpose<<<blocks, thr, 0, h->stream>>>(A, B, bin, alpha, beta, n0, nq, d.strA[q],
-                                                    d.strB[0], nbatch, rest);
+    k_perm_transpose<<<dim3((unsigned)gx, (unsigned)gy), thr, 0, h->stream>>>(A, B, bin, alpha, beta, n0, nq,
+                                                                            d.strA[q], d.strB[0], nbatch, rest);
   }
   ITG_CHECK_LAUNCH(h);
   return ITG_OK;
