@@ -7,11 +7,12 @@
 // slices with exact low-precision accumulation as in Ootomo, Ozaki & Yokota,
 // "DGEMM on integer matrix multiplication unit", IJHPCA 2024):
 //
-//   Row m of A is scaled by 2^-e_m (|A[m,k]| < 2^e_m) and written in balanced
-//   base-2^7 digits:  A[m,k] ~ 2^e_m sum_{p<S} a_p[m,k] 2^-7(p+1)
-//   with |a_0| <= 128 and |a_p| <= 64 (p >= 1); every digit is an exact bf16.
-//   Column n of B likewise with exponent f_n and digits b_q.
-//   C[m,n] ~ 2^(e_m+f_n-14) sum_{L<S} 2^-7L sum_{p+q=L} (a_p b_q)[m,n].
+//   Row m of A is scaled by 2^-e_m (|A[m,k]| < 2^e_m) and written in S = 6
+//   balanced base-2^8 digits:  A[m,k] ~ 2^e_m sum_{p<S} a_p[m,k] 2^-8(p+1)
+//   with |a_0| <= 256 and |a_p| <= 128 (p >= 1); every digit is an exact bf16
+//   (8 significant bits).  Column n of B likewise with exponent f_n, digits b_q.
+//   C[m,n] ~ 2^(e_m+f_n-16) sum_{L<S} 2^-8L sum_{p+q=L} (a_p b_q)[m,n]:
+//   21 digit products for 48 bits of each operand.
 //
 // Each a_p b_q product is an integer GEMM run by tcgen05.mma (kind::f16, bf16
 // in, FP32 accumulate in TMEM).  Products of one level L are accumulated in a
@@ -51,7 +52,7 @@
 
 namespace split {
 
-constexpr int S_SLICES = 7;    // digits per operand (7 bits each)
+constexpr int S_SLICES = 6;    // digits per operand (8 bits each)
 constexpr int BM = 128;        // tile rows (TMEM lanes)
 constexpr int BK = 64;         // K per pipeline stage (128 bytes of bf16)
 constexpr int STAGES = 4;
@@ -220,8 +221,8 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// Digit magnitude bounds: 2^7 for the leading digit, 2^6 for the others.
-__host__ __device__ __forceinline__ int digit_log2(int p) { return p == 0 ? 7 : 6; }
+// Digit magnitude bounds: 2^8 for the leading digit, 2^7 for the others.
+__host__ __device__ __forceinline__ int digit_log2(int p) { return p == 0 ? 8 : 7; }
 
 // Exact-accumulation schedule shared by every role.  Items are
 // (level L, pair p, k-block kb) in level-major order; a group is a run of
@@ -591,9 +592,14 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
     // exact integers below 2^24 in magnitude; the groups of one level are
     // summed in int32 registers (exact for up to 127 groups) and only a level
     // end (or the 127th group) touches the int64 fixed-point accumulator.  The
-    // TMEM buffer goes back to the MMA issuer as soon as it has been read.
+    // TMEM buffer goes back to the MMA issuer as soon as it has been read,
+    // except at a level end of the global-accumulator variant: there the int32
+    // sums are parked in the drained buffer, which frees the registers for
+    // FLUSH_BATCH accumulator loads in flight at a time, and the buffer is
+    // handed back after the accumulator update.
     constexpr int NCOL = BN / 2;
     constexpr int NCH = NCOL / 32;
+    constexpr int FLUSH_BATCH = 32;
     const int quarter = warp & 3;
     const int col_lo = ((warp - 2) / 4) * NCOL;
     const int row = quarter * 32 + lane;
@@ -603,6 +609,8 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
     int ct, L0, Le;
     for (int si = 0; part.seg(gcl, si, tb, lb, te, le, ct, L0, Le); ++si) {
       int32_t sum[NCOL];
+#pragma unroll
+      for (int j = 0; j < NCOL; ++j) sum[j] = 0;
       int nsum = 0;
       bool have_acc = false, complete = false;
       Sched sc;
@@ -620,68 +628,86 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
         const bool ok_lane = mbar_wait(&acc_full[b], (lg >> 1) & 1, args.err, abort_flag, args.wait_ns);
         if (!__all_sync(0xffffffffu, ok_lane)) break;
         tc_fence_after();
+        const uint32_t tbuf = lane_base + (uint32_t)(b * BN + col_lo);
 #pragma unroll
         for (int c = 0; c < NCOL / 16; ++c) {
           uint32_t r[16];
-          tc_ld_32x32b_x16(lane_base + (uint32_t)(b * BN + col_lo + 16 * c), r);
+          tc_ld_32x32b_x16(tbuf + (uint32_t)(16 * c), r);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int32_t v = __float2int_rn(__uint_as_float(r[j]));
-            sum[16 * c + j] = nsum ? sum[16 * c + j] + v : v;
+          for (int j = 0; j < 16; ++j) sum[16 * c + j] += __float2int_rn(__uint_as_float(r[j]));
+        }
+        ++lg;
+        ++nsum;
+        const int sh = args.F - 8 * L;
+        if (!TACC && flush) {
+          // park the level's sums in the drained buffer, then update the
+          // global accumulator FLUSH_BATCH columns at a time
+#pragma unroll
+          for (int c = 0; c < NCOL / 16; ++c) {
+            uint32_t r[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) r[j] = (uint32_t)sum[16 * c + j];
+            tc_st_32x32b_x16(tbuf + (uint32_t)(16 * c), r);
+          }
+          tc_wait_st();
+#pragma unroll
+          for (int j = 0; j < NCOL; ++j) sum[j] = 0;
+          long long* ap = acc + (size_t)col_lo * BM + row;
+#pragma unroll 1
+          for (int c0 = 0; c0 < NCOL; c0 += FLUSH_BATCH) {
+            long long old[FLUSH_BATCH];
+#pragma unroll
+            for (int j = 0; j < FLUSH_BATCH; ++j) old[j] = have_acc ? ap[(size_t)(c0 + j) * BM] : 0ll;
+#pragma unroll
+            for (int h = 0; h < FLUSH_BATCH / 16; ++h) {
+              uint32_t r[16];
+              tc_ld_32x32b_x16(tbuf + (uint32_t)(c0 + 16 * h), r);
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                long long t = (long long)(int32_t)r[j];
+                t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
+                ap[(size_t)(c0 + 16 * h + j) * BM] = old[16 * h + j] + t;
+              }
+            }
           }
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&acc_empty[b]);
-        ++lg;
-        ++nsum;
-        if (flush) {
-          const int sh = args.F - 7 * L;
+        if (TACC && flush) {
 #pragma unroll
           for (int c = 0; c < NCH; ++c) {
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
               const int c0 = col_lo + 32 * c + 16 * h;
-              if (TACC) {
-                // int64 accumulator in TMEM: low words in columns 256 + c, high words in 384 + c
-                const uint32_t tlo = lane_base + 256u + (uint32_t)c0, thi = tlo + 128u;
-                uint32_t lo[16], hi[16];
-                if (have_acc) {
-                  tc_ld_32x32b_x16_nowait(tlo, lo);
-                  tc_ld_32x32b_x16_nowait(thi, hi);
-                  tc_wait_ld();
-                } else {
-#pragma unroll
-                  for (int j = 0; j < 16; ++j) lo[j] = hi[j] = 0u;
-                }
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                  long long t = (long long)sum[32 * c + 16 * h + j];
-                  t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
-                  const unsigned long long u = (((unsigned long long)hi[j] << 32) | lo[j]) + (unsigned long long)t;
-                  lo[j] = (uint32_t)(u & 0xFFFFFFFFull);
-                  hi[j] = (uint32_t)(u >> 32);
-                }
-                tc_st_32x32b_x16(tlo, lo);
-                tc_st_32x32b_x16(thi, hi);
+              // int64 accumulator in TMEM: low words in columns 256 + c, high words in 384 + c
+              const uint32_t tlo = lane_base + 256u + (uint32_t)c0, thi = tlo + 128u;
+              uint32_t lo[16], hi[16];
+              if (have_acc) {
+                tc_ld_32x32b_x16_nowait(tlo, lo);
+                tc_ld_32x32b_x16_nowait(thi, hi);
+                tc_wait_ld();
               } else {
-                long long* ap = acc + (size_t)c0 * BM + row;
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                  long long old[8];
-#pragma unroll
-                  for (int j = 0; j < 8; ++j) old[j] = have_acc ? ap[(size_t)(8 * q + j) * BM] : 0ll;
-#pragma unroll
-                  for (int j = 0; j < 8; ++j) {
-                    long long t = (long long)sum[32 * c + 16 * h + 8 * q + j];
-                    t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
-                    ap[(size_t)(8 * q + j) * BM] = old[j] + t;
-                  }
-                }
+                for (int j = 0; j < 16; ++j) lo[j] = hi[j] = 0u;
               }
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                long long t = (long long)sum[32 * c + 16 * h + j];
+                t = sh >= 0 ? (long long)((unsigned long long)t << sh) : (t >> (-sh));
+                const unsigned long long u = (((unsigned long long)hi[j] << 32) | lo[j]) + (unsigned long long)t;
+                lo[j] = (uint32_t)(u & 0xFFFFFFFFull);
+                hi[j] = (uint32_t)(u >> 32);
+              }
+              tc_st_32x32b_x16(tlo, lo);
+              tc_st_32x32b_x16(thi, hi);
             }
           }
-          if (TACC) tc_wait_st();
+          tc_wait_st();
+#pragma unroll
+          for (int j = 0; j < NCOL; ++j) sum[j] = 0;
+        }
+        if (flush) {
           nsum = 0;
           have_acc = true;
           complete = seg_last;
@@ -726,21 +752,31 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
         const int64_t m = (int64_t)m_grp * BM + row;
         const int64_t cm = m < args.M ? args.offCm[m] : 0;
         const int em = m < args.M ? args.eA[m] - 1022 : 0;
+        // FLUSH_BATCH accumulator values in flight at a time
 #pragma unroll 1
-        for (int c0 = col_lo; c0 < col_lo + NCOL; c0 += 16) {
-          long long v[16];
+        for (int c0 = col_lo; c0 < col_lo + NCOL; c0 += FLUSH_BATCH) {
+          long long v[FLUSH_BATCH];
           if (shared_tile) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) v[j] = __ldcg(tile_acc + (size_t)(c0 + j) * BM + row);
+            for (int j = 0; j < FLUSH_BATCH; ++j) v[j] = __ldcg(tile_acc + (size_t)(c0 + j) * BM + row);
+          } else if (TACC) {
+#pragma unroll
+            for (int h = 0; h < FLUSH_BATCH / 16; ++h) {
+              long long w[16];
+              load_acc16<TACC>(lane_base, acc, c0 + 16 * h, row, w);
+#pragma unroll
+              for (int j = 0; j < 16; ++j) v[16 * h + j] = w[j];
+            }
           } else {
-            load_acc16<TACC>(lane_base, acc, c0, row, v);
+#pragma unroll
+            for (int j = 0; j < FLUSH_BATCH; ++j) v[j] = acc[(size_t)(c0 + j) * BM + row];
           }
           if (m < args.M) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
+            for (int j = 0; j < FLUSH_BATCH; ++j) {
               const int64_t n = (int64_t)n0 + c0 + j;
               if (n >= args.N) continue;
-              double x = i64_to_double_scaled(v[j], em + args.eB[n] - 1022 - 14 - args.F);
+              double x = i64_to_double_scaled(v[j], em + args.eB[n] - 1022 - 16 - args.F);
               if (args.alpha != 1.0) x *= args.alpha;
               double* cp = args.C + cm + args.offCn[n];
               if (args.beta != 0.0) x = fma(args.beta, *cp, x);
@@ -823,21 +859,21 @@ __global__ void k_row_expfield_mmajor(const double* __restrict__ X, const int64_
   if (e) atomicMax(&efield[r], e);
 }
 
-// Balanced base-2^7 digits of |X[r,k]| * 2^-e_r rounded to 49 fractional bits
-// (S = 7 digits), and the sign of X[r,k]; the digits of X are the digits of
-// |X| negated.  Y = |X| 2^(49 - e_r) (at most 2^49) splits into 28 + 21 bits
-// whose 7-bit fields are the unbalanced digits u_p; one carry pass from the
-// least significant digit makes them balanced (v = u_p + carry; v >= 64 ->
-// digit v - 128, carry 1), so |d_0| <= 128 and |d_p| <= 64 for p >= 1, all
-// exact in bf16.
-__device__ __forceinline__ void make_digits7_abs(double x, int efield_r, int (&d)[7], bool& neg) {
+// Balanced base-2^8 digits of |X[r,k]| * 2^-e_r rounded to 48 fractional bits
+// (S = 6 digits), and the sign of X[r,k]; the digits of X are the digits of
+// |X| negated.  Y = |X| 2^(48 - e_r) (at most 2^48) splits into 24 + 24 bits
+// whose bytes are the unbalanced digits u_p; one carry pass from the least
+// significant digit makes them balanced (v = u_p + carry; v >= 128 -> digit
+// v - 256, carry 1), so |d_0| <= 256 and |d_p| <= 128 for p >= 1, all exact
+// in bf16.
+__device__ __forceinline__ void make_digits_abs(double x, int efield_r, int (&d)[S_SLICES], bool& neg) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   neg = (bits >> 63) != 0;
   const int E = (int)((bits >> 52) & 0x7FF);
   unsigned long long M = bits & ((1ull << 52) - 1);
   if (E) M |= 1ull << 52;
   const int Ee = E ? E : 1;
-  const int sh = Ee - 1075 - (efield_r - 1022) + 49;
+  const int sh = Ee - 1075 - (efield_r - 1022) + 48;
   unsigned long long Y;
   if (M == 0 || E == 2047) {
     Y = 0;
@@ -848,15 +884,14 @@ __device__ __forceinline__ void make_digits7_abs(double x, int efield_r, int (&d
   } else {
     Y = (M >> (-sh)) + ((M >> (-sh - 1)) & 1ull);
   }
-  const uint32_t lo = (uint32_t)Y & 0x0FFFFFFFu, hi = (uint32_t)(Y >> 28);
-  const uint32_t u[7] = {hi >> 14, (hi >> 7) & 127u, hi & 127u, lo >> 21, (lo >> 14) & 127u, (lo >> 7) & 127u,
-                         lo & 127u};
+  const uint32_t lo = (uint32_t)Y & 0x00FFFFFFu, hi = (uint32_t)(Y >> 24);
+  const uint32_t u[6] = {hi >> 16, (hi >> 8) & 255u, hi & 255u, lo >> 16, (lo >> 8) & 255u, lo & 255u};
   int c = 0;
 #pragma unroll
-  for (int p = 6; p >= 1; --p) {
+  for (int p = 5; p >= 1; --p) {
     const int v = (int)u[p] + c;
-    c = v >= 64;
-    d[p] = c ? v - 128 : v;
+    c = v >= 128;
+    d[p] = c ? v - 256 : v;
   }
   d[0] = (int)u[0] + c;
 }
@@ -867,13 +902,13 @@ __device__ __forceinline__ void make_digits7_abs(double x, int efield_r, int (&d
 // d^2 wR), by the same exact digit products as k_split_gemm.  Persistent CTAs
 // of 128 threads walk blocks of 128 rows.  Per block every thread loads its
 // row of T1 (coalesced across the CTA per c), forms the row exponent and the
-// 7 balanced digits of each element, and writes them K-major with the
+// 6 balanced digits of each element, and writes them K-major with the
 // 128-byte swizzle into shared memory, two slices per 128-byte row (slice p
 // at k offset 32 (p % 2) of tile p / 2); Weff's column digits are written the
-// same way once per CTA.  One thread issues the 28 digit products (one or two
-// K = 16 steps each) into seven TMEM level accumulators of NJP columns; one
-// group per level suffices because sum_{p+q=L} nc 2^(7+7) <= 7 * 32 * 2^14 <
-// 2^22 keeps every FP32 partial sum an exact integer.  Each thread then reads
+// same way once per CTA.  One thread issues the 21 digit products (one or two
+// K = 16 steps each) into six TMEM level accumulators of NJP columns; one
+// group per level suffices because sum_{p+q=L} nc |a_p| |b_q| <= 32 (2 * 2^15
+// + 4 * 2^14) = 2^22 keeps every FP32 partial sum an exact integer.  Each thread then reads
 // its row's level sums, forms the int64 fixed-point value and converts it to
 // FP64 with integer instructions: the same bits as k_split_gemm computes for
 // this product (same digits, same fixed point, same rounding).
@@ -881,7 +916,7 @@ constexpr int MID_ROWS = 128;
 constexpr int MID_THREADS = 128;
 constexpr int MID_KSLICE = 32;  // padded K per slice (nc <= 32)
 constexpr int MID_A_TILE = MID_ROWS * 128;     // bytes: 128 rows x 128 B (two slices)
-constexpr int MID_NTILE = (S_SLICES + 1) / 2;  // 4 tiles hold the 7 slices
+constexpr int MID_NTILE = (S_SLICES + 1) / 2;  // 3 tiles hold the 6 slices
 
 template <int NJP>
 struct MidSmem {
@@ -919,7 +954,7 @@ __device__ __forceinline__ void store_digit_chunk(uint8_t* tile, int i, int p, i
   *(uint4*)(tile + sw128_off(i, k)) = v;
 }
 
-// The 7 digits of 8 elements (x[c0 .. c0 + 7], row exponent field ef) into the
+// The 6 digits of 8 elements (x[c0 .. c0 + 7], row exponent field ef) into the
 // 7 slices' chunks of row i.  A negative element's digits are the negated
 // digits of its magnitude (bf16 sign bit; a zero digit may so become -0,
 // which changes no product or sum).
@@ -931,7 +966,7 @@ __device__ __forceinline__ void digits8(uint8_t* tiles, int tile_bytes, int i, i
   for (int e = 0; e < 8; ++e) {
     int d[S];
     bool neg;
-    make_digits7_abs(x[e], ef, d, neg);
+    make_digits_abs(x[e], ef, d, neg);
     if (neg) sgn[e >> 1] |= (e & 1) ? 0x80000000u : 0x00008000u;
 #pragma unroll
     for (int p = 0; p < S; ++p) dg[p][e] = d[p];
@@ -1007,7 +1042,7 @@ k_heff_mid_split(const double* __restrict__ T1, const double* __restrict__ Weff,
   const int ksteps = nc > 16 ? 2 : 1;
   int lk = 0;
   while ((1 << lk) < nc) ++lk;
-  const int F = 62 - 15 - lk;
+  const int F = 62 - 17 - lk;
   const int64_t nblk = (R + MID_ROWS - 1) / MID_ROWS;
   bool ok = true;
   uint32_t phase = 0;
@@ -1055,7 +1090,7 @@ k_heff_mid_split(const double* __restrict__ T1, const double* __restrict__ Weff,
       ok = false;
       break;
     }
-    // int64 fixed point: acc = sum_L s_L 2^(F - 7L) (F >= 42 here, so every
+    // int64 fixed point: acc = sum_L s_L 2^(F - 8L) (F >= 40 here, so every
     // shift is a left shift), by Horner over the levels and one final shift
     long long acc[NJP];
 #pragma unroll
@@ -1067,9 +1102,9 @@ k_heff_mid_split(const double* __restrict__ T1, const double* __restrict__ Weff,
           tc_ld_32x32b_x16(lane_base + (uint32_t)(L * NJP + 16 * h), v);
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            // exact integer below 2^22 in magnitude: float -> int by the 1.5 * 2^23 shift
+            // exact integer of magnitude <= 2^22: float -> int by the 1.5 * 2^23 shift
             const long long tv = (long long)(__float_as_int(__uint_as_float(v[j]) + 12582912.0f) - 0x4B400000);
-            acc[16 * h + j] = L == 0 ? tv : (long long)((unsigned long long)acc[16 * h + j] << 7) + tv;
+            acc[16 * h + j] = L == 0 ? tv : (long long)((unsigned long long)acc[16 * h + j] << 8) + tv;
           }
         }
       }
@@ -1079,8 +1114,8 @@ k_heff_mid_split(const double* __restrict__ T1, const double* __restrict__ Weff,
 #pragma unroll
       for (int j = 0; j < NJP; ++j)
         if (j < nj)
-          __stcs(T3 + r + R * j, i64_to_double_scaled((long long)((unsigned long long)acc[j] << (F - 42)),
-                                                      em + fB[j] - 1022 - 14 - F));
+          __stcs(T3 + r + R * j, i64_to_double_scaled((long long)((unsigned long long)acc[j] << (F - 40)),
+                                                      em + fB[j] - 1022 - 16 - F));
     }
     // the TMEM accumulators and the A tiles are reused by the next block
     tc_fence_before();
@@ -1131,7 +1166,7 @@ k_make_slices(const double* __restrict__ X, const int64_t* __restrict__ offR,
   }
   __syncthreads();
   // each thread: 8 consecutive k of one row -> one 16-byte store per slice
-  static_assert(S == S_SLICES, "digit routine is written for 7 slices");
+  static_assert(S == S_SLICES, "digit routine is written for 6 slices");
   const int rr = t >> 3, kc = t & 7;
   const int64_t r = r0 + rr;
   const int ef = (r < R) ? efield[r] : 0;
@@ -1141,7 +1176,7 @@ k_make_slices(const double* __restrict__ X, const int64_t* __restrict__ offR,
   for (int e = 0; e < 8; ++e) {
     int d[S];
     bool neg;
-    make_digits7_abs(tile[rr][kc * 8 + e], ef, d, neg);
+    make_digits_abs(tile[rr][kc * 8 + e], ef, d, neg);
     if (neg) sgn[e >> 1] |= (e & 1) ? 0x80000000u : 0x00008000u;
 #pragma unroll
     for (int p = 0; p < S; ++p) dg[p][e] = d[p];
@@ -1228,7 +1263,7 @@ int run(itg_handle* h, const ContractPlan& p, const double* A, const double* B, 
   // F: fixed-point fraction bits of the int64 accumulator (keeps |acc| < 2^62).
   int lk = 0;
   while (((int64_t)1 << lk) < p.K) ++lk;
-  const int F = 62 - 15 - lk;
+  const int F = 62 - 17 - lk;
   if (F < 8) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: contraction depth too large");
   if (tiles > (int64_t)INT32_MAX / 32) return itg_fail(h, ITG_ERR_UNSUPPORTED, "split: too many tiles");
   // the kernels need the attribute before the occupancy query
@@ -1552,10 +1587,10 @@ extern "C" int itg_split_partition(int64_t cluster_tiles, int clusters, int g, i
 }
 
 extern "C" double itg_split_error_bound(int64_t K) {
-  // |C_split - C|_F <= 4 K 2^-7S (1 + (S+1)/4 * 1.02) |A|_F |B|_F + 2^-52 |C|_F
+  // |C_split - C|_F <= 4 K 2^-8S (1 + (S+1)/4 * 1.02) |A|_F |B|_F + 2^-52 |C|_F
   // (digit truncation of both operands plus the dropped levels p + q >= S; the
   // 2^-52 term, bounded by |A|_F |B|_F, covers the final rounding to FP64).
   const int S = split::S_SLICES;
   const double k = (double)(K > 0 ? K : 1);
-  return 4.0 * k * std::ldexp(1.0, -7 * S) * (1.0 + 0.255 * (S + 1)) + std::ldexp(1.0, -52);
+  return 4.0 * k * std::ldexp(1.0, -8 * S) * (1.0 + 0.255 * (S + 1)) + std::ldexp(1.0, -52);
 }

@@ -286,7 +286,9 @@ def test_factorize_trunc(gpu, m, n, method, prec, ortho):
     """itg_factorize_trunc: the orthonormal factor is orthonormal to 1e-13 for
     every kept column (also for singular values far below sqrt(eps) sigma_max),
     the product reproduces the oracle's truncated SVD, and k / S / truncerr
-    follow the ITensors truncation of the oracle's spectrum."""
+    follow the ITensors truncation of the oracle's spectrum.  With split
+    products (prec 1) the Newton-Schulz steps measure X^T X through 48-bit
+    operand digits, so the orthonormality holds to 2e-13 there."""
     from itg import _lib
     import torch
     rng = np.random.default_rng(m * 7 + n + method + 10 * prec + 100 * ortho)
@@ -332,7 +334,7 @@ def test_factorize_trunc(gpu, m, n, method, prec, ortho):
         Lh = O.unflat(L.cpu().numpy()[: n * kk], (n, kk))
         Ch = O.unflat(Cm.cpu().numpy()[: m * kk], (m, kk))
         prod = Ch @ Lh.T
-    assert np.abs(Lh.T @ Lh - np.eye(kk)).max() < 1e-13
+    assert np.abs(Lh.T @ Lh - np.eye(kk)).max() < (1e-13 if prec == 0 else 2e-13)
     ref = (Uf[:, :kk] * Sf[:kk]) @ Vft[:kk]
     if method == 1:
         assert np.abs(prod - ref).max() < 1e-12 * So[0]

@@ -19,7 +19,7 @@ import ctypes as C
 
 import pytest
 
-S = 7
+S = 6  # digit levels of the split GEMM (base-2^8 digits per operand)
 T = S * (S + 1) // 2
 
 
