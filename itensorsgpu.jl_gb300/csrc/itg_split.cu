@@ -772,15 +772,30 @@ k_split_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ C
             for (int j = 0; j < FLUSH_BATCH; ++j) v[j] = acc[(size_t)(c0 + j) * BM + row];
           }
           if (m < args.M) {
+            // the column exponents and offsets are read-only for the whole
+            // launch: read-only loads, issued 8 at a time ahead of the stores
+            // (plain loads would be ordered after every store to C)
 #pragma unroll
-            for (int j = 0; j < FLUSH_BATCH; ++j) {
-              const int64_t n = (int64_t)n0 + c0 + j;
-              if (n >= args.N) continue;
-              double x = i64_to_double_scaled(v[j], em + args.eB[n] - 1022 - 16 - args.F);
-              if (args.alpha != 1.0) x *= args.alpha;
-              double* cp = args.C + cm + args.offCn[n];
-              if (args.beta != 0.0) x = fma(args.beta, *cp, x);
-              *cp = x;
+            for (int h = 0; h < FLUSH_BATCH / 8; ++h) {
+              int eb[8];
+              long long ocn[8];
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                const int64_t n = (int64_t)n0 + c0 + 8 * h + j;
+                const int64_t nc = n < args.N ? n : args.N - 1;
+                eb[j] = __ldg(args.eB + nc);
+                ocn[j] = __ldg((const long long*)args.offCn + nc);
+              }
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                const int64_t n = (int64_t)n0 + c0 + 8 * h + j;
+                if (n >= args.N) continue;
+                double x = i64_to_double_scaled(v[8 * h + j], em + eb[j] - 1022 - 16 - args.F);
+                if (args.alpha != 1.0) x *= args.alpha;
+                double* cp = args.C + cm + ocn[j];
+                if (args.beta != 0.0) x = fma(args.beta, *cp, x);
+                *cp = x;
+              }
             }
           }
         }
