@@ -775,7 +775,7 @@ def run_svd(args):
         t0 = time.perf_counter()
         try:
             h.call("itg_factorize_trunc", C.c_int64(n), C.c_int64(n), p(A), C.c_int64(n), C.c_int64(n // 2),
-                   C.c_int64(1), C.c_double(0.0), 0, 1, 0, 0, args.svd_method, prec, p(L), p(S), p(Cm),
+                   C.c_int64(1), C.c_double(0.0), 0, 1, 0, args.svd_ortho, args.svd_method, prec, p(L), p(S), p(Cm),
                    C.byref(k), None, None)
         except _lib.NotConverged:
             converged[0] = False   # factors are still written; reported below
@@ -784,19 +784,35 @@ def run_svd(args):
 
     # --svd-reps 1 (the profiled command): one cold call; more: one warm-up, best of the rest
     dt = once() if args.svd_reps <= 1 else min([once() for _ in range(args.svd_reps + 1)][1:])
+    phases = {}
+    if args.svd_reps > 1:
+        # one more (warm) call with the library's event profiler: stream time per phase
+        h.call("itg_profile", 1)
+        once()
+        for name, kind in (("qr", 4), ("jacobi", 5), ("refine", 6), ("gemm_split", 1), ("split_prep", 2),
+                           ("gemm_f64", 0)):
+            ms, nl = C.c_double(), C.c_int64()
+            h.call("itg_profile_read", kind, C.byref(ms), C.byref(nl))
+            phases[name] = round(ms.value, 3)
+        h.call("itg_profile", 0)
     sw, mu, fb = C.c_int(), C.c_int(), C.c_int64()
     h.call("itg_svd_info", C.byref(sw), C.byref(mu), C.byref(fb))
     kk = k.value
     Lh = L[: n * kk].reshape(kk, n).T.cpu().numpy()
-    Ch = Cm[: kk * n].reshape(n, kk).T.cpu().numpy()
     iso = float(np.abs(Lh.T @ Lh - np.eye(kk)).max())
     sv = np.exp(-np.arange(n) / 60.0)
-    rec = float(np.abs(Lh @ Ch - M).max() / sv[kk])
+    if args.svd_ortho == 0:   # L (n x k) isometric, C (k x n)
+        prod = Lh @ Cm[: kk * n].reshape(n, kk).T.cpu().numpy()
+    else:                     # C (n x k), L (n x k) isometric: A ~ C L^T
+        prod = Cm[: n * kk].reshape(kk, n).T.cpu().numpy() @ Lh.T
+    rec = float(np.abs(prod - M).max() / sv[kk])
     print(json.dumps({"metric": f"bond factorisation n={n}", "value": dt, "unit": "s", "higher_is_better": False,
                       "method": "mixed" if args.svd_method == 2 else "fp64 jacobi", "qr_precondition": args.svd_qr,
+                      "ortho": "right" if args.svd_ortho else "left",
                       "k": kk, "jacobi_sweeps": sw.value, "converged": converged[0], "mixed_used": mu.value,
                       "fallbacks": fb.value,
-                      "isometry_err": iso, "reconstruction_err_over_sigma_k": rec}), flush=True)
+                      "isometry_err": iso, "reconstruction_err_over_sigma_k": rec,
+                      "phase_ms": phases or None}), flush=True)
     return 0
 
 
@@ -974,7 +990,8 @@ def main():
     ap.add_argument("--svd-method", type=int, default=2, choices=[1, 2])
     ap.add_argument("--svd-qr", type=int, default=1, choices=[0, 1], help="Householder QR preconditioning")
     ap.add_argument("--svd-reps", type=int, default=1, help="timed factorisations (after one warm-up if > 1)")
-    ap.add_argument("--svd-jacobi-mode", type=int, default=0, choices=[0, 1, 2],
+    ap.add_argument("--svd-ortho", type=int, default=0, choices=[0, 1], help="isometric side: 0 left, 1 right")
+    ap.add_argument("--svd-jacobi-mode", type=int, default=0, choices=[0, 1, 2, 3],
                     help="itg_set_svd_options jacobi_mode")
     ap.add_argument("--config3", type=int, default=1, choices=[0, 1],
                     help="run the N=100 cutoff-1e-12 chosen-form DMRG against the FP64 oracle's energies")

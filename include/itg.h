@@ -100,8 +100,16 @@ ITG_API int itg_version(void);
  *   ITG_KERNEL_GEMM_F64   the FP64 gather-GEMM (k_gemm_gather_f64)
  *   ITG_KERNEL_GEMM_SPLIT the tcgen05 split-precision GEMM (k_split_gemm)
  *   ITG_KERNEL_SPLIT_PREP the split operand preparation (exponents + digits)
- *   ITG_KERNEL_HEFF_MID   the middle (merged-MPO) step of the H_eff matvec */
-enum { ITG_KERNEL_GEMM_F64 = 0, ITG_KERNEL_GEMM_SPLIT = 1, ITG_KERNEL_SPLIT_PREP = 2, ITG_KERNEL_HEFF_MID = 3 };
+ *   ITG_KERNEL_HEFF_MID   the middle (merged-MPO) step of the H_eff matvec
+ * and three phases of the SVD / bond factorisation (stream time from the
+ * phase's first launch to its last, including the host reads it waits on):
+ *   ITG_KERNEL_SVD_QR     Householder QR preconditioning and the application
+ *                         of its Q to the kept columns
+ *   ITG_KERNEL_SVD_JACOBI the Jacobi sweeps (FP32 in the mixed method)
+ *   ITG_KERNEL_SVD_REFINE the mixed method's FP64 refinement, Newton-Schulz
+ *                         steps and the polish of the isometric factor */
+enum { ITG_KERNEL_GEMM_F64 = 0, ITG_KERNEL_GEMM_SPLIT = 1, ITG_KERNEL_SPLIT_PREP = 2, ITG_KERNEL_HEFF_MID = 3,
+       ITG_KERNEL_SVD_QR = 4, ITG_KERNEL_SVD_JACOBI = 5, ITG_KERNEL_SVD_REFINE = 6 };
 ITG_API int itg_profile(itg_handle* h, int enable);
 ITG_API int itg_profile_read(itg_handle* h, int kernel, double* total_ms, int64_t* launches);
 /* Measured FP64 FMA throughput of the handle's GPU in TFLOP/s (independent
@@ -391,7 +399,9 @@ ITG_API int itg_svd_info(itg_handle* h, int* sweeps, int* mixed_used, int64_t* m
  * 0 (default): block-cyclic Jacobi, block pairs staged in shared memory,
  * one launch per block step; 1: one CTA per column pair, one launch per
  * round-robin step; 2: element pairs with all sweeps in one cooperative
- * launch and a grid barrier between steps (measured slower than 1 on GB300). */
+ * launch and a grid barrier between steps (measured slower than 1 on GB300);
+ * 3: as 0 with 4-column blocks (half the shared memory per CTA, so several
+ * CTAs share an SM). */
 ITG_API int itg_set_svd_options(itg_handle* h, int qr_precondition, int jacobi_mode);
 
 /* Eigendecomposition of the symmetric n x n matrix A: A = U diag(D) U^T with D

@@ -519,7 +519,7 @@ int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* f
     *sweeps_done = hp[0];
     return hp[0] >= JACOBI_MAX_SWEEPS ? ITG_ERR_NOTCONVERGED : ITG_OK;
   }
-  if (h->jacobi_mode == 0) {
+  if (h->jacobi_mode == 0 || h->jacobi_mode == 3) {
     const int st = itg::jacobi_blocked<double>(h, W, m, (int)n, V, tol, 0.0, JACOBI_MAX_SWEEPS, flag_dev,
                                                sweeps_done, amin_conv);
     if (st != ITG_ERR_UNSUPPORTED) return st;
@@ -549,8 +549,9 @@ int jacobi_run(itg_handle* h, double* W, int64_t m, int64_t n, double* V, int* f
 namespace itg {
 int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, int precision,
                    double* X, double* lam, double* Uw, double* ws, float* ws32, int* flag,
-                   int* sweeps_out);
+                   int* sweeps_out, bool need_u);
 size_t svd_mixed_ws_doubles(int64_t mm, int64_t nn);
+int ns_polish(itg_handle* h, double* L, int64_t rows, int64_t cols, double* ws, double* tmp, int precision);
 }  // namespace itg
 
 __global__ void k_sqrt_clamp(const double* __restrict__ lam, int n, double* __restrict__ sig) {
@@ -565,7 +566,7 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
                           int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
                           int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
                           int64_t* k, double* truncerr, double* docut, int method, int precision,
-                          int iso);
+                          int iso, bool want_other = true, bool square_t = false);
 
 extern "C" int itg_svd_trunc(itg_handle* h, int64_t m, int64_t n, const double* A, int64_t lda,
                              int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
@@ -601,7 +602,7 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
                           int64_t maxdim, int64_t mindim, double cutoff, int absoluteCutoff,
                           int doRelCutoff, int legacy_gpu, double* U, double* S, double* V,
                           int64_t* k, double* truncerr, double* docut, int method, int precision,
-                          int iso) {
+                          int iso, bool want_other, bool square_t) {
   if (!h || m < 0 || n < 0 || lda < m || !A || !U || !S || !V) return ITG_ERR_INVALID;
   if (m == 0 || n == 0) {
     if (k) *k = 0;
@@ -609,7 +610,8 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
     if (docut) *docut = 0;
     return ITG_OK;
   }
-  const bool tr = m < n;
+  // square_t: a square A is worked on as W = A^T (A's right side is W's left)
+  const bool tr = m < n || (square_t && m == n);
   const int64_t mm = tr ? n : m, nn = tr ? m : n;  // working shape, mm >= nn
   if (nn > 65535) return itg_fail(h, ITG_ERR_UNSUPPORTED, "svd: min(m,n) too large");
   size_t off = 0;
@@ -683,6 +685,7 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
     J = (double*)(base + oB);
     Tq = (double*)(base + oTq);
     Qws = (double*)(base + oQws);
+    ProfScope prof(h, ITG_KERNEL_SVD_QR);
     ITG_TRY(itg::qr_blocked(h, W, mm, nn, nn, Vh, tau, rd, Tq, Qws, qr_prec));
     k_build_rt<<<itg_blocks_for(nn * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(W, mm, (int)nn, rd, J);
     ITG_CHECK_LAUNCH(h);
@@ -713,7 +716,7 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
     double* lam = (double*)(base + oLam);
     double* Uw = (double*)(base + oUw);
     const int ms = itg::svd_mixed_core(h, J, mj, nn, precision, Vw, lam, Uw, (double*)(base + oWs),
-                                       (float*)(base + oWs32), flag, &sweeps);
+                                       (float*)(base + oWs32), flag, &sweeps, want_other || !pre);
     if (ms == ITG_ERR_NOTCONVERGED) {
       use_mixed = false;  // refinement failed its check: FP64 Jacobi on the same J
       h->svd_fallbacks++;
@@ -728,7 +731,7 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
     k_rank_desc<<<itg_blocks_for(nn, 256, 1024), 256, 0, h->stream>>>(sig, (int)nn, 0.0, order, S, P, 1);
     ITG_CHECK_LAUNCH(h);
     ITG_TRY(itg::truncate_dev(h, P, nn, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, out3));
-    k_gather_cols<<<g1, 256, 0, h->stream>>>(Uw, mj, order, sig, 0, (int)nn, Jl_dst, ld_l);
+    if (want_other || !pre) k_gather_cols<<<g1, 256, 0, h->stream>>>(Uw, mj, order, sig, 0, (int)nn, Jl_dst, ld_l);
     k_gather_cols<<<g2, 256, 0, h->stream>>>(Vw, nn, order, sig, 0, (int)nn, Jr_dst, ld_r);
     ITG_CHECK_LAUNCH(h);
   } else {
@@ -750,8 +753,18 @@ static int svd_trunc_impl(itg_handle* h, int64_t m, int64_t n, const double* A, 
   if (pre) {
     // rotate the kept columns back
     const int64_t kk = (k && *k > 0) ? *k : nn;
-    ITG_TRY(itg::q_apply_blocked(h, Uw_dst, mm, nn, kk, Vh, Tq, Qws));
-    if (two) ITG_TRY(itg::q_apply_blocked(h, Vw_dst, nn, nn, kk, Vh2, Tq2, Qws));
+    {
+      ProfScope prof(h, ITG_KERNEL_SVD_QR);
+      // with two QRs W's left slot holds the non-isometric factor
+      if (!two || want_other) ITG_TRY(itg::q_apply_blocked(h, Uw_dst, mm, nn, kk, Vh, Tq, Qws));
+      if (two) ITG_TRY(itg::q_apply_blocked(h, Vw_dst, nn, nn, kk, Vh2, Tq2, Qws));
+    }
+    // the mixed method's isometric factor: one Newton-Schulz step after the
+    // Householder rotation (W, the QR's input, is free by now)
+    if (use_mixed) {
+      ProfScope prof(h, ITG_KERNEL_SVD_REFINE);
+      ITG_TRY(itg::ns_polish(h, two ? Vw_dst : Uw_dst, two ? nn : mm, kk, (double*)(base + oWs), W, precision));
+    }
   }
   if (st == ITG_ERR_NOTCONVERGED)
     return itg_fail(h, ITG_ERR_NOTCONVERGED, "Jacobi SVD did not converge in %d sweeps", sweeps);
@@ -779,16 +792,21 @@ extern "C" int itg_factorize_trunc(itg_handle* h, int64_t m, int64_t n, const do
   if (lda != m) return itg_fail(h, ITG_ERR_UNSUPPORTED, "factorize needs lda == m");
   // the isometric factor in L's slot (U for ortho left, V for right); the other
   // SVD factor is scratch output in C's slot and replaced by the projection.
-  // (A square right-isometric split could go through A^T with one QR instead
-  // of ISO_RIGHT's two; measured at chi = 1024 the second QR pays for itself:
-  // Jacobi on R2^T needs fewer sweeps; the FP64 N = 24 sweep took 20.6 s with
-  // two QRs and 26.9 s with one, the mixed one was unchanged.)
+  // A square right-isometric split: the FP64 Jacobi keeps ISO_RIGHT's two QRs
+  // (Jacobi on R2^T needs fewer sweeps; the FP64 N = 24 sweep at chi = 1024
+  // took 20.6 s with two QRs and 26.9 s with one); the mixed method factors
+  // A^T with its left side isometric, one QR (2048 x 2048: 0.153 s against
+  // 0.178 s with two QRs).
   const bool tr = m < n;
-  const int iso = (ortho == ITG_ORTHO_LEFT) == !tr ? ISO_LEFT : ISO_RIGHT;
+  int iso = (ortho == ITG_ORTHO_LEFT) == !tr ? ISO_LEFT : ISO_RIGHT;
+  const bool mixed_path = method == ITG_SVD_MIXED || (method == ITG_SVD_AUTO && (m < n ? m : n) > ONECTA_MAX_N);
+  const bool square_t = mixed_path && m == n && iso == ISO_RIGHT;
+  if (square_t) iso = ISO_LEFT;
   double* Ubuf = ortho == ITG_ORTHO_LEFT ? L : C;
   double* Vbuf = ortho == ITG_ORTHO_LEFT ? C : L;
+  // the non-isometric factor is not needed: C is the projection below
   int st = svd_trunc_impl(h, m, n, A, lda, maxdim, mindim, cutoff, absoluteCutoff, doRelCutoff, legacy_gpu, Ubuf,
-                          S, Vbuf, &kk, truncerr, docut, method, precision, iso);
+                          S, Vbuf, &kk, truncerr, docut, method, precision, iso, false, square_t);
   if (st != ITG_OK && st != ITG_ERR_NOTCONVERGED) return st;
   if (k) *k = kk;
   if (kk == 0) return st;
@@ -947,7 +965,7 @@ extern "C" int itg_svd_info(itg_handle* h, int* sweeps, int* mixed_used, int64_t
 }
 
 extern "C" int itg_set_svd_options(itg_handle* h, int qr_precondition, int jacobi_mode) {
-  if (!h || jacobi_mode < 0 || jacobi_mode > 2) return ITG_ERR_INVALID;
+  if (!h || jacobi_mode < 0 || jacobi_mode > 3) return ITG_ERR_INVALID;
   h->svd_qr_precond = qr_precondition != 0;
   h->jacobi_mode = jacobi_mode;
   return ITG_OK;

@@ -123,7 +123,7 @@ struct itg_handle {
   bool last_mixed = false;    // the last SVD finished on the mixed method
   int64_t svd_fallbacks = 0;  // mixed SVDs redone with FP64 Jacobi
   bool svd_qr_precond = true; // itg_set_svd_options
-  int jacobi_mode = 0;        // 0 blocked, 1 element pairs per step, 2 one cooperative launch
+  int jacobi_mode = 0;        // 0 blocked, 1 element pairs per step, 2 one cooperative launch, 3 blocked narrow
 };
 
 // Record a timing event pair around a launch when profiling is on.

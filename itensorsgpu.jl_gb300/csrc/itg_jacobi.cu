@@ -22,6 +22,8 @@
 #include "itg_internal.cuh"
 
 #include <cmath>
+#include <cstdint>
+#include <type_traits>
 
 namespace {
 
@@ -258,14 +260,24 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
     return (blk < nb && gc < n) ? gc : -1;
   };
   if (t == 0) any = major = 0;
-  for (int c = 0; c < C2; ++c) {
-    const int gc = gcol(c);
-    T* dst = cols + (int64_t)c * m;
-    if (gc >= 0) {
-      const T* src = W + (int64_t)gc * m;
-      for (int64_t i = t; i < m; i += THREADS) dst[i] = src[i];
-    } else {
-      for (int64_t i = t; i < m; i += THREADS) dst[i] = T(0);
+  int gcs[C2];
+#pragma unroll
+  for (int c = 0; c < C2; ++c) gcs[c] = gcol(c);
+  // Stage the pair's columns: a thread issues its loads of all 2 WB columns
+  // (two rows at a time) before storing any of them, so the L2 latency is paid
+  // once per 4 WB loads instead of once per element.
+  for (int64_t i0 = t; i0 < m; i0 += 2 * THREADS) {
+    const int64_t i1 = i0 + THREADS;
+    T v0[C2], v1[C2];
+#pragma unroll
+    for (int c = 0; c < C2; ++c) {
+      v0[c] = gcs[c] >= 0 ? W[(int64_t)gcs[c] * m + i0] : T(0);
+      v1[c] = (gcs[c] >= 0 && i1 < m) ? W[(int64_t)gcs[c] * m + i1] : T(0);
+    }
+#pragma unroll
+    for (int c = 0; c < C2; ++c) {
+      cols[(int64_t)c * m + i0] = v0[c];
+      if (i1 < m) cols[(int64_t)c * m + i1] = v1[c];
     }
   }
   for (int i = t; i < C2 * C2; i += THREADS) Q[i] = (i % (C2 + 1) == 0) ? T(1) : T(0);
@@ -288,13 +300,36 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
     }
     T* xp = cols + (int64_t)p * m;
     T* xq = cols + (int64_t)q * m;
-    T a = 0, b = 0, gg = 0;
-    for (int64_t i = lt; i < m; i += TP) {
+    // the pair's column slices: four independent loads per iteration, two
+    // accumulator sets (m fits in shared memory, so 32-bit indices)
+    const int mi = (int)m;
+    T a = 0, b = 0, gg = 0, a1 = 0, b1 = 0, g1 = 0;
+    int i = lt;
+    for (; i + 3 * TP < mi; i += 4 * TP) {
+      const T x0 = xp[i], y0 = xq[i], x1 = xp[i + TP], y1 = xq[i + TP];
+      const T x2 = xp[i + 2 * TP], y2 = xq[i + 2 * TP], x3 = xp[i + 3 * TP], y3 = xq[i + 3 * TP];
+      a = fma(x0, x0, a);
+      b = fma(y0, y0, b);
+      gg = fma(x0, y0, gg);
+      a1 = fma(x1, x1, a1);
+      b1 = fma(y1, y1, b1);
+      g1 = fma(x1, y1, g1);
+      a = fma(x2, x2, a);
+      b = fma(y2, y2, b);
+      gg = fma(x2, y2, gg);
+      a1 = fma(x3, x3, a1);
+      b1 = fma(y3, y3, b1);
+      g1 = fma(x3, y3, g1);
+    }
+    for (; i < mi; i += TP) {
       const T x = xp[i], y = xq[i];
       a = fma(x, x, a);
       b = fma(y, y, b);
       gg = fma(x, y, gg);
     }
+    a += a1;
+    b += b1;
+    gg += g1;
     a = jp_warp_sum(a);
     b = jp_warp_sum(b);
     gg = jp_warp_sum(gg);
@@ -320,10 +355,24 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
       const T zeta = (b - a) / (T(2) * gg);
       const T tt = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
       const T c = T(1) / sqrt(T(1) + tt * tt), sn = c * tt;
-      for (int64_t i = lt; i < m; i += TP) {
-        const T x = xp[i], y = xq[i];
-        xp[i] = c * x - sn * y;
-        xq[i] = sn * x + c * y;
+      int j = lt;
+      for (; j + 3 * TP < mi; j += 4 * TP) {
+        T x[4], y[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          x[u] = xp[j + u * TP];
+          y[u] = xq[j + u * TP];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          xp[j + u * TP] = c * x[u] - sn * y[u];
+          xq[j + u * TP] = sn * x[u] + c * y[u];
+        }
+      }
+      for (; j < mi; j += TP) {
+        const T x = xp[j], y = xq[j];
+        xp[j] = c * x - sn * y;
+        xq[j] = sn * x + c * y;
       }
       if (lt < C2) {
         const T x = Q[lt + p * C2], y = Q[lt + q * C2];
@@ -345,14 +394,17 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
     T* dst = W + (int64_t)gc * m;
     for (int64_t i = t; i < m; i += THREADS) dst[i] = src[i];
   }
-  // V[:, cols] <- V[:, cols] Q, one row per thread
-  int gcs[C2];
+  // V[:, cols] <- V[:, cols] Q, one row per thread; the next row's loads are
+  // issued before the current row is combined and stored
+  int row = t;
+  T v[C2];
 #pragma unroll
-  for (int c = 0; c < C2; ++c) gcs[c] = gcol(c);
-  for (int row = t; row < n; row += THREADS) {
-    T v[C2];
+  for (int c = 0; c < C2; ++c) v[c] = (gcs[c] >= 0 && row < n) ? V[row + (int64_t)gcs[c] * n] : T(0);
+  for (; row < n; row += THREADS) {
+    const int nrow = row + THREADS;
+    T vn[C2];
 #pragma unroll
-    for (int c = 0; c < C2; ++c) v[c] = gcs[c] >= 0 ? V[row + (int64_t)gcs[c] * n] : T(0);
+    for (int c = 0; c < C2; ++c) vn[c] = (gcs[c] >= 0 && nrow < n) ? V[nrow + (int64_t)gcs[c] * n] : T(0);
 #pragma unroll
     for (int c = 0; c < C2; ++c) {
       if (gcs[c] < 0) continue;
@@ -361,6 +413,214 @@ k_jacobi_block_step(T* __restrict__ W, int64_t m, int n, T* __restrict__ V, T to
       for (int d = 0; d < C2; ++d) s = fma(v[d], Q[d + c * C2], s);
       V[row + (int64_t)gcs[c] * n] = s;
     }
+#pragma unroll
+    for (int c = 0; c < C2; ++c) v[c] = vn[c];
+  }
+  if (t == 0 && major) *rotated = 1;
+}
+
+// FP32 block step with 16-byte accesses (m and n multiples of 4, n <= m):
+// the rotations of k_jacobi_block_step<float> in the same order, with the
+// pair's columns staged, summed and rotated four rows at a time.  V's columns
+// are staged in shared memory (the column buffer is free after the write-back)
+// and each thread applies Q to four rows x four columns with its four Q
+// columns held in registers; the per-output sums run over d in the same order
+// as the element-wise kernel's.
+template <int WB, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+k_jacobi_block_step_f4(float* __restrict__ W, int64_t m, int n, float* __restrict__ V, float tol, float tol_conv,
+                       float amin, float amin_conv, int step, int first, int* __restrict__ rotated) {
+  constexpr int C2 = 2 * WB;          // local columns
+  constexpr int TP = THREADS / WB;    // threads per pair
+  constexpr int WPG = TP / 32;        // warps per pair group
+  constexpr int NG = C2 / 4;          // output column groups of the V update
+  extern __shared__ __align__(16) unsigned char jb_smem[];
+  float* cols = (float*)jb_smem;       // [C2][m]
+  float* Q = cols + (int64_t)C2 * m;   // [C2][C2], column-major
+  float* red = Q + C2 * C2;            // [WB][WPG][3]
+  __shared__ int any, major;
+  const int nb = (n + WB - 1) / WB, nbp = nb + (nb & 1);
+  const int bi = jp_player(blockIdx.x, step, nbp), bj = jp_player(nbp - 1 - blockIdx.x, step, nbp);
+  const int t = threadIdx.x;
+  const int m4 = (int)(m >> 2), n4 = n >> 2;
+  float4* cols4 = reinterpret_cast<float4*>(cols);
+  float4* W4 = reinterpret_cast<float4*>(W);
+  float4* V4 = reinterpret_cast<float4*>(V);
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  int gcs[C2];
+#pragma unroll
+  for (int c = 0; c < C2; ++c) {
+    const int blk = c < WB ? bi : bj;
+    const int gc = blk * WB + (c < WB ? c : c - WB);
+    gcs[c] = (blk < nb && gc < n) ? gc : -1;
+  }
+  if (t == 0) any = major = 0;
+  for (int i = t; i < m4; i += THREADS) {
+    float4 v[C2];
+#pragma unroll
+    for (int c = 0; c < C2; ++c) v[c] = gcs[c] >= 0 ? W4[(int64_t)gcs[c] * m4 + i] : zero4;
+#pragma unroll
+    for (int c = 0; c < C2; ++c) cols4[(int64_t)c * m4 + i] = v[c];
+  }
+  for (int i = t; i < C2 * C2; i += THREADS) Q[i] = (i % (C2 + 1) == 0) ? 1.f : 0.f;
+  __syncthreads();
+  const int g = t / TP, lt = t % TP, wg = lt / 32, lane = t & 31;
+  const int rounds = first ? C2 - 1 : WB;
+  for (int r = 0; r < rounds; ++r) {
+    int p, q;
+    if (first) {
+      p = jp_player(g, r, C2);
+      q = jp_player(C2 - 1 - g, r, C2);
+    } else {
+      p = g;
+      q = WB + (g + r) % WB;
+    }
+    if (p > q) {
+      const int tmp = p;
+      p = q;
+      q = tmp;
+    }
+    float4* xp = cols4 + (int64_t)p * m4;
+    float4* xq = cols4 + (int64_t)q * m4;
+    float a = 0.f, b = 0.f, gg = 0.f, a1 = 0.f, b1 = 0.f, g1 = 0.f;
+    int i = lt;
+    for (; i + TP < m4; i += 2 * TP) {
+      const float4 x0 = xp[i], y0 = xq[i], x1 = xp[i + TP], y1 = xq[i + TP];
+      a = fmaf(x0.x, x0.x, a);
+      b = fmaf(y0.x, y0.x, b);
+      gg = fmaf(x0.x, y0.x, gg);
+      a1 = fmaf(x0.y, x0.y, a1);
+      b1 = fmaf(y0.y, y0.y, b1);
+      g1 = fmaf(x0.y, y0.y, g1);
+      a = fmaf(x0.z, x0.z, a);
+      b = fmaf(y0.z, y0.z, b);
+      gg = fmaf(x0.z, y0.z, gg);
+      a1 = fmaf(x0.w, x0.w, a1);
+      b1 = fmaf(y0.w, y0.w, b1);
+      g1 = fmaf(x0.w, y0.w, g1);
+      a = fmaf(x1.x, x1.x, a);
+      b = fmaf(y1.x, y1.x, b);
+      gg = fmaf(x1.x, y1.x, gg);
+      a1 = fmaf(x1.y, x1.y, a1);
+      b1 = fmaf(y1.y, y1.y, b1);
+      g1 = fmaf(x1.y, y1.y, g1);
+      a = fmaf(x1.z, x1.z, a);
+      b = fmaf(y1.z, y1.z, b);
+      gg = fmaf(x1.z, y1.z, gg);
+      a1 = fmaf(x1.w, x1.w, a1);
+      b1 = fmaf(y1.w, y1.w, b1);
+      g1 = fmaf(x1.w, y1.w, g1);
+    }
+    if (i < m4) {
+      const float4 x0 = xp[i], y0 = xq[i];
+      a = fmaf(x0.x, x0.x, a);
+      b = fmaf(y0.x, y0.x, b);
+      gg = fmaf(x0.x, y0.x, gg);
+      a1 = fmaf(x0.y, x0.y, a1);
+      b1 = fmaf(y0.y, y0.y, b1);
+      g1 = fmaf(x0.y, y0.y, g1);
+      a = fmaf(x0.z, x0.z, a);
+      b = fmaf(y0.z, y0.z, b);
+      gg = fmaf(x0.z, y0.z, gg);
+      a1 = fmaf(x0.w, x0.w, a1);
+      b1 = fmaf(y0.w, y0.w, b1);
+      g1 = fmaf(x0.w, y0.w, g1);
+    }
+    a += a1;
+    b += b1;
+    gg += g1;
+    a = jp_warp_sum(a);
+    b = jp_warp_sum(b);
+    gg = jp_warp_sum(gg);
+    if constexpr (WPG > 1) {
+      if (lane == 0) {
+        red[(g * WPG + wg) * 3 + 0] = a;
+        red[(g * WPG + wg) * 3 + 1] = b;
+        red[(g * WPG + wg) * 3 + 2] = gg;
+      }
+      __syncthreads();
+      a = 0.f;
+      b = 0.f;
+      gg = 0.f;
+#pragma unroll
+      for (int w = 0; w < WPG; ++w) {
+        a += red[(g * WPG + w) * 3 + 0];
+        b += red[(g * WPG + w) * 3 + 1];
+        gg += red[(g * WPG + w) * 3 + 2];
+      }
+    }
+    const bool rot = !(a <= amin || b <= amin || fabsf(gg) <= tol * sqrtf(a) * sqrtf(b));
+    if (rot) {
+      const float zeta = (b - a) / (2.f * gg);
+      const float tt = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+      const float c = 1.f / sqrtf(1.f + tt * tt), sn = c * tt;
+      for (int j = lt; j < m4; j += TP) {
+        const float4 x = xp[j], y = xq[j];
+        xp[j] = make_float4(c * x.x - sn * y.x, c * x.y - sn * y.y, c * x.z - sn * y.z, c * x.w - sn * y.w);
+        xq[j] = make_float4(sn * x.x + c * y.x, sn * x.y + c * y.y, sn * x.z + c * y.z, sn * x.w + c * y.w);
+      }
+      if (lt < C2) {
+        const float x = Q[lt + p * C2], y = Q[lt + q * C2];
+        Q[lt + p * C2] = c * x - sn * y;
+        Q[lt + q * C2] = sn * x + c * y;
+      }
+      if (lt == 0) {
+        any = 1;
+        if (a > amin_conv && b > amin_conv && fabsf(gg) > tol_conv * sqrtf(a) * sqrtf(b)) major = 1;
+      }
+    }
+    __syncthreads();  // columns, Q and red are reused by the next round
+  }
+  if (!any) return;  // block-uniform (read after the last barrier)
+#pragma unroll
+  for (int c = 0; c < C2; ++c) {
+    if (gcs[c] < 0) continue;
+    const float4* src = cols4 + (int64_t)c * m4;
+    float4* dst = W4 + (int64_t)gcs[c] * m4;
+    for (int i = t; i < m4; i += THREADS) dst[i] = src[i];
+  }
+  __syncthreads();  // the column buffer now takes V's columns
+  for (int i = t; i < n4; i += THREADS) {
+    float4 v[C2];
+#pragma unroll
+    for (int c = 0; c < C2; ++c) v[c] = gcs[c] >= 0 ? V4[(int64_t)gcs[c] * n4 + i] : zero4;
+#pragma unroll
+    for (int c = 0; c < C2; ++c) cols4[(int64_t)c * n4 + i] = v[c];
+  }
+  __syncthreads();
+  // V[:, cols] <- V[:, cols] Q: output columns 4 og .. 4 og + 3, rows 4 r4 .. 4 r4 + 3
+  const int og = t % NG;
+  int ogc[4];  // global columns of this thread's outputs (-1: none)
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = 4 * og + j;
+    const int blk = c < WB ? bi : bj;
+    const int gc = blk * WB + (c < WB ? c : c - WB);
+    ogc[j] = (blk < nb && gc < n) ? gc : -1;
+  }
+  float qr[C2][4];
+#pragma unroll
+  for (int d = 0; d < C2; ++d)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) qr[d][j] = Q[d + (4 * og + j) * C2];
+  for (int r4 = t / NG; r4 < n4; r4 += THREADS / NG) {
+    float4 acc[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[j] = zero4;
+#pragma unroll
+    for (int d = 0; d < C2; ++d) {
+      const float4 x = cols4[(int64_t)d * n4 + r4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        acc[j].x = fmaf(x.x, qr[d][j], acc[j].x);
+        acc[j].y = fmaf(x.y, qr[d][j], acc[j].y);
+        acc[j].z = fmaf(x.z, qr[d][j], acc[j].z);
+        acc[j].w = fmaf(x.w, qr[d][j], acc[j].w);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (ogc[j] >= 0) V4[(int64_t)ogc[j] * n4 + r4] = acc[j];
   }
   if (t == 0 && major) *rotated = 1;
 }
@@ -450,20 +710,35 @@ template <class T, int WB, int THREADS>
 int jb_run_t(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, T amin_conv, int max_sweeps, int* flag,
              int* sweeps) {
   const size_t smem = jb_smem_bytes<T, WB>(m);
+  // FP32 with 16-byte aligned columns of W and V (and V's columns fitting in
+  // the column buffer): the vectorised step
+  const bool vec = std::is_same<T, float>::value && m % 4 == 0 && n % 4 == 0 && n <= m &&
+                   ((uintptr_t)W % 16) == 0 && ((uintptr_t)V % 16) == 0;
   static bool attr = false;
   if (!attr) {
     ITG_CUDA(h, cudaFuncSetAttribute(k_jacobi_block_step<T, WB, THREADS>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    if constexpr (std::is_same<T, float>::value)
+      ITG_CUDA(h, cudaFuncSetAttribute(k_jacobi_block_step_f4<WB, THREADS>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr = true;
   }
   const int nb = (n + WB - 1) / WB, nbp = nb + (nb & 1);
   int* hp = (int*)h->pinned;
   for (int sw = 0; sw < max_sweeps; ++sw) {
     ITG_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
-    for (int step = 0; step < nbp - 1; ++step)
+    for (int step = 0; step < nbp - 1; ++step) {
+      if constexpr (std::is_same<T, float>::value) {
+        if (vec) {
+          k_jacobi_block_step_f4<WB, THREADS><<<nbp / 2, THREADS, smem, h->stream>>>(
+              W, m, n, V, tol, conv_tol(tol), amin, amin_conv, step, step == 0, flag);
+          continue;
+        }
+      }
       k_jacobi_block_step<T, WB, THREADS><<<nbp / 2, THREADS, smem, h->stream>>>(W, m, n, V, tol, conv_tol(tol),
                                                                                  amin, amin_conv, step, step == 0,
                                                                                  flag);
+    }
     ITG_CHECK_LAUNCH(h);
     ITG_CUDA(h, cudaMemcpyAsync(hp, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     ITG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -494,7 +769,9 @@ int jacobi_blocked(itg_handle* h, T* W, int64_t m, int n, T* V, T tol, T amin, i
     *sweeps = 0;
     return ITG_OK;
   }
-  if (jb_smem_bytes<T, 8>(m) <= LIM && n >= 64) return jb_run<T, 8>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, flag, sweeps);
+  // jacobi_mode 3 keeps the blocks at 4 columns (half the shared memory per CTA, more CTAs per SM)
+  if (h->jacobi_mode != 3 && jb_smem_bytes<T, 8>(m) <= LIM && n >= 64)
+    return jb_run<T, 8>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, flag, sweeps);
   if (jb_smem_bytes<T, 4>(m) <= LIM) return jb_run<T, 4>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, flag, sweeps);
   if (jb_smem_bytes<T, 2>(m) <= LIM) return jb_run<T, 2>(h, W, m, n, V, tol, amin, amin_conv, max_sweeps, flag, sweeps);
   return ITG_ERR_UNSUPPORTED;

@@ -34,6 +34,8 @@
 // accuracy on tiny singular values.
 #include "itg_internal.cuh"
 
+#include <optional>
+
 #include <cmath>
 
 namespace itg {
@@ -309,9 +311,11 @@ namespace itg {
 // Uw (mm x nn).  `Awork` is the FP64 working matrix (mm x nn, ld = mm).
 int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, int precision,
                    double* X, double* lam, double* Uw, double* ws, float* ws32, int* flag,
-                   int* sweeps_out) {
+                   int* sweeps_out, bool need_u) {
   const int n = (int)nn;
   // 1. FP32 Jacobi
+  std::optional<ProfScope> prof_jacobi;
+  prof_jacobi.emplace(h, ITG_KERNEL_SVD_JACOBI);
   float* W32 = ws32;
   float* V32 = ws32 + mm * nn;
   k_to_float<<<itg_blocks_for(mm * nn, 256, h->num_sms * 16), 256, 0, h->stream>>>(Awork, mm, mm, nn, false, W32);
@@ -344,7 +348,7 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
     sweeps = hp[0];
   } else {
     int st = ITG_ERR_UNSUPPORTED;
-    if (h->jacobi_mode == 0)
+    if (h->jacobi_mode == 0 || h->jacobi_mode == 3)
       st = itg::jacobi_blocked<float>(h, W32, mm, n, V32, tol32, amin, 30, flag, &sweeps);
     else if (h->jacobi_mode == 2)
       st = itg::jacobi_persistent<float>(h, W32, mm, n, V32, tol32, amin, 30, flag, &sweeps);
@@ -365,6 +369,8 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
     }
   }
   *sweeps_out = sweeps;
+  prof_jacobi.reset();
+  ProfScope prof_refine(h, ITG_KERNEL_SVD_REFINE);
   // 2. refinement of X on G = A^T A
   // G P Q E Xn (nn^2 each) | S (max(mm*nn, nn^2), also the copy of U) | max slot
   double* G = ws;
@@ -440,6 +446,7 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
   // Newton-Schulz steps, or not finite) the caller redoes the problem with
   // FP64 Jacobi.
   if (!(dev <= 1e-12) || !std::isfinite(h->pinned[0])) return ITG_ERR_NOTCONVERGED;
+  if (!need_u) return ITG_OK;  // the caller keeps only the right vectors
   const double smax = sqrt(h->pinned[0] > 0.0 ? h->pinned[0] : 0.0);
   // 3. U = A X diag(1/sigma), one Newton-Schulz step
   ITG_TRY(gemm(h, false, mm, nn, nn, 1.0, Awork, X, 0.0, Uw, precision));
@@ -457,6 +464,32 @@ int svd_mixed_core(itg_handle* h, const double* Awork, int64_t mm, int64_t nn, i
   ITG_CUDA(h, cudaMemcpyAsync(Ucp, Uw, sizeof(double) * mm * nn, cudaMemcpyDeviceToDevice, h->stream));
   ITG_TRY(gemm(h, false, mm, nn, nn, 1.0, Ucp, Q, 1.0, Uw, precision));
   return ITG_OK;
+}
+
+// One Newton-Schulz step on an isometry L (rows x cols, ld rows, rows >= cols):
+// L <- L + L (I - L^T L) / 2, which squares its deviation from orthonormality.
+// The factor that leaves the bond split (Q times the refined eigenvectors)
+// carries the rounding of the Householder application, O(rows eps).  L^T L is
+// measured with FP64 products: split products resolve it only to about
+// 2^-48 sqrt(rows) (1e-13 at rows = 512), which is what this step removes;
+// the correction L (I - L^T L) / 2 is of that size, so its own product may be
+// split.  ws: 2 cols^2 doubles, tmp: rows x cols doubles (L's copy; the
+// product must not alias its operand).
+int ns_polish(itg_handle* h, double* L, int64_t rows, int64_t cols, double* ws, double* tmp, int precision) {
+  if (rows <= 0 || cols <= 0) return ITG_OK;
+  double* P = ws;
+  double* Q = ws + cols * cols;
+  // heuristic FP64 tiles: the shapes change from bond to bond, and timing the
+  // three tile variants of each new shape would cost more than the product
+  const bool tune = h->autotune;
+  h->autotune = false;
+  const int st = gemm(h, true, cols, cols, rows, 1.0, L, L, 0.0, P, ITG_PREC_FP64);
+  h->autotune = tune;
+  ITG_TRY(st);
+  k_half_identity_minus<<<itg_blocks_for(cols * cols, 256, h->num_sms * 16), 256, 0, h->stream>>>(P, (int)cols, Q);
+  ITG_CHECK_LAUNCH(h);
+  ITG_CUDA(h, cudaMemcpyAsync(tmp, L, sizeof(double) * rows * cols, cudaMemcpyDeviceToDevice, h->stream));
+  return gemm(h, false, rows, cols, cols, 1.0, tmp, Q, 1.0, L, precision);
 }
 
 size_t svd_mixed_ws_doubles(int64_t mm, int64_t nn) {
