@@ -13,8 +13,6 @@
 // on the FP64 gather-GEMM or on the split tensor-core path without copies.
 #include "itg_internal.cuh"
 
-#include <cooperative_groups.h>
-
 namespace itg {
 int run_plan(itg_handle* h, const ContractPlan& p, double alpha, const double* A, const double* B, double beta,
              double* C, int precision);
@@ -102,165 +100,6 @@ __global__ void k_larft(const double* __restrict__ Y, int ldy, const double* __r
     if (i == j) T[j + (int64_t)j * ldt] = tj;
     __syncthreads();
   }
-}
-
-// Panel factorisation in one launch: a cluster of PQ_CL CTAs holds the panel
-// (bw <= QR_NB columns) with its rows split evenly between the CTAs in shared
-// memory.  Column by column, every CTA forms its part of the column norm and
-// of the reflector's dot products with the remaining panel columns, sends the
-// partial sums to every CTA of the cluster through distributed shared memory,
-// and after a cluster barrier adds them in rank order, so every CTA derives
-// the same reflector and the same update without a further exchange.  Same
-// Householder reflector and outputs as the column steps of k_house_step
-// (v = [0, 1, x(j+1:)/(alpha - beta)], tau = (beta - alpha)/beta, R's
-// diagonal beta); the panel's columns below the diagonal come back holding
-// the reflectors (not read by any caller).  Two cluster barriers per column
-// replace two launches per column; all waits are the hardware cluster
-// barrier, which every thread of the cluster reaches the same number of times.
-namespace cg = cooperative_groups;
-constexpr int PQ_CL = 8;
-constexpr int PQ_THREADS = 256;
-constexpr int PQ_WARPS = PQ_THREADS / 32;
-
-__global__ void __launch_bounds__(PQ_THREADS)
-k_panel_qr(double* __restrict__ W, int64_t m, int64_t jb, int bw, int rb, double* __restrict__ Vh,
-           double* __restrict__ tau, double* __restrict__ rdiag) {
-  cg::cluster_group cl = cg::this_cluster();
-  const int rank = (int)cl.block_rank();
-  extern __shared__ __align__(16) double pq_smem[];
-  double* P = pq_smem;                        // [bw][rb]: this CTA's rows of the panel
-  double* red_a = P + (int64_t)bw * rb;       // [2][PQ_CL][2]: partial norm^2 and alpha (by column parity)
-  double* red_b = red_a + 2 * PQ_CL * 2;      // [PQ_CL][QR_NB]: partial dot products
-  double* part = red_b + PQ_CL * QR_NB;       // [QR_NB]: this CTA's dot products
-  double* wsum = part + QR_NB;                // [QR_NB]: the summed dot products
-  __shared__ double sh[PQ_WARPS];
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const int64_t r0 = (int64_t)rank * rb;
-  const int nr = (int)(m - r0 < 0 ? 0 : (m - r0 < rb ? m - r0 : rb));
-  for (int c = 0; c < bw; ++c) {
-    const double* src = W + (jb + c) * m + r0;
-    for (int i = t; i < nr; i += PQ_THREADS) P[(int64_t)c * rb + i] = src[i];
-  }
-  __syncthreads();
-  for (int jj = 0; jj < bw; ++jj) {
-    const int64_t j = jb + jj;
-    double* x = P + (int64_t)jj * rb;
-    // rows of this CTA with global index > j, and >= j
-    const int ilo = (int)(j + 1 - r0 < 0 ? 0 : (j + 1 - r0 > nr ? nr : j + 1 - r0));
-    const int ijlo = (int)(j - r0 < 0 ? 0 : (j - r0 > nr ? nr : j - r0));
-    double s = 0.0;
-    for (int i = ilo + t; i < nr; i += PQ_THREADS) s = fma(x[i], x[i], s);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) sh[warp] = s;
-    __syncthreads();
-    if (t < PQ_CL) {
-      double ps = 0.0;
-      for (int w = 0; w < PQ_WARPS; ++w) ps += sh[w];
-      const double al = (j >= r0 && j < r0 + nr) ? x[j - r0] : 0.0;
-      double* dst = cl.map_shared_rank(red_a, t) + ((jj & 1) * PQ_CL + rank) * 2;
-      dst[0] = ps;
-      dst[1] = al;
-    }
-    cl.sync();
-    double s2 = 0.0, alpha = 0.0;
-    const double* ra = red_a + (jj & 1) * PQ_CL * 2;
-    for (int r = 0; r < PQ_CL; ++r) {
-      s2 += ra[2 * r];
-      alpha += ra[2 * r + 1];
-    }
-    double tj = 0.0, beta = alpha, scale = 0.0;
-    if (s2 > 0.0) {
-      beta = -copysign(hypot(alpha, sqrt(s2)), alpha);
-      tj = (beta - alpha) / beta;
-      scale = 1.0 / (alpha - beta);
-    }
-    // the reflector over this CTA's rows; kept in place for rows >= j (rows
-    // above j hold R's entries of this column)
-    double* vcol = Vh + j * m + r0;
-    for (int i = t; i < nr; i += PQ_THREADS) {
-      const int64_t gi = r0 + i;
-      double v;
-      if (gi < j) {
-        v = 0.0;
-      } else {
-        v = gi == j ? 1.0 : x[i] * scale;
-        x[i] = v;
-      }
-      vcol[i] = v;
-    }
-    if (rank == 0 && t == 0) {
-      tau[j] = tj;
-      rdiag[j] = beta;
-    }
-    __syncthreads();
-    const int ncol = bw - jj - 1;
-    if (tj == 0.0 || ncol == 0) continue;  // the same decision in every CTA (same s2)
-    // this CTA's part of w_c = v . col_c over rows >= j, one warp per column
-    for (int cc = warp; cc < ncol; cc += PQ_WARPS) {
-      const double* col = P + (int64_t)(jj + 1 + cc) * rb;
-      double d = 0.0;
-      for (int i = ijlo + lane; i < nr; i += 32) d = fma(x[i], col[i], d);
-      for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-      if (lane == 0) part[cc] = d;
-    }
-    __syncthreads();
-    for (int q = t; q < PQ_CL * ncol; q += PQ_THREADS) {
-      const int r = q / ncol, cc = q - r * ncol;
-      cl.map_shared_rank(red_b, r)[rank * QR_NB + cc] = part[cc];
-    }
-    cl.sync();
-    if (t < ncol) {
-      double w = 0.0;
-      for (int r = 0; r < PQ_CL; ++r) w += red_b[r * QR_NB + t];
-      wsum[t] = tj * w;
-    }
-    __syncthreads();
-    const int len = nr - ijlo;
-    for (int q = t; q < ncol * len; q += PQ_THREADS) {
-      const int cc = q / len, i = ijlo + (q - cc * len);
-      P[(int64_t)(jj + 1 + cc) * rb + i] -= wsum[cc] * x[i];
-    }
-    __syncthreads();
-  }
-  for (int c = 0; c < bw; ++c) {
-    double* dst = W + (jb + c) * m + r0;
-    for (int i = t; i < nr; i += PQ_THREADS) dst[i] = P[(int64_t)c * rb + i];
-  }
-  cl.sync();  // no CTA leaves while a peer may still address its shared memory
-}
-
-size_t panel_qr_smem(int64_t rb) {
-  return sizeof(double) * ((size_t)QR_NB * rb + 2 * PQ_CL * 2 + PQ_CL * QR_NB + 2 * QR_NB);
-}
-
-// One launch for the panel's column steps when its rows fit the cluster's
-// shared memory; false: the caller runs the column steps (k_house_step).
-int panel_qr_launch(itg_handle* h, double* W, int64_t m, int64_t jb, int bw, double* Vh, double* tau, double* rd,
-                    bool& done) {
-  done = false;
-  const int64_t rb = (m + PQ_CL - 1) / PQ_CL;
-  const size_t smem = panel_qr_smem(rb);
-  if (m < 256 || smem > 200 * 1024 || bw > QR_NB) return ITG_OK;
-  static bool attr = false;
-  if (!attr) {
-    ITG_CUDA(h, cudaFuncSetAttribute(k_panel_qr, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = true;
-  }
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(PQ_CL);
-  cfg.blockDim = dim3(PQ_THREADS);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = h->stream;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = PQ_CL;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  ITG_CUDA(h, cudaLaunchKernelEx(&cfg, k_panel_qr, W, m, jb, bw, (int)rb, Vh, tau, rd));
-  done = true;
-  return ITG_OK;
 }
 
 // C (bw x N, ld ldc) = V_p^T B for the panel's reflectors V_p (columns jb..jb+bw
@@ -359,10 +198,7 @@ int qr_blocked(itg_handle* h, double* W, int64_t m, int64_t n, int64_t nref, dou
   const int64_t part_doubles = QR_PART_CHUNKS * 32 * n;
   for (int64_t jb = 0, panel = 0; jb < nref; jb += NB, ++panel) {
     const int64_t bw = (nref - jb < NB) ? nref - jb : NB;
-    bool one_launch = false;
-    ITG_TRY(panel_qr_launch(h, W, m, jb, (int)bw, Vh, tau, rd, one_launch));
-    if (!one_launch)
-      for (int64_t j = jb; j < jb + bw; ++j) house_step_launch(h, W, m, (int)j, (int)(jb + bw - j), Vh, tau, rd);
+    for (int64_t j = jb; j < jb + bw; ++j) house_step_launch(h, W, m, (int)j, (int)(jb + bw - j), Vh, tau, rd);
     ITG_CHECK_LAUNCH(h);
     const int64_t nt = n - jb - bw;
     double* Tp = Tbuf + panel * NB * NB;
