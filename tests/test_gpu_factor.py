@@ -122,10 +122,12 @@ def test_svd_truncation_matches_oracle(gpu):
         assert spec.truncerr == pytest.approx(te, rel=1e-9, abs=1e-16)
 
 
-@pytest.mark.parametrize("n,prec", [(300, 0), (512, 1), (1024, 1)])
+@pytest.mark.parametrize("n,prec", [(300, 0), (258, 1), (512, 1), (1024, 1)])
 def test_svd_mixed_haar_exp_spectrum(gpu, n, prec):
     """The Jacobi-SVD microbench matrix: A = U diag(exp(-k/20)) V^T with Haar U, V;
-    mixed path (FP32 Jacobi + refinement, products at FP64 or split precision)."""
+    mixed path (FP32 Jacobi + refinement, products at FP64 or split precision).
+    n = 258 (not a multiple of 4) runs the element-wise FP32 block step, the
+    other sizes the float4 one."""
     from itg import _lib
     import torch
     rng = np.random.default_rng(n)
