@@ -146,6 +146,10 @@ extern "C" int itg_destroy(itg_handle* h) {
   if (h->dev_status) cudaFree(h->dev_status);
   if (h->gemv_part) cudaFree(h->gemv_part);
   if (h->tab_buf) cudaFree(h->tab_buf);
+  if (h->tab_buf2) cudaFree(h->tab_buf2);
+  if (h->qr_ev_ready) cudaEventDestroy(h->qr_ev_ready);
+  if (h->qr_ev_done) cudaEventDestroy(h->qr_ev_done);
+  if (h->qr_stream) cudaStreamDestroy(h->qr_stream);
   if (h->cplx_buf) cudaFree(h->cplx_buf);
   delete h;
   return ITG_OK;

@@ -114,6 +114,13 @@ struct itg_handle {
   size_t cplx_buf_bytes = 0;
   int64_t* tab_buf = nullptr; // offset tables of the blocked QR's submatrix products
   int64_t tab_buf_elems = 0;
+  // Look-ahead of the blocked QR: the trailing updates run on qr_stream while
+  // the next panel is factored on `stream` (own offset tables, two events).
+  cudaStream_t qr_stream = nullptr;
+  cudaEvent_t qr_ev_ready = nullptr;  // panel's reflectors and T are final (on `stream`)
+  cudaEvent_t qr_ev_done = nullptr;   // trailing update finished (on qr_stream)
+  int64_t* tab_buf2 = nullptr;
+  int64_t tab_buf2_elems = 0;
   // Split operand slice reuse: [0] the A operand, [1] the B operand of the
   // next split contraction when slice_keep[i] is set (see SliceCache).
   SliceCache slice_cache[2];

@@ -47,34 +47,41 @@ struct TabPlan : ContractPlan {
   ~TabPlan() { tables = nullptr; }  // the tables live in the handle's buffer
 };
 
+// Both offset-table buffers hold at least `elems` entries.  Growing one waits
+// for the whole device: the look-ahead stream may still read the old buffer.
 int tab_reserve(itg_handle* h, int64_t elems) {
-  if (elems <= h->tab_buf_elems) return ITG_OK;
-  if (h->tab_buf) {
-    ITG_CUDA(h, cudaStreamSynchronize(h->stream));
-    cudaFree(h->tab_buf);
-    h->tab_buf = nullptr;
-    h->tab_buf_elems = 0;
+  if (elems <= h->tab_buf_elems && elems <= h->tab_buf2_elems) return ITG_OK;
+  ITG_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (h->qr_stream) ITG_CUDA(h, cudaStreamSynchronize(h->qr_stream));
+  for (int b = 0; b < 2; ++b) {
+    int64_t*& buf = b ? h->tab_buf2 : h->tab_buf;
+    int64_t& cap = b ? h->tab_buf2_elems : h->tab_buf_elems;
+    if (elems <= cap) continue;
+    if (buf) cudaFree(buf);
+    buf = nullptr;
+    cap = 0;
+    if (cudaMalloc((void**)&buf, sizeof(int64_t) * elems) != cudaSuccess)
+      return itg_fail(h, ITG_ERR_ALLOC, "QR offset tables");
+    cap = elems;
   }
-  if (cudaMalloc((void**)&h->tab_buf, sizeof(int64_t) * elems) != cudaSuccess)
-    return itg_fail(h, ITG_ERR_ALLOC, "QR offset tables");
-  h->tab_buf_elems = elems;
   return ITG_OK;
 }
 
-// C[M x N] = alpha * A B + beta * C over submatrices described by affine offsets.
+// C[M x N] = alpha * A B + beta * C over submatrices described by affine
+// offsets, on the handle's current stream with the offset tables in `tab`
+// (tab_reserve'd: at least 2 (M + N + K) entries).
 int strided_gemm(itg_handle* h, int64_t M, int64_t N, int64_t K, double alpha, const double* A, Aff am, Aff ak,
                  bool a_kmaj, const double* B, Aff bk, Aff bn, bool b_kmaj, double beta, double* C, Aff cm, Aff cn,
-                 int precision) {
+                 int precision, int64_t* tab) {
   if (M <= 0 || N <= 0 || K <= 0) return ITG_OK;
   const int64_t tot = 2 * M + 2 * N + 2 * K;
-  ITG_TRY(tab_reserve(h, tot));
-  k_fill_tables<<<itg_blocks_for(tot, 256, 64), 256, 0, h->stream>>>(h->tab_buf, M, N, K, am, cm, bn, cn, ak, bk);
+  k_fill_tables<<<itg_blocks_for(tot, 256, 64), 256, 0, h->stream>>>(tab, M, N, K, am, cm, bn, cn, ak, bk);
   ITG_CHECK_LAUNCH(h);
   TabPlan p;
   p.M = M;
   p.N = N;
   p.K = K;
-  p.tables = h->tab_buf;
+  p.tables = tab;
   p.a_kmaj = a_kmaj;
   p.b_kmaj = b_kmaj;
   return itg::run_plan(h, p, alpha, A, B, beta, C, precision);
@@ -188,34 +195,114 @@ namespace itg {
 // Vh (m x nref, explicit unit diagonal, zeros above), tau, R's diagonal in rd,
 // the rest of R's rows above the diagonal in W; Tbuf holds QR_NB^2 doubles
 // per panel of reflectors and ws qr_blocked_ws_doubles(n) doubles.
+//
+// Look-ahead: the column steps of a panel are bound by their serial FP64
+// scalar work and occupy few SMs.  They run on a stream of the greatest
+// priority (qr_stream), so that their blocks are scheduled ahead of the
+// trailing updates' product blocks, which run on the handle's stream: once
+// panel p's reflectors and T are final, the panel stream updates the columns
+// of panel p + 1 by them and factors panel p + 1 at once, while the handle's
+// stream updates the rest of the trailing matrix by panel p.  The panel stream
+// waits for that update before it applies the next panel's reflectors to the
+// columns the update covers.  Each stream has its own Z, Z2, partial-sum and
+// offset-table buffers.  Results are deterministic (the split of V^T A's K
+// range into chunks depends only on the column counts).
+namespace {
+struct QrBufs {
+  double *Z, *Z2, *part;
+  int64_t part_doubles;
+  int64_t* tab;
+};
+
+// A(:, c0 : c0 + nc) -= V_p (T_p^T (V_p^T A(:, c0 : c0 + nc))) on the handle's current stream
+int qr_update_cols(itg_handle* h, double* W, int64_t m, int64_t jb, int64_t bw, const double* Vh, const double* Tp,
+                   int64_t c0, int64_t nc, const QrBufs& b, int precision) {
+  if (nc <= 0) return ITG_OK;
+  const int NB = QR_NB;
+  ITG_TRY(skinny_vt_b(h, Vh, m, jb, (int)bw, W, m, c0, nc, b.Z, bw, b.part, b.part_doubles));
+  ITG_TRY(strided_gemm(h, bw, nc, bw, 1.0, Tp, Aff{0, NB}, Aff{0, 1}, true, b.Z, Aff{0, 1}, Aff{0, bw}, true, 0.0,
+                       b.Z2, Aff{0, 1}, Aff{0, bw}, precision, b.tab));
+  return strided_gemm(h, m - jb, nc, bw, -1.0, Vh, Aff{jb, 1}, Aff{jb * m, m}, false, b.Z2, Aff{0, 1}, Aff{0, bw},
+                      true, 1.0, W, Aff{jb, 1}, Aff{c0 * m, m}, precision, b.tab);
+}
+
+// The handle's stream is swapped for the panel stream while this lives.
+struct OnStream {
+  itg_handle* h;
+  cudaStream_t saved;
+  OnStream(itg_handle* hh, cudaStream_t s) : h(hh), saved(hh->stream) { h->stream = s; }
+  ~OnStream() { h->stream = saved; }
+};
+
+int qr_lookahead_init(itg_handle* h) {
+  if (h->qr_stream) return ITG_OK;
+  int least = 0, greatest = 0;
+  ITG_CUDA(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  ITG_CUDA(h, cudaStreamCreateWithPriority(&h->qr_stream, cudaStreamNonBlocking, greatest));
+  ITG_CUDA(h, cudaEventCreateWithFlags(&h->qr_ev_ready, cudaEventDisableTiming));
+  ITG_CUDA(h, cudaEventCreateWithFlags(&h->qr_ev_done, cudaEventDisableTiming));
+  return ITG_OK;
+}
+}  // namespace
+
 int qr_blocked(itg_handle* h, double* W, int64_t m, int64_t n, int64_t nref, double* Vh, double* tau, double* rd,
                double* Tbuf, double* ws, int precision) {
   const int NB = QR_NB;
-  double* Ym = ws;
-  double* Z = ws + NB * NB;
-  double* Z2 = Z + (int64_t)NB * n;
-  double* part = Z2 + (int64_t)NB * n;
   const int64_t part_doubles = QR_PART_CHUNKS * 32 * n;
+  double* Ym = ws;
+  QrBufs bp{ws + NB * NB, ws + NB * NB + (int64_t)NB * n, ws + NB * NB + 2 * (int64_t)NB * n, part_doubles,
+            nullptr};  // panel stream
+  double* ws2 = bp.part + part_doubles;
+  QrBufs bu{ws2, ws2 + (int64_t)NB * n, ws2 + 2 * (int64_t)NB * n, part_doubles, nullptr};  // update stream
+  ITG_TRY(qr_lookahead_init(h));
+  ITG_TRY(tab_reserve(h, 2 * (m + n + NB)));
+  bp.tab = h->tab_buf;
+  bu.tab = h->tab_buf2;
+  cudaStream_t main_stream = h->stream;
+  // the panel stream starts after everything already queued on the handle's stream
+  ITG_CUDA(h, cudaEventRecord(h->qr_ev_done, main_stream));
+  {
+    OnStream on(h, h->qr_stream);
+    ITG_CUDA(h, cudaStreamWaitEvent(h->stream, h->qr_ev_done, 0));
+    if (nref > 0)
+      for (int64_t j = 0; j < (nref < NB ? nref : NB); ++j)
+        house_step_launch(h, W, m, (int)j, (int)((nref < NB ? nref : NB) - j), Vh, tau, rd);
+    ITG_CHECK_LAUNCH(h);
+  }
   for (int64_t jb = 0, panel = 0; jb < nref; jb += NB, ++panel) {
     const int64_t bw = (nref - jb < NB) ? nref - jb : NB;
-    for (int64_t j = jb; j < jb + bw; ++j) house_step_launch(h, W, m, (int)j, (int)(jb + bw - j), Vh, tau, rd);
-    ITG_CHECK_LAUNCH(h);
     const int64_t nt = n - jb - bw;
     double* Tp = Tbuf + panel * NB * NB;
-    // Y = V_p^T V_p (FP64: it defines T)
-    ITG_TRY(skinny_vt_b(h, Vh, m, jb, (int)bw, Vh, m, jb, bw, Ym, bw, part, part_doubles));
-    k_larft<<<1, QR_NB_MAX, 0, h->stream>>>(Ym, (int)bw, tau + jb, (int)bw, Tp, NB);
-    ITG_CHECK_LAUNCH(h);
-    if (nt <= 0) continue;
-    // Z = V_p^T A_t
-    ITG_TRY(skinny_vt_b(h, Vh, m, jb, (int)bw, W, m, jb + bw, nt, Z, bw, part, part_doubles));
-    // Z2 = T^T Z
-    ITG_TRY(strided_gemm(h, bw, nt, bw, 1.0, Tp, Aff{0, NB}, Aff{0, 1}, true, Z, Aff{0, 1}, Aff{0, bw}, true, 0.0,
-                         Z2, Aff{0, 1}, Aff{0, bw}, precision));
-    // A_t -= V_p Z2
-    ITG_TRY(strided_gemm(h, m - jb, nt, bw, -1.0, Vh, Aff{jb, 1}, Aff{jb * m, m}, false, Z2, Aff{0, 1},
-                         Aff{0, bw}, true, 1.0, W, Aff{jb, 1}, Aff{(jb + bw) * m, m}, precision));
+    const int64_t jn = jb + bw;
+    const int64_t nnext = nt > 0 && jn < nref ? ((nref - jn < NB) ? nref - jn : NB) : 0;
+    const int64_t nrest = nt > 0 ? nt - nnext : 0;
+    {
+      OnStream on(h, h->qr_stream);
+      // Y = V_p^T V_p (FP64: it defines T)
+      ITG_TRY(skinny_vt_b(h, Vh, m, jb, (int)bw, Vh, m, jb, bw, Ym, bw, bp.part, part_doubles));
+      k_larft<<<1, QR_NB_MAX, 0, h->stream>>>(Ym, (int)bw, tau + jb, (int)bw, Tp, NB);
+      ITG_CHECK_LAUNCH(h);
+      if (nt <= 0) continue;
+      // V_p and T_p are final: the handle's stream may update the rest
+      ITG_CUDA(h, cudaEventRecord(h->qr_ev_ready, h->stream));
+      // panel p + 1's columns got panel p - 1's update on the handle's stream
+      if (panel > 0) ITG_CUDA(h, cudaStreamWaitEvent(h->stream, h->qr_ev_done, 0));
+      ITG_TRY(qr_update_cols(h, W, m, jb, bw, Vh, Tp, jn, nnext, bp, precision));
+    }
+    if (nrest > 0) {
+      ITG_CUDA(h, cudaStreamWaitEvent(main_stream, h->qr_ev_ready, 0));
+      ITG_TRY(qr_update_cols(h, W, m, jb, bw, Vh, Tp, jn + nnext, nrest, bu, precision));
+    }
+    ITG_CUDA(h, cudaEventRecord(h->qr_ev_done, main_stream));
+    if (nnext > 0) {
+      OnStream on(h, h->qr_stream);
+      for (int64_t j = jn; j < jn + nnext; ++j) house_step_launch(h, W, m, (int)j, (int)(jn + nnext - j), Vh, tau, rd);
+      ITG_CHECK_LAUNCH(h);
+    }
   }
+  // the handle's stream continues after the last panel's work
+  ITG_CUDA(h, cudaEventRecord(h->qr_ev_ready, h->qr_stream));
+  ITG_CUDA(h, cudaStreamWaitEvent(main_stream, h->qr_ev_ready, 0));
   return ITG_OK;
 }
 
@@ -229,6 +316,7 @@ int q_apply_blocked(itg_handle* h, double* Y, int64_t m, int64_t n, int64_t ncol
   double* Z2 = Z + (int64_t)NB * ncols;
   double* part = Z2 + (int64_t)NB * ncols;
   const int64_t part_doubles = QR_PART_CHUNKS * 32 * ncols;
+  ITG_TRY(tab_reserve(h, 2 * (m + ncols + NB)));
   const int64_t npanel = (n + NB - 1) / NB;
   for (int64_t panel = npanel - 1; panel >= 0; --panel) {
     const int64_t jb = panel * NB;
@@ -238,16 +326,18 @@ int q_apply_blocked(itg_handle* h, double* Y, int64_t m, int64_t n, int64_t ncol
     ITG_TRY(skinny_vt_b(h, Vh, m, jb, (int)bw, Y, m, 0, ncols, Z, bw, part, part_doubles));
     // Z2 = T Z
     ITG_TRY(strided_gemm(h, bw, ncols, bw, 1.0, Tp, Aff{0, 1}, Aff{0, NB}, false, Z, Aff{0, 1}, Aff{0, bw}, true,
-                         0.0, Z2, Aff{0, 1}, Aff{0, bw}, ITG_PREC_FP64));
+                         0.0, Z2, Aff{0, 1}, Aff{0, bw}, ITG_PREC_FP64, h->tab_buf));
     // Y(jb:m, :) -= V_p Z2
     ITG_TRY(strided_gemm(h, m - jb, ncols, bw, -1.0, Vh, Aff{jb, 1}, Aff{jb * m, m}, false, Z2, Aff{0, 1},
-                         Aff{0, bw}, true, 1.0, Y, Aff{jb, 1}, Aff{0, m}, ITG_PREC_FP64));
+                         Aff{0, bw}, true, 1.0, Y, Aff{jb, 1}, Aff{0, m}, ITG_PREC_FP64, h->tab_buf));
   }
   return ITG_OK;
 }
 
+// Y, then Z, Z2 and the partial sums of the handle's stream, then those of the
+// look-ahead stream.
 size_t qr_blocked_ws_doubles(int64_t n) {
-  return (size_t)QR_NB * QR_NB + 2 * (size_t)QR_NB * n + (size_t)QR_PART_CHUNKS * 32 * n;
+  return (size_t)QR_NB * QR_NB + 2 * (2 * (size_t)QR_NB * n + (size_t)QR_PART_CHUNKS * 32 * n);
 }
 size_t qr_blocked_t_doubles(int64_t n) { return (size_t)((n + QR_NB - 1) / QR_NB) * QR_NB * QR_NB; }
 
