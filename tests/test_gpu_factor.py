@@ -388,3 +388,47 @@ def test_jacobi_rank_deficient_converges(gpu, pre, shape):
             assert np.abs(rec - X).max() < 1e-12 * np.abs(X).max()
     finally:
         h.call("itg_set_svd_options", 1, 0)
+
+
+def test_svd_phase_profiler_covers_the_factorisation(gpu):
+    """The event profiler's SVD phases (ITG_KERNEL_SVD_QR / _JACOBI / _REFINE =
+    4 / 5 / 6) each record time for a mixed bond split large enough for the
+    QR-preconditioned blocked path, their sum stays within the call's wall time,
+    and recording them does not change the factors."""
+    import time
+    from itg import _lib
+    import torch
+    n = 512
+    rng = np.random.default_rng(11)
+    Q1, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    Q2, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    M = (Q1 * np.exp(-np.arange(n) / 40.0)) @ Q2.T
+    h = _lib.handle(0)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    A = torch.from_numpy(O.flat(M).copy()).cuda()
+
+    def split():
+        L = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        S = torch.empty(n, dtype=torch.float64, device="cuda")
+        Cm = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        k = C.c_int64()
+        h.call("itg_factorize_trunc", C.c_int64(n), C.c_int64(n), p(A), C.c_int64(n), C.c_int64(n // 2),
+               C.c_int64(1), C.c_double(0.0), 0, 1, 0, 0, 2, 1, p(L), p(S), p(Cm), C.byref(k), None, None)
+        return L[: n * k.value].clone(), S[: k.value].clone()
+
+    L0, S0 = split()
+    torch.cuda.synchronize()
+    h.call("itg_profile", 1)
+    t0 = time.perf_counter()
+    L1, S1 = split()
+    torch.cuda.synchronize()
+    wall_ms = (time.perf_counter() - t0) * 1e3
+    phases = []
+    for kind in (4, 5, 6):
+        ms, nl = C.c_double(), C.c_int64()
+        h.call("itg_profile_read", kind, C.byref(ms), C.byref(nl))
+        assert nl.value >= 1 and ms.value > 0.0, kind
+        phases.append(ms.value)
+    h.call("itg_profile", 0)
+    assert sum(phases) <= wall_ms * 1.05 + 0.5, (phases, wall_ms)
+    assert torch.equal(L0, L1) and torch.equal(S0, S1)
