@@ -15,7 +15,10 @@
  *    `Dense` storage of NDTensors (src/tensor/cudense.jl:19).  Dimensions are
  *    int64, mode labels are int32.
  *  - All device work is enqueued on the handle's stream and is asynchronous,
- *    except where an output is documented as a host scalar.
+ *    except where an output is documented as a host scalar.  The blocked
+ *    Householder QR inside the factorisations forks a second, internal stream
+ *    from the handle's stream (through an event) and joins it again before the
+ *    call returns, so later work on the handle's stream sees its results.
  *  - A handle is not thread-safe; use one per host thread.
  *  - The library never frees caller memory.  Memory the library needs beyond the
  *    caller's inputs and outputs (index tables, Jacobi scratch, reductions) comes
